@@ -1,0 +1,361 @@
+#!/usr/bin/env python3
+"""Benchmark of the Spectral2D time step on GB300.
+
+Workload (one "step" = one TVD-RK3 step of the hot path): decaying 2-D
+turbulence, N = 2048 (3072^2 collocation grid, 3/2 rule), FP64, nu = 1e-4,
+dt from CFL 0.5 of the seeded initial condition (E(k) ~ k^4 exp(-2(k/10)^2),
+total energy 0.5).  Metric: Mpt*steps/s = N^2 * steps/s / 1e6.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* ``value``: device-resident state, K steps replayed from a CUDA graph, timed
+  with CUDA events on the solver's stream between two synchronisations.
+* ``e2e``: the same metric through the C-ABI drop-in for the reference's
+  IntegrateOneStep with host arrays (s2d_integrate_one_step_host): every step
+  copies wC in from pinned host memory and wC, psiC out.
+* ``roofline``: the dominant kernel's algorithmic bytes per launch (byte model
+  below) over its CUDA-event launch time, against the measured HBM peak; the
+  FP64-ALU view of the same kernel is reported beside it.
+* ``cpu_baseline``: the FP64 CPU restatement of the reference (scipy/pocketfft
+  on all host cores) timed on a bounded sample of the same workload.
+* ``--impl reference``: that CPU restatement as the reference arm (the
+  reference itself, Fortran + FFTW-MPI, cannot be built on these machines).
+
+Multi-GPU: one independent replica per rank (a single run does not shard);
+``value`` is the sum over ranks, time is the max over ranks.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 2048
+NU = 1e-4
+CFL = 0.5
+SEED = 0
+FALLBACK_HBM_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+# byte and flop model of one step (shared with the design notes)
+# ---------------------------------------------------------------------------
+def byte_model(n: int, wbytes: int) -> dict:
+    """Compulsory HBM bytes of the fused two-pass step.
+    I = (N/2+1)*M*w (half-spectral intermediate), S = (N/2+1)*(N+1)*w
+    (compact state).  Per RHS: K1 reads S, writes 3I; K2 reads 3I, writes 2I;
+    K3 reads 2I and 2S (stage input, w^n), writes S.  B_rhs = 10I + 4S."""
+    m = 3 * n // 2
+    I = (n // 2 + 1) * m * wbytes
+    S = (n // 2 + 1) * (n + 1) * wbytes
+    per = {"yinv": S + 3 * I, "xpass": 5 * I, "yfwd": 2 * I + 3 * S}
+    return {"I": I, "S": S, "per_kernel": per, "rhs": 10 * I + 4 * S, "step": 3 * (10 * I + 4 * S)}
+
+
+def flop_model(n: int) -> dict:
+    """benchFFT convention: 2.5*M*log2(M) flops per real 1-D transform of
+    length M, i.e. 2.5*M^2*log2(M) per field per direction of an M x M real
+    2-D FFT.  K1: 3 fields (y), K2: 5 fields (x), K3: 2 fields (y)."""
+    m = 3 * n // 2
+    f = 2.5 * m * m * math.log2(m)
+    return {"yinv": 3 * f, "xpass": 5 * f, "yfwd": 2 * f, "rhs": 10 * f, "step": 30 * f}
+
+
+# ---------------------------------------------------------------------------
+def read_peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        try:
+            with open(p) as f:
+                return json.load(f)
+        except Exception:
+            return {}
+    return {}
+
+
+def hbm_peak(peaks: dict):
+    for k in ("hbm_gbs", "hbm_GBs", "hbm_copy_gbs"):
+        if k in peaks and peaks[k]:
+            return float(peaks[k]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="s2d_clocks_", suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    smax.append(float(c[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max/sum over ranks (torch.distributed, only when N > 1)."""
+
+    def __init__(self, world, local):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch
+            import torch.distributed as dist
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+            self.torch, self.dist = torch, dist
+            self.dev = torch.device("cuda", local)
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def reduce(self, x: float, op: str) -> float:
+        if self.world == 1:
+            return x
+        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=getattr(self.dist.ReduceOp, op))
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float):
+    """Time the oracle (FP64 CPU restatement) on all host cores.  Returns
+    (Mpt*steps/s, timed steps, cores, seconds per step)."""
+    import numpy as np  # noqa: F401
+    import oracle as O
+    cores = O.cpu_count()
+    O.set_workers(cores)
+    g = O.get_grid_size(n, n)
+    w, psi = O.set_turbulent(g, SEED, kind=O.SPECTRUM_K4_GAUSS, k0=10.0, tke_target=0.5)
+    dt = O.cfl_dt(w, g, CFL)
+    for _ in range(warmup):
+        w, psi = O.integrate_one_step(w, psi, g, NU, dt)
+    done, t0 = 0, time.perf_counter()
+    while done < steps:
+        w, psi = O.integrate_one_step(w, psi, g, NU, dt)
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    el = time.perf_counter() - t0
+    return n * n * done / el / 1e6, done, cores, el / done
+
+
+def run_reference(args, rank, world):
+    metric = f"Mpt*steps/s at {args.n}^2 FP64 (RK3 step of the vorticity-streamfunction RHS)"
+    if rank != 0:
+        return 0
+    warm = min(args.warmup, 1)
+    rate, done, cores, sps = cpu_step_rate(args.n, args.steps, warm, budget_s=args.ref_budget)
+    line = {
+        "impl": "reference", "metric": metric, "value": rate, "unit": "Mpt*steps/s",
+        "n_gpus": world, "steps": done, "warmup": warm, "ms_per_step": sps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-phase IC)",
+        "config": workload_config(args.n),
+        "cpu_baseline": {"value": rate, "unit": "Mpt*steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{done} RK3 steps of the {args.n}^2 FP64 workload, "
+                                   f"numpy/scipy.fft restatement of the reference, {cores} threads"},
+        "e2e": {"value": rate, "unit": "Mpt*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(n):
+    return {"workload": f"decaying 2-D turbulence DNS, N={n} (padded {3 * n // 2}^2, 3/2 rule), "
+                        f"FP64, nu={NU}, dt=CFL {CFL}, TVD-RK3",
+            "n": n, "padded": 3 * n // 2, "nu": NU, "cfl": CFL, "seed": SEED,
+            "ic": "E(k)~k^4 exp(-2(k/10)^2), TKE 0.5",
+            "l2": "no flush: per-step working set ~0.3 GB > 126 MB L2",
+            "parallelism": "replicas (one independent run per GPU)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=25.0)
+    ap.add_argument("--ref-budget", type=float, default=150.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    # CPU baseline first (no GPU context yet in this process)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        rate, done, cores, sps = cpu_step_rate(args.n, 1, 0, budget_s=args.cpu_budget)
+        cpu = {"value": rate, "unit": "Mpt*steps/s", "cores": cores, "kind": "port",
+               "sample": f"{done} RK3 step(s) of the {args.n}^2 FP64 workload, numpy/scipy.fft "
+                         f"restatement of the reference on {cores} threads ({sps:.2f} s/step)"}
+
+    import numpy as np
+    from spectral2d_gb300 import Spectral2D, probe_fp64_peak
+
+    D = Dist(world, local)
+    n = args.n
+    s = Spectral2D(n, nu=NU, precision=args.precision, device=local)
+    s.set_turbulent_velocity(seed=SEED + rank, spectrum="k4gauss", k0=10.0, tke=0.5)
+    dt = s.compute_time_step(CFL)
+
+    # warm-up (graph build + first launches)
+    s.integrate_steps(args.warmup, dt)
+    s.synchronize()
+
+    clocks = Clocks(local)
+    D.barrier()
+    clocks.start()
+    ms = s.time_steps(args.steps, dt)          # events on the solver stream, synced both sides
+    clk = clocks.stop()
+    D.barrier()
+    s.check_finite()
+    ms_max = D.reduce(ms, "MAX")
+    value = D.reduce(n * n * args.steps / (ms_max * 1e-3) / 1e6, "SUM")
+    ms_per_step = ms_max / args.steps
+
+    # per-kernel launch times (events between every launch) for the roofline
+    kms_total, kms = s.time_steps(max(3, min(args.steps, 10)), dt, per_kernel=True)
+    ksteps = max(3, min(args.steps, 10))
+    launches_per_kernel = 3 * ksteps
+    wbytes = 16 if args.precision == "fp64" else 8
+    bm = byte_model(n, wbytes)
+    fm = flop_model(n)
+    names = ["yinv", "xpass", "yfwd"]
+    avg = {k: kms[i] / launches_per_kernel for i, k in enumerate(names)}
+    dom = max(names, key=lambda k: avg[k])
+    peaks = read_peaks()
+    hbm, hbm_src = hbm_peak(peaks)
+    achieved = bm["per_kernel"][dom] / (avg[dom] * 1e-3) / 1e9
+    fp64 = probe_fp64_peak(local) if rank == 0 else None
+    alu = fm[dom] / (avg[dom] * 1e-3) / 1e12
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", f"traffic_{dom}_n{n}_{args.precision}.json")
+    if os.path.exists(tp):
+        try:
+            traffic = json.load(open(tp)).get("bytes_per_launch")
+        except Exception:
+            traffic = None
+
+    # e2e through the reference-facing C-ABI with host arrays
+    e2e = None
+    if args.e2e_steps > 0:
+        w_host, _ = s.get_state()
+        s.synchronize()
+        D.barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            w_host, p_host = s.integrate_one_step_host(w_host, dt)
+        t1 = time.perf_counter()
+        el = D.reduce(t1 - t0, "MAX")
+        nbytes = w_host.nbytes
+        e2e = {"value": D.reduce(n * n * args.e2e_steps / el / 1e6, "SUM"), "unit": "Mpt*steps/s",
+               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+               "steps": args.e2e_steps,
+               "path": "s2d_integrate_one_step_host (reference-layout wC in; wC, psiC out)"}
+
+    if rank == 0:
+        line = {
+            "metric": f"Mpt*steps/s at {n}^2 {args.precision.upper()} (RK3 step of the "
+                      "vorticity-streamfunction RHS)",
+            "value": value, "unit": "Mpt*steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "synthetic (seeded random-phase IC)",
+            "config": workload_config(n),
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
+                         "unit": "GB/s", "frac": achieved / hbm,
+                         "peak_source": f"{hbm_src} HBM copy bandwidth",
+                         "traffic": traffic,
+                         "algorithmic_bytes_per_launch": bm["per_kernel"][dom],
+                         "launch_ms": avg[dom],
+                         "fp64_alu": {"achieved_tflops": alu, "peak_tflops": fp64,
+                                      "frac": (alu / fp64) if fp64 else None,
+                                      "peak_source": "measured FP64 FMA loop on this GPU",
+                                      "flops_per_launch": fm[dom]},
+                         "step_hbm_frac": bm["step"] / (ms_per_step * 1e-3) / 1e9 / hbm,
+                         "kernel_ms_per_step": {k: kms[i] / ksteps for i, k in enumerate(names)}},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": s.kernels_per_step() * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    D.close()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,203 @@
+/*
+ * s2d.h -- C-ABI of the GB300 (sm_103a) Spectral2D time-step library.
+ *
+ * Drop-in replacement for the hot path of mpclay/Spectral2D: the
+ * vorticity-streamfunction right-hand side and the TVD (Shu-Osher) RK3 step.
+ * Plain C types only (no C++ or framework types), so Fortran binds it through
+ * ISO_C_BINDING (scalars by VALUE, arrays as assumed-size or TYPE(C_PTR)),
+ * and Python through ctypes.
+ *
+ * Array conventions at the boundary are the reference's:
+ *   - a spectral field is the Fortran array COMPLEX(C_DOUBLE_COMPLEX)
+ *     (cISize, nyG), i.e. interleaved (re, im) doubles with the kx index
+ *     contiguous; cISize = nxG/2+1, nyG = 3*ny/2 (src/Spectral.F90:162-190);
+ *   - row j holds ky = j for j <= nyG/2 and j - nyG above
+ *     (src/Spectral.F90:209-218);
+ *   - forward transforms are normalised by nxG*nyG, inverse transforms are
+ *     not (src/Spectral.F90:749-781).
+ *
+ * Every entry point returns S2D_OK (0) or a negative S2D_ERR_* code and sets a
+ * per-thread message readable with s2d_last_error().  A handle owns all its
+ * device memory and one CUDA stream; it is not thread-safe, separate handles
+ * may be used from separate threads.  Host arrays are borrowed for the
+ * duration of a call only.
+ */
+#ifndef S2D_H
+#define S2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define S2D_API __declspec(dllexport)
+#else
+#define S2D_API __attribute__((visibility("default")))
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define S2D_OK                 0
+#define S2D_ERR_INVALID       -1   /* bad argument, size or null pointer      */
+#define S2D_ERR_CUDA          -2   /* a CUDA runtime call failed              */
+#define S2D_ERR_NONFINITE     -3   /* NaN/Inf detected in the state           */
+#define S2D_ERR_TIMEOUT       -4   /* a bounded device wait gave up           */
+#define S2D_ERR_UNSUPPORTED   -5   /* option the reference leaves unimplemented */
+#define S2D_ERR_NOMEM         -6   /* device or host allocation failed        */
+
+/* ---- dealiasing (values of src/Spectral.F90:41-47) --------------------- */
+#define S2D_NO_DEALIASING      0
+#define S2D_DEALIAS_3_2_RULE   1
+
+/* ---- arithmetic of the FFTs and products ------------------------------- */
+#define S2D_FP64               0   /* the reference's precision (RWPC=C_DOUBLE) */
+#define S2D_FP32               1   /* FP32 FFTs/products; 1/k^2 stays FP64      */
+
+/* ---- initial-condition spectra ----------------------------------------- */
+#define S2D_SPECTRUM_SCHUMANN  0   /* 1.5 urms^2 (k/k0) exp(-k/k0), SetIC.F90:374-381 */
+#define S2D_SPECTRUM_K4_GAUSS  1   /* k^4 exp(-2 (k/k0)^2)                             */
+
+/* Output of GetGridSize (src/Spectral.F90:117-219). */
+typedef struct s2d_grid {
+    int32_t nx, ny, dealias;
+    int32_t nxG, nyG;
+    int32_t kxLG, kyLG, kxMG, kyMG;
+    int32_t kxLU, kyLU, kxMU, kyMU;
+    double  kMax;
+    int32_t rISize, cISize;
+} s2d_grid;
+
+/* Run-time configuration.  The reference fixes these as compile-time
+ * PARAMETERs of the driver (src/Spectral2D.F90:70-127). */
+typedef struct s2d_config {
+    int32_t nx, ny;          /* nominal grid; nx == ny, multiple of 8          */
+    int32_t dealias;         /* S2D_DEALIAS_3_2_RULE (the only working option) */
+    int32_t precision;       /* S2D_FP64 or S2D_FP32                           */
+    double  nu;              /* kinematic viscosity                            */
+    double  alpha;           /* linear drag: dW -= alpha*w (0 = off)           */
+    double  forcing_amp;     /* vorticity source amp*cos(kf*y) (0 = off)       */
+    int32_t forcing_k;       /* kf                                             */
+    int32_t device;          /* CUDA device ordinal                            */
+} s2d_config;
+
+typedef struct s2d_handle s2d_handle;
+
+/* Library version (major*10000 + minor*100 + patch). */
+S2D_API int s2d_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+S2D_API const char* s2d_last_error(void);
+
+/* GetGridSize -- src/Spectral.F90:117-219.  Host only. */
+S2D_API int s2d_get_grid_size(int32_t nx, int32_t ny, int32_t dealias, s2d_grid* out);
+
+/* Set up one simulation: replaces GetGridSize + GetAllocSize + SetupMask +
+ * SetupTruncation + TimeIntegrationSetup + SetupPlans
+ * (src/Spectral2D.F90:263-307; src/Alloc.F90:62-122; src/Spectral.F90:229-353;
+ * src/TimeIntegration.F90:79-108).  The state starts at zero. */
+S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out);
+
+/* Free all device memory of the handle (SpectralFinalize +
+ * TimeIntegrationFinalize, src/Spectral.F90:805-813,
+ * src/TimeIntegration.F90:218-233). */
+S2D_API void s2d_destroy(s2d_handle* h);
+
+/* Load the vorticity wC from a host array in the reference layout
+ * (cISize, nyG) complex128.  Modes outside |k| <= nx/2 are dropped (the
+ * reference truncates them at the end of every step,
+ * src/TimeIntegration.F90:208). psiC is derived from wC
+ * (src/Spectral.F90:508-560) and is not an input. */
+S2D_API int s2d_set_state(s2d_handle* h, const double* wC, int32_t cISize, int32_t nyG);
+
+/* Store wC and psiC (either may be NULL) into host arrays in the reference
+ * layout; every mode outside the retained set is written as zero.  psiC is
+ * ComputePsi + Truncate of wC (src/TimeIntegration.F90:205-209). */
+S2D_API int s2d_get_state(s2d_handle* h, double* wC, double* psiC, int32_t cISize, int32_t nyG);
+
+/* IntegrateOneStep -- src/TimeIntegration.F90:130-210.  Advances the
+ * device-resident state by one TVD-RK3 step of size dt.  Asynchronous on the
+ * handle's stream. */
+S2D_API int s2d_integrate_one_step(s2d_handle* h, double dt);
+
+/* n calls of IntegrateOneStep, replayed from a CUDA graph of one step
+ * (the graph is rebuilt when dt changes).  Asynchronous. */
+S2D_API int s2d_integrate_steps(s2d_handle* h, int32_t n, double dt);
+
+/* IntegrateOneStep with the reference's host arrays, for callers that keep
+ * wC/psiC on the host: wC (in/out) and psiC (out), reference layout.  Copies
+ * in, steps, copies out, synchronises. */
+S2D_API int s2d_integrate_one_step_host(s2d_handle* h, double* wC, double* psiC,
+                                        int32_t cISize, int32_t nyG, double dt);
+
+/* ComputeRHS -- src/Spectral.F90:396-482.  dW of the current state, written
+ * to a host array in the reference layout (zero outside the retained set). */
+S2D_API int s2d_compute_rhs(s2d_handle* h, double* dW, int32_t cISize, int32_t nyG);
+
+/* ComputeSpectrum -- src/Analysis.F90:267-460 (velocity from psi as in
+ * src/Analysis.F90:230-234).  Ek has nbins entries (bin centres 0..nbins-1);
+ * nbins must equal s2d_spectrum_bins().  Any output may be NULL. */
+S2D_API int s2d_spectrum_bins(const s2d_handle* h);
+S2D_API int s2d_spectrum(s2d_handle* h, double* Ek, int32_t nbins,
+                         double* tke, double* eps, double* enstDiss);
+
+/* Mean enstrophy 1/2 <omega^2> of the current state (no reference counterpart). */
+S2D_API int s2d_enstrophy(s2d_handle* h, double* enstrophy);
+
+/* max|wC|, min|wC|, max|psiC|, min|psiC| over the reference array, as the
+ * driver prints every printPeriod steps (src/Spectral2D.F90:358-367). */
+S2D_API int s2d_minmax_abs(s2d_handle* h, double out[4]);
+
+/* SetTaylorGreen -- src/SetIC.F90:70-101 (with the 1-based grid offset of
+ * :91-94).  Sets the device state. */
+S2D_API int s2d_set_taylor_green(s2d_handle* h);
+
+/* SetTurbulentVelocity -- src/SetIC.F90:125-151, :175-364, with a
+ * reproducible counter-based phase per (seed, kx, ky), a Hermitian kx=0
+ * column, and omega scaled so that ComputeSpectrum's TKE equals tke
+ * (no scaling when tke <= 0).  Sets the device state. */
+S2D_API int s2d_set_turbulent(s2d_handle* h, uint64_t seed, int32_t spectrum,
+                              double k0, double urms, double tke);
+
+/* The same generator writing wC into a host array (reference layout);
+ * needs no GPU. */
+S2D_API int s2d_turbulent_ic_host(int32_t nx, uint64_t seed, int32_t spectrum,
+                                  double k0, double urms, double tke, double* wC);
+
+/* CFL time step cfl / max(|u|/dx + |v|/dy) over the nxG x nyG collocation
+ * grid of the current state.  Fills the empty ComputeTimeStep stub
+ * (src/TimeIntegration.F90:213-215).  Synchronises. */
+S2D_API int s2d_cfl_dt(s2d_handle* h, double cfl, double* dt);
+
+/* S2D_ERR_NONFINITE if a NaN/Inf was written to the state since the last
+ * call (flag raised on the device by the stage update); clears the flag. */
+S2D_API int s2d_check_finite(s2d_handle* h);
+
+/* Block until all work queued on the handle's stream has finished. */
+S2D_API int s2d_synchronize(s2d_handle* h);
+
+/* Run n steps and time them with CUDA events on the handle's stream;
+ * *ms receives the elapsed time.  If kernel_ms is non-NULL it receives the
+ * summed device time of each kernel class over the n steps:
+ * [0] inverse y-pass, [1] x-pass with product, [2] forward y-pass with the
+ * stage update. */
+S2D_API int s2d_time_steps(s2d_handle* h, int32_t n, double dt, double* ms,
+                           double* kernel_ms);
+
+/* Kernels launched per RK3 step (for launch accounting). */
+S2D_API int s2d_kernels_per_step(const s2d_handle* h);
+
+/* Page-locked host memory for fast host<->device copies. */
+S2D_API int s2d_host_alloc(size_t bytes, void** ptr);
+S2D_API int s2d_host_free(void* ptr);
+
+/* Measured FP64 throughput of this GPU (a register-resident FMA loop),
+ * in TFLOP/s (2 flops per FMA). */
+S2D_API int s2d_probe_fp64_peak(int32_t device, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* S2D_H */

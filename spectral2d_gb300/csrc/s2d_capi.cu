@@ -1,0 +1,729 @@
+// s2d_capi.cu -- C-ABI of the Spectral2D GB300 library (see include/s2d.h).
+//
+// Host logic: grid setup (GetGridSize, src/Spectral.F90:117-219), FFT plans
+// and twiddle tables, device buffers, launch shapes, the RK3 step
+// (IntegrateOneStep, src/TimeIntegration.F90:130-210) as 9 kernel launches
+// (3 stages x {inverse y-pass, x-pass, forward y-pass + stage update}), its
+// CUDA graph, host I/O in the reference layout, diagnostics and initial
+// conditions.  No framework types cross this boundary.
+#include "s2d.h"
+#include "s2d_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace s2d;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define S2D_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return fail(S2D_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_),   \
+                        __FILE__, __LINE__);                                                    \
+    } while (0)
+
+#define S2D_TRY(call)                   \
+    do {                                \
+        int r_ = (call);                \
+        if (r_ != S2D_OK) return r_;    \
+    } while (0)
+
+// exp(-2 pi i r / M) correctly rounded in practice: octant reduction with
+// exact integer arithmetic, residual angle in [0, pi/4] in long double.
+void twiddle(long long r, long long M, double* c, double* s) {
+    const long double PI_4 = 0.785398163397448309615660845819875721L;
+    r %= M;
+    const long long n8 = 8 * r;
+    const int oct = (int)(n8 / M);
+    const long long rem = n8 - (long long)oct * M;
+    const long double x = ((oct & 1) ? (long double)(M - rem) : (long double)rem) / (long double)M * PI_4;
+    const long double cx = cosl(x), sx = sinl(x);
+    long double C = 0, S = 0;
+    switch (oct) {
+        case 0: C = cx; S = sx; break;
+        case 1: C = sx; S = cx; break;
+        case 2: C = -sx; S = cx; break;
+        case 3: C = -cx; S = sx; break;
+        case 4: C = -cx; S = -sx; break;
+        case 5: C = -sx; S = -cx; break;
+        case 6: C = sx; S = -cx; break;
+        default: C = cx; S = -sx; break;
+    }
+    *c = (double)C;
+    *s = -(double)S;  // forward sign
+}
+
+bool factor_plan(int M, Dims* d) {
+    int m = M, a = 0, b = 0;
+    while (m % 2 == 0) { m /= 2; ++a; }
+    while (m % 3 == 0) { m /= 3; ++b; }
+    if (m != 1 || M % kElemsPerThread != 0) return false;
+    int np = 0;
+    for (int i = 0; i < b; ++i) d->radix[np++] = 3;
+    if (a % 2) d->radix[np++] = 2;
+    for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
+    if (np > kMaxPasses) return false;
+    d->npass = np;
+    return true;
+}
+
+int kIntMaxBins(int kxMG, int kyMG) {
+    const double kMax = std::sqrt((double)(kxMG * kxMG + kyMG * kyMG));
+    const int kIntMax = (int)(kMax + 1.0);
+    return kIntMax + 1;
+}
+
+}  // namespace
+
+struct s2d_handle {
+    s2d_config cfg;
+    s2d_grid grid;
+    Dims d;
+    Phys ph;
+    int prec;            // S2D_FP64 / S2D_FP32
+    size_t vsz;          // bytes of one complex element of the state
+    int device;
+    cudaStream_t stream = nullptr;
+    void* S0 = nullptr;  // w^n
+    void* S1 = nullptr;  // stage vorticity
+    void* Sdw = nullptr; // dW for compute_rhs (lazily allocated)
+    void* Ibase = nullptr;
+    void* I[3] = {nullptr, nullptr, nullptr};
+    size_t Ibytes = 0;
+    double* rk2 = nullptr;
+    void* tw = nullptr;
+    double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
+    size_t ref_bytes = 0;          // bytes of one reference-layout array
+    unsigned int* flags = nullptr;
+    unsigned long long* red64 = nullptr;  // 8 reduction words
+    double* dscratch = nullptr;           // spectrum / partial sums
+    size_t dscratch_n = 0;
+    Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    double graph_dt = 0.0;
+    int max_smem = 0;
+};
+
+namespace {
+
+int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_group, int target_threads,
+                Launch* L, const char* what) {
+    const size_t cap_pair = (size_t)h->max_smem / 2;
+    if (bytes_per_group > (size_t)h->max_smem)
+        return fail(S2D_ERR_UNSUPPORTED, "%s: %zu bytes of shared memory per transform exceed %d", what,
+                    bytes_per_group, h->max_smem);
+    if (threads_per_group > 512)
+        return fail(S2D_ERR_UNSUPPORTED, "%s: %d threads per transform exceed 512", what, threads_per_group);
+    int G = std::max(1, target_threads / threads_per_group);
+    while (G > 1 && (G * threads_per_group > 512 || G * bytes_per_group > cap_pair)) --G;
+    L->G = G;
+    L->threads = G * threads_per_group;
+    L->smem = G * bytes_per_group;
+    L->blocks = 0;
+    return S2D_OK;
+}
+
+template <typename T>
+int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
+    const Dims& d = h->d;
+    FieldSet fs{};
+    fs.nf = 3;
+    fs.op[0] = OP_U;
+    fs.op[1] = OP_V;
+    fs.op[2] = OP_W;
+    fs.out[0] = h->I[0];
+    fs.out[1] = h->I[1];
+    fs.out[2] = h->I[2];
+    const void* win = (stage <= 1) ? h->S0 : h->S1;
+    if (ev) S2D_CUDA(cudaEventRecord(ev[0], h->stream));
+    S2D_CUDA(Kern<T>::yinv(d, win, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    if (ev) S2D_CUDA(cudaEventRecord(ev[1], h->stream));
+    S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
+    if (ev) S2D_CUDA(cudaEventRecord(ev[2], h->stream));
+    S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, stage, dt, h->ph, h->tw, h->flags,
+                               h->stream, h->L_yfwd));
+    if (ev) S2D_CUDA(cudaEventRecord(ev[3], h->stream));
+    return S2D_OK;
+}
+
+int launch_rhs_stage_any(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
+    return h->prec == S2D_FP64 ? launch_rhs_stage<double>(h, stage, dt, ev)
+                               : launch_rhs_stage<float>(h, stage, dt, ev);
+}
+
+int launch_step(s2d_handle* h, double dt) {
+    for (int s = 1; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr));
+    return S2D_OK;
+}
+
+int check_ref_dims(const s2d_handle* h, int cISize, int nyG) {
+    if (cISize != h->grid.cISize || nyG != h->grid.nyG)
+        return fail(S2D_ERR_INVALID, "array shape (%d,%d) does not match (cISize,nyG)=(%d,%d)", cISize, nyG,
+                    h->grid.cISize, h->grid.nyG);
+    return S2D_OK;
+}
+
+int ensure_ref_stage(s2d_handle* h) {
+    if (h->ref_stage) return S2D_OK;
+    S2D_CUDA(cudaMalloc(&h->ref_stage, 2 * h->ref_bytes));
+    return S2D_OK;
+}
+
+int upload_ref(s2d_handle* h, const double* wC) {
+    S2D_TRY(ensure_ref_stage(h));
+    S2D_CUDA(cudaMemcpyAsync(h->ref_stage, wC, h->ref_bytes, cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == S2D_FP64)
+        S2D_CUDA(Kern<double>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
+    else
+        S2D_CUDA(Kern<float>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
+    return S2D_OK;
+}
+
+int download_ref(s2d_handle* h, const void* S, double* wC, double* psiC) {
+    if (!wC && !psiC) return S2D_OK;
+    S2D_TRY(ensure_ref_stage(h));
+    double* dW = h->ref_stage;
+    double* dP = (double*)((char*)h->ref_stage + h->ref_bytes);
+    if (h->prec == S2D_FP64)
+        S2D_CUDA(Kern<double>::compact_to_ref(h->d, S, h->grid.cISize, wC ? dW : nullptr, psiC ? dP : nullptr,
+                                              h->stream));
+    else
+        S2D_CUDA(Kern<float>::compact_to_ref(h->d, S, h->grid.cISize, wC ? dW : nullptr, psiC ? dP : nullptr,
+                                             h->stream));
+    if (wC) S2D_CUDA(cudaMemcpyAsync(wC, dW, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (psiC) S2D_CUDA(cudaMemcpyAsync(psiC, dP, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    return S2D_OK;
+}
+
+void drop_graph(s2d_handle* h) {
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->graph) cudaGraphDestroy(h->graph);
+    h->gexec = nullptr;
+    h->graph = nullptr;
+}
+
+int build_graph(s2d_handle* h, double dt) {
+    drop_graph(h);
+    S2D_CUDA(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int r = launch_step(h, dt);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (r != S2D_OK) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+    }
+    if (e != cudaSuccess) return fail(S2D_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+    h->graph = g;
+    S2D_CUDA(cudaGraphInstantiate(&h->gexec, g, 0));
+    h->graph_dt = dt;
+    return S2D_OK;
+}
+
+// Spectrum -> (Ek, tke, eps, enstDiss) as ComputeSpectrum (src/Analysis.F90:414-448).
+int spectrum_impl(s2d_handle* h, std::vector<double>& Ek) {
+    const int nb = kIntMaxBins(h->grid.kxMG, h->grid.kyMG);
+    Ek.assign(nb, 0.0);
+    const int nk = h->d.K + 1;
+    if (h->prec == S2D_FP64) S2D_CUDA(Kern<double>::spectrum(h->d, h->S0, h->dscratch, h->stream));
+    else S2D_CUDA(Kern<float>::spectrum(h->d, h->S0, h->dscratch, h->stream));
+    S2D_CUDA(cudaMemcpyAsync(Ek.data(), h->dscratch, sizeof(double) * std::min(nk, nb), cudaMemcpyDeviceToHost,
+                             h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    return S2D_OK;
+}
+
+}  // namespace
+
+int s2d::handle_nx(const s2d_handle* h) { return h->cfg.nx; }
+
+// ============================================================================
+// C-ABI
+// ============================================================================
+
+extern "C" {
+
+S2D_API int s2d_version(void) { return 100; }
+
+S2D_API const char* s2d_last_error(void) { return g_err.c_str(); }
+
+S2D_API int s2d_get_grid_size(int32_t nx, int32_t ny, int32_t dealias, s2d_grid* o) {
+    if (!o) return fail(S2D_ERR_INVALID, "null output");
+    if (nx <= 0 || ny <= 0) return fail(S2D_ERR_INVALID, "nx, ny must be positive");
+    std::memset(o, 0, sizeof(*o));
+    o->nx = nx;
+    o->ny = ny;
+    o->dealias = dealias;
+    if (dealias == S2D_NO_DEALIASING) {
+        o->nxG = nx;
+        o->nyG = ny;
+    } else if (dealias == S2D_DEALIAS_3_2_RULE) {
+        o->nxG = 3 * nx / 2;
+        o->nyG = 3 * ny / 2;
+    } else {
+        return fail(S2D_ERR_UNSUPPORTED, "dealias=%d is an empty case in the reference", dealias);
+    }
+    o->kxLG = 0;
+    o->kyLG = -o->nyG / 2 + 1;
+    o->kxMG = o->nxG / 2;
+    o->kyMG = o->nyG / 2;
+    o->kxLU = 0;
+    o->kyLU = -ny / 2 + 1;
+    o->kxMU = nx / 2;
+    o->kyMU = ny / 2;
+    o->kMax = (double)o->kxMU;
+    o->rISize = 2 * (o->nxG / 2 + 1);
+    o->cISize = o->nxG / 2 + 1;
+    return S2D_OK;
+}
+
+S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
+    if (!cfg || !out) return fail(S2D_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (cfg->dealias != S2D_DEALIAS_3_2_RULE)
+        return fail(S2D_ERR_UNSUPPORTED,
+                    "only the 3/2 rule is supported (without dealiasing the reference truncation is "
+                    "undefined on the ky=0 row)");
+    if (cfg->nx != cfg->ny) return fail(S2D_ERR_UNSUPPORTED, "nx must equal ny");
+    if (cfg->nx < 8 || cfg->nx % 8 != 0) return fail(S2D_ERR_INVALID, "nx must be a positive multiple of 8");
+    if (cfg->precision != S2D_FP64 && cfg->precision != S2D_FP32)
+        return fail(S2D_ERR_INVALID, "precision must be S2D_FP64 or S2D_FP32");
+    if (!(cfg->nu >= 0.0) || !std::isfinite(cfg->nu)) return fail(S2D_ERR_INVALID, "nu must be finite, >= 0");
+
+    s2d_handle* h = new (std::nothrow) s2d_handle();
+    if (!h) return fail(S2D_ERR_NOMEM, "host allocation failed");
+    h->cfg = *cfg;
+    h->prec = cfg->precision;
+    h->vsz = h->prec == S2D_FP64 ? sizeof(double2) : sizeof(float2);
+    h->device = cfg->device;
+    int r = s2d_get_grid_size(cfg->nx, cfg->ny, cfg->dealias, &h->grid);
+    if (r != S2D_OK) {
+        delete h;
+        return r;
+    }
+    Dims& d = h->d;
+    d.K = cfg->nx / 2;
+    d.KX = d.K + 1;
+    d.KY = 2 * d.K + 1;
+    d.M = h->grid.nxG;
+    d.ldS = d.KY + 1;                  // even pitch: 16-byte aligned FP32 columns
+    d.ldI = (d.KX + 3) / 4 * 4;
+    if (!factor_plan(d.M, &d)) {
+        delete h;
+        return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", d.M);
+    }
+    d.Tg = d.M / kElemsPerThread;
+    h->ph.nu = cfg->nu;
+    h->ph.alpha = cfg->alpha;
+    h->ph.fk = cfg->forcing_amp != 0.0 ? cfg->forcing_k : 0;
+    if (h->ph.fk < 0 || h->ph.fk > d.K) {
+        delete h;
+        return fail(S2D_ERR_INVALID, "forcing wavenumber %d outside [0, %d]", cfg->forcing_k, d.K);
+    }
+    {
+        // amp cos(kf y) on the 1-based grid y_j = 2 pi j / nyG: coefficient
+        // amp/2 exp(i kf dy) at ky = +kf (and the conjugate at -kf).
+        const double dy = 2.0 * M_PI / (double)d.M;
+        h->ph.f_re = 0.5 * cfg->forcing_amp * std::cos(h->ph.fk * dy);
+        h->ph.f_im = 0.5 * cfg->forcing_amp * std::sin(h->ph.fk * dy);
+    }
+
+    auto bail = [&](int code) {
+        s2d_destroy(h);
+        return code;
+    };
+    if (cudaSetDevice(h->device) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "cudaSetDevice(%d) failed", h->device));
+    cudaDeviceProp prop{};
+    if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess)
+        return bail(fail(S2D_ERR_CUDA, "cudaGetDeviceProperties failed"));
+    h->max_smem = (int)prop.sharedMemPerBlockOptin - 1024;
+    {
+        static bool configured[64] = {false};
+        if (h->device >= 0 && h->device < 64 && !configured[h->device]) {
+            if (configure_kernels(h->max_smem) != cudaSuccess)
+                return bail(fail(S2D_ERR_CUDA, "cudaFuncSetAttribute failed"));
+            configured[h->device] = true;
+        }
+    }
+    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(S2D_ERR_CUDA, "stream creation failed"));
+
+    const size_t state_bytes = (size_t)d.KX * d.ldS * h->vsz;
+    h->Ibytes = (size_t)d.M * d.ldI * h->vsz;
+#define S2D_ALLOC(p, n)                                                                                   \
+    if (cudaMalloc((void**)&(p), (n)) != cudaSuccess)                                                    \
+        return bail(fail(S2D_ERR_NOMEM, "cudaMalloc of %zu bytes failed", (size_t)(n)));                 \
+    cudaMemsetAsync((p), 0, (n), h->stream);
+    S2D_ALLOC(h->S0, state_bytes);
+    S2D_ALLOC(h->S1, state_bytes);
+    S2D_ALLOC(h->Ibase, 3 * h->Ibytes);
+    h->I[0] = h->Ibase;
+    h->I[1] = (char*)h->Ibase + h->Ibytes;
+    h->I[2] = (char*)h->Ibase + 2 * h->Ibytes;
+    S2D_ALLOC(h->rk2, (size_t)d.KX * d.ldS * sizeof(double));
+    S2D_ALLOC(h->tw, (size_t)d.M * h->vsz);
+    S2D_ALLOC(h->flags, 64);
+    S2D_ALLOC(h->red64, 8 * sizeof(unsigned long long));
+    h->dscratch_n = std::max<size_t>(d.K + 1, 4096);
+    S2D_ALLOC(h->dscratch, h->dscratch_n * sizeof(double));
+#undef S2D_ALLOC
+    h->ref_bytes = (size_t)h->grid.cISize * h->grid.nyG * 2 * sizeof(double);
+
+    // twiddles exp(-2 pi i t / M)
+    {
+        std::vector<double> twd(2 * (size_t)d.M);
+        for (int t = 0; t < d.M; ++t) twiddle(t, d.M, &twd[2 * t], &twd[2 * t + 1]);
+        if (h->prec == S2D_FP64) {
+            if (cudaMemcpy(h->tw, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+                return bail(fail(S2D_ERR_CUDA, "twiddle upload failed"));
+        } else {
+            std::vector<float> twf(twd.begin(), twd.end());
+            if (cudaMemcpy(h->tw, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+                return bail(fail(S2D_ERR_CUDA, "twiddle upload failed"));
+        }
+    }
+    if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess)
+        return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
+
+    // launch shapes
+    const size_t tb = (size_t)d.M * h->vsz;
+    int rr;
+    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_yinv, "inverse y-pass")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, 2 * tb, 512, &h->L_xpass, "x-pass")) != S2D_OK) return bail(rr);
+    {
+        // forward y-pass: G columns x 2 fields; up to two transforms at a time
+        Launch L{};
+        if ((rr = pick_launch(h, d.Tg, 2 * tb, 512, &L, "forward y-pass")) != S2D_OK) return bail(rr);
+        const int conc = std::max(1, std::min(2 * L.G, 512 / d.Tg));
+        int c = conc;
+        while ((2 * L.G) % c) --c;
+        L.threads = c * d.Tg;
+        h->L_yfwd = L;
+    }
+    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
+
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
+    *out = h;
+    return S2D_OK;
+}
+
+S2D_API void s2d_destroy(s2d_handle* h) {
+    if (!h) return;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    drop_graph(h);
+    void* ptrs[] = {h->S0, h->S1, h->Sdw, h->Ibase, h->rk2, h->tw, h->ref_stage, h->flags, h->red64, h->dscratch};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+}
+
+S2D_API int s2d_set_state(s2d_handle* h, const double* wC, int32_t cISize, int32_t nyG) {
+    if (!h || !wC) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_TRY(check_ref_dims(h, cISize, nyG));
+    S2D_CUDA(cudaSetDevice(h->device));
+    S2D_TRY(upload_ref(h, wC));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    return S2D_OK;
+}
+
+S2D_API int s2d_get_state(s2d_handle* h, double* wC, double* psiC, int32_t cISize, int32_t nyG) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    S2D_TRY(check_ref_dims(h, cISize, nyG));
+    S2D_CUDA(cudaSetDevice(h->device));
+    return download_ref(h, h->S0, wC, psiC);
+}
+
+S2D_API int s2d_integrate_one_step(s2d_handle* h, double dt) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    if (!std::isfinite(dt)) return fail(S2D_ERR_INVALID, "dt must be finite");
+    S2D_CUDA(cudaSetDevice(h->device));
+    return launch_step(h, dt);
+}
+
+S2D_API int s2d_integrate_steps(s2d_handle* h, int32_t n, double dt) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    if (n < 0 || !std::isfinite(dt)) return fail(S2D_ERR_INVALID, "bad step count or dt");
+    S2D_CUDA(cudaSetDevice(h->device));
+    if (n == 0) return S2D_OK;
+    if (!h->gexec || h->graph_dt != dt) S2D_TRY(build_graph(h, dt));
+    for (int i = 0; i < n; ++i) S2D_CUDA(cudaGraphLaunch(h->gexec, h->stream));
+    return S2D_OK;
+}
+
+S2D_API int s2d_integrate_one_step_host(s2d_handle* h, double* wC, double* psiC, int32_t cISize, int32_t nyG,
+                                        double dt) {
+    if (!h || !wC) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_TRY(check_ref_dims(h, cISize, nyG));
+    S2D_CUDA(cudaSetDevice(h->device));
+    S2D_TRY(upload_ref(h, wC));
+    S2D_TRY(launch_step(h, dt));
+    return download_ref(h, h->S0, wC, psiC);
+}
+
+S2D_API int s2d_compute_rhs(s2d_handle* h, double* dW, int32_t cISize, int32_t nyG) {
+    if (!h || !dW) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_TRY(check_ref_dims(h, cISize, nyG));
+    S2D_CUDA(cudaSetDevice(h->device));
+    if (!h->Sdw) S2D_CUDA(cudaMalloc(&h->Sdw, (size_t)h->d.KX * h->d.ldS * h->vsz));
+    S2D_TRY(launch_rhs_stage_any(h, 0, 0.0, nullptr));
+    return download_ref(h, h->Sdw, dW, nullptr);
+}
+
+S2D_API int s2d_spectrum_bins(const s2d_handle* h) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    return kIntMaxBins(h->grid.kxMG, h->grid.kyMG);
+}
+
+S2D_API int s2d_spectrum(s2d_handle* h, double* Ek, int32_t nbins, double* tke, double* eps, double* enstDiss) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    const int nb = kIntMaxBins(h->grid.kxMG, h->grid.kyMG);
+    if (Ek && nbins != nb) return fail(S2D_ERR_INVALID, "nbins=%d, expected %d", nbins, nb);
+    S2D_CUDA(cudaSetDevice(h->device));
+    std::vector<double> E;
+    S2D_TRY(spectrum_impl(h, E));
+    // src/Analysis.F90:414-448 (dk = 1): sums over bins in order
+    double t = 0.0, e = 0.0, z = 0.0;
+    for (int i = 0; i < nb; ++i) {
+        const double k = (double)i;
+        t = t + E[i] * 1.0;
+        e = e + k * k * E[i] * 1.0;
+        z = z + (k * k) * (k * k) * E[i] * 1.0;
+    }
+    if (Ek) std::memcpy(Ek, E.data(), sizeof(double) * nb);
+    if (tke) *tke = t;
+    if (eps) *eps = 2.0 * h->cfg.nu * e;
+    if (enstDiss) *enstDiss = 2.0 * h->cfg.nu * z;
+    return S2D_OK;
+}
+
+S2D_API int s2d_enstrophy(s2d_handle* h, double* out) {
+    if (!h || !out) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_CUDA(cudaSetDevice(h->device));
+    const int nblk = 304;
+    if (h->prec == S2D_FP64) S2D_CUDA(Kern<double>::enstrophy_partial(h->d, h->S0, h->dscratch, nblk, h->stream));
+    else S2D_CUDA(Kern<float>::enstrophy_partial(h->d, h->S0, h->dscratch, nblk, h->stream));
+    std::vector<double> part(nblk);
+    S2D_CUDA(cudaMemcpyAsync(part.data(), h->dscratch, sizeof(double) * nblk, cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    double s = 0.0;
+    for (double p : part) s += p;
+    *out = 0.5 * s;
+    return S2D_OK;
+}
+
+S2D_API int s2d_minmax_abs(s2d_handle* h, double out[4]) {
+    if (!h || !out) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_CUDA(cudaSetDevice(h->device));
+    unsigned long long init[4];
+    const double big = 1.0e308;
+    init[0] = 0ULL;
+    std::memcpy(&init[1], &big, 8);
+    init[2] = 0ULL;
+    std::memcpy(&init[3], &big, 8);
+    S2D_CUDA(cudaMemcpyAsync(h->red64, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    if (h->prec == S2D_FP64) S2D_CUDA(Kern<double>::minmax(h->d, h->S0, h->red64, h->stream));
+    else S2D_CUDA(Kern<float>::minmax(h->d, h->S0, h->red64, h->stream));
+    unsigned long long res[4];
+    S2D_CUDA(cudaMemcpyAsync(res, h->red64, sizeof(res), cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    for (int i = 0; i < 4; ++i) std::memcpy(&out[i], &res[i], 8);
+    // the reference array also stores the zero-padded modes beyond the
+    // retained rectangle, so its minimum magnitude is zero
+    out[1] = 0.0;
+    out[3] = 0.0;
+    return S2D_OK;
+}
+
+S2D_API int s2d_set_taylor_green(s2d_handle* h) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    S2D_CUDA(cudaSetDevice(h->device));
+    const int M = h->d.M;
+    // SIN(2 PI i / nxG) for 1-based i (src/SetIC.F90:91-94), FP64 libm
+    std::vector<double> s(M);
+    for (int i = 0; i < M; ++i) s[i] = std::sin(2.0 * M_PI * (double)(i + 1) / (double)M);
+    double* ds = nullptr;
+    S2D_CUDA(cudaMalloc(&ds, sizeof(double) * M));
+    cudaError_t e = cudaMemcpyAsync(ds, s.data(), sizeof(double) * M, cudaMemcpyHostToDevice, h->stream);
+    // physical omega in I[0..1] (M*M reals fit in 2 intermediates), its
+    // x-spectrum in I[2], then the y-transform into S0
+    if (e == cudaSuccess) {
+        if (h->prec == S2D_FP64) {
+            e = Kern<double>::fill_tg(h->d, ds, ds, h->I[0], h->stream);
+            if (e == cudaSuccess) e = Kern<double>::xfwd_phys(h->d, h->I[0], h->I[2], h->tw, h->stream, h->L_xrow);
+            if (e == cudaSuccess) e = Kern<double>::yfwd_store(h->d, h->I[2], h->S0, h->tw, h->stream, h->L_ystore);
+        } else {
+            e = Kern<float>::fill_tg(h->d, ds, ds, h->I[0], h->stream);
+            if (e == cudaSuccess) e = Kern<float>::xfwd_phys(h->d, h->I[0], h->I[2], h->tw, h->stream, h->L_xrow);
+            if (e == cudaSuccess) e = Kern<float>::yfwd_store(h->d, h->I[2], h->S0, h->tw, h->stream, h->L_ystore);
+        }
+    }
+    cudaError_t e2 = cudaStreamSynchronize(h->stream);
+    cudaFree(ds);
+    if (e != cudaSuccess) return fail(S2D_ERR_CUDA, "Taylor-Green setup failed: %s", cudaGetErrorString(e));
+    if (e2 != cudaSuccess) return fail(S2D_ERR_CUDA, "Taylor-Green setup failed: %s", cudaGetErrorString(e2));
+    return S2D_OK;
+}
+
+S2D_API int s2d_cfl_dt(s2d_handle* h, double cfl, double* dt) {
+    if (!h || !dt) return fail(S2D_ERR_INVALID, "null argument");
+    if (!(cfl > 0.0)) return fail(S2D_ERR_INVALID, "cfl must be positive");
+    S2D_CUDA(cudaSetDevice(h->device));
+    FieldSet fs{};
+    fs.nf = 2;
+    fs.op[0] = OP_U;
+    fs.op[1] = OP_V;
+    fs.out[0] = h->I[0];
+    fs.out[1] = h->I[1];
+    S2D_CUDA(cudaMemsetAsync(h->red64, 0, sizeof(unsigned long long), h->stream));
+    if (h->prec == S2D_FP64) {
+        S2D_CUDA(Kern<double>::yinv(h->d, h->S0, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+        S2D_CUDA(Kern<double>::xinv_cfl(h->d, h->I[0], h->I[1], h->tw, h->red64, h->stream, h->L_xrow));
+    } else {
+        S2D_CUDA(Kern<float>::yinv(h->d, h->S0, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+        S2D_CUDA(Kern<float>::xinv_cfl(h->d, h->I[0], h->I[1], h->tw, h->red64, h->stream, h->L_xrow));
+    }
+    unsigned long long bits = 0;
+    S2D_CUDA(cudaMemcpyAsync(&bits, h->red64, 8, cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    double m;
+    std::memcpy(&m, &bits, 8);
+    if (!(m > 0.0) || !std::isfinite(m)) return fail(S2D_ERR_NONFINITE, "max(|u|/dx+|v|/dy) = %g", m);
+    *dt = cfl / m;
+    return S2D_OK;
+}
+
+S2D_API int s2d_check_finite(s2d_handle* h) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    S2D_CUDA(cudaSetDevice(h->device));
+    unsigned int f = 0;
+    S2D_CUDA(cudaMemcpyAsync(&f, h->flags, sizeof(f), cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(f), h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    if (f & 1u) return fail(S2D_ERR_NONFINITE, "non-finite vorticity written by a stage update");
+    return S2D_OK;
+}
+
+S2D_API int s2d_synchronize(s2d_handle* h) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    S2D_CUDA(cudaSetDevice(h->device));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    return S2D_OK;
+}
+
+S2D_API int s2d_time_steps(s2d_handle* h, int32_t n, double dt, double* ms, double* kernel_ms) {
+    if (!h || !ms || n <= 0) return fail(S2D_ERR_INVALID, "bad argument");
+    S2D_CUDA(cudaSetDevice(h->device));
+    cudaEvent_t e0, e1;
+    S2D_CUDA(cudaEventCreate(&e0));
+    S2D_CUDA(cudaEventCreate(&e1));
+    int r = S2D_OK;
+    if (!kernel_ms) {
+        if (!h->gexec || h->graph_dt != dt) r = build_graph(h, dt);
+        if (r == S2D_OK) {
+            S2D_CUDA(cudaStreamSynchronize(h->stream));
+            S2D_CUDA(cudaEventRecord(e0, h->stream));
+            for (int i = 0; i < n && r == S2D_OK; ++i)
+                if (cudaGraphLaunch(h->gexec, h->stream) != cudaSuccess) r = fail(S2D_ERR_CUDA, "graph launch failed");
+            S2D_CUDA(cudaEventRecord(e1, h->stream));
+        }
+    } else {
+        const int nev = 3 * 4 * n;
+        std::vector<cudaEvent_t> ev(nev);
+        for (auto& e : ev) S2D_CUDA(cudaEventCreate(&e));
+        S2D_CUDA(cudaStreamSynchronize(h->stream));
+        S2D_CUDA(cudaEventRecord(e0, h->stream));
+        for (int i = 0; i < n && r == S2D_OK; ++i)
+            for (int s = 1; s <= 3 && r == S2D_OK; ++s) r = launch_rhs_stage_any(h, s, dt, &ev[(i * 3 + s - 1) * 4]);
+        S2D_CUDA(cudaEventRecord(e1, h->stream));
+        S2D_CUDA(cudaEventSynchronize(e1));
+        kernel_ms[0] = kernel_ms[1] = kernel_ms[2] = 0.0;
+        if (r == S2D_OK)
+            for (int q = 0; q < 3 * n; ++q)
+                for (int k = 0; k < 3; ++k) {
+                    float t = 0.f;
+                    cudaEventElapsedTime(&t, ev[q * 4 + k], ev[q * 4 + k + 1]);
+                    kernel_ms[k] += t;
+                }
+        for (auto& e : ev) cudaEventDestroy(e);
+    }
+    S2D_CUDA(cudaEventSynchronize(e1));
+    float t = 0.f;
+    S2D_CUDA(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return r;
+}
+
+S2D_API int s2d_kernels_per_step(const s2d_handle* h) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    return 9;
+}
+
+S2D_API int s2d_host_alloc(size_t bytes, void** ptr) {
+    if (!ptr) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_CUDA(cudaMallocHost(ptr, bytes));
+    return S2D_OK;
+}
+
+S2D_API int s2d_host_free(void* ptr) {
+    if (ptr) S2D_CUDA(cudaFreeHost(ptr));
+    return S2D_OK;
+}
+
+S2D_API int s2d_probe_fp64_peak(int32_t device, double* tflops) {
+    if (!tflops) return fail(S2D_ERR_INVALID, "null argument");
+    S2D_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop{};
+    S2D_CUDA(cudaGetDeviceProperties(&prop, device));
+    double* sink = nullptr;
+    S2D_CUDA(cudaMalloc(&sink, 1024 * sizeof(double)));
+    cudaStream_t st;
+    S2D_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    const int threads = 256, blocks = prop.multiProcessorCount * 8, iters = 4096;
+    cudaEvent_t e0, e1;
+    S2D_CUDA(cudaEventCreate(&e0));
+    S2D_CUDA(cudaEventCreate(&e1));
+    S2D_CUDA(launch_fp64_probe(sink, blocks, threads, iters, st));  // warm-up
+    S2D_CUDA(cudaEventRecord(e0, st));
+    const int reps = 5;
+    for (int i = 0; i < reps; ++i) S2D_CUDA(launch_fp64_probe(sink, blocks, threads, iters, st));
+    S2D_CUDA(cudaEventRecord(e1, st));
+    S2D_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    S2D_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    const double flops = 2.0 * 8.0 * iters * (double)threads * blocks * reps;
+    *tflops = flops / (ms * 1e-3) / 1e12;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    cudaFree(sink);
+    return S2D_OK;
+}
+
+}  // extern "C"

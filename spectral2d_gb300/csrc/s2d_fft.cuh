@@ -1,0 +1,169 @@
+// s2d_fft.cuh -- block-level mixed-radix (2, 3, 4) Stockham FFT in shared memory.
+//
+// One transform of length M is owned by Tg = M/12 consecutive threads; a CTA
+// runs several transforms of the same length side by side.  Each pass with
+// radix R is the self-sorting Stockham step (Govindaraju et al., SC'08):
+// butterfly j (0 <= j < M/R) reads x[j + r*M/R], multiplies by the twiddle
+// w^(r*(j mod Ns)*M/(Ns*R)) with w = exp(-2 pi i/M), does a radix-R DFT and
+// writes x[(j/Ns)*Ns*R + j mod Ns + r*Ns], Ns being the product of the
+// earlier radices.  The pass is done in place: every thread first loads all
+// 12 of its elements into registers, the CTA synchronises, then every thread
+// writes its results.
+//
+// FP64 on GB300 has a small fraction of the FP32 issue rate, so the code is
+// written to minimise FP64 instructions: twiddles come from a table (a load,
+// not a sincos), complex twiddle products are 2 MUL + 2 FMA, and the radix-3
+// and radix-4 butterflies use only additions and FMAs.
+#pragma once
+
+#include "s2d_internal.h"
+
+namespace s2d {
+
+template <typename T>
+struct Vec;
+template <>
+struct Vec<double> {
+    using t = double2;
+};
+template <>
+struct Vec<float> {
+    using t = float2;
+};
+
+template <typename VT, typename T>
+__device__ __forceinline__ VT mk(T x, T y) {
+    VT r;
+    r.x = x;
+    r.y = y;
+    return r;
+}
+
+// a * w (forward) or a * conj(w) (inverse)
+template <bool INV, typename VT>
+__device__ __forceinline__ VT twmul(VT a, VT w) {
+    VT r;
+    if (!INV) {
+        r.x = a.x * w.x - a.y * w.y;
+        r.y = a.x * w.y + a.y * w.x;
+    } else {
+        r.x = a.x * w.x + a.y * w.y;
+        r.y = a.y * w.x - a.x * w.y;
+    }
+    return r;
+}
+
+template <bool INV, typename VT>
+__device__ __forceinline__ void bf2(VT* v) {
+    VT a = v[0], b = v[1];
+    v[0].x = a.x + b.x;
+    v[0].y = a.y + b.y;
+    v[1].x = a.x - b.x;
+    v[1].y = a.y - b.y;
+}
+
+// Radix-3 DFT: y1 = a - (b+c)/2 -/+ i sin(2pi/3) (b-c) (forward/inverse).
+template <bool INV, typename VT>
+__device__ __forceinline__ void bf3(VT* v) {
+    using T = decltype(v[0].x);
+    const T s = (T)0.86602540378443864676;
+    const T h = (T)0.5;
+    VT a = v[0], b = v[1], c = v[2];
+    T t1x = b.x + c.x, t1y = b.y + c.y;
+    T t2x = b.x - c.x, t2y = b.y - c.y;
+    T mx = a.x - h * t1x, my = a.y - h * t1y;
+    v[0].x = a.x + t1x;
+    v[0].y = a.y + t1y;
+    if (!INV) {
+        v[1].x = mx + s * t2y;
+        v[1].y = my - s * t2x;
+        v[2].x = mx - s * t2y;
+        v[2].y = my + s * t2x;
+    } else {
+        v[1].x = mx - s * t2y;
+        v[1].y = my + s * t2x;
+        v[2].x = mx + s * t2y;
+        v[2].y = my - s * t2x;
+    }
+}
+
+template <bool INV, typename VT>
+__device__ __forceinline__ void bf4(VT* v) {
+    VT a = v[0], b = v[1], c = v[2], d = v[3];
+    auto t0x = a.x + c.x, t0y = a.y + c.y;
+    auto t1x = a.x - c.x, t1y = a.y - c.y;
+    auto t2x = b.x + d.x, t2y = b.y + d.y;
+    auto t3x = b.x - d.x, t3y = b.y - d.y;
+    v[0].x = t0x + t2x;
+    v[0].y = t0y + t2y;
+    v[2].x = t0x - t2x;
+    v[2].y = t0y - t2y;
+    if (!INV) {  // y1 = t1 - i t3, y3 = t1 + i t3
+        v[1].x = t1x + t3y;
+        v[1].y = t1y - t3x;
+        v[3].x = t1x - t3y;
+        v[3].y = t1y + t3x;
+    } else {
+        v[1].x = t1x - t3y;
+        v[1].y = t1y + t3x;
+        v[3].x = t1x + t3y;
+        v[3].y = t1y - t3x;
+    }
+}
+
+template <int R, bool INV, typename VT>
+__device__ __forceinline__ void butterfly(VT* v) {
+    if constexpr (R == 2) bf2<INV>(v);
+    else if constexpr (R == 3) bf3<INV>(v);
+    else bf4<INV>(v);
+}
+
+// One in-place Stockham pass of radix R over the transform in buf.
+template <int R, bool INV, typename VT>
+__device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int Tg,
+                                         const VT* __restrict__ tw) {
+    constexpr int NB = kElemsPerThread / R;
+    VT v[NB][R];
+    const int stride = M / R;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = lane + b * Tg;
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[b][r] = buf[j + r * stride];
+    }
+    __syncthreads();
+    const int tstep = M / (Ns * R);
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = lane + b * Tg;
+        const int k = j % Ns;
+        if (Ns > 1) {
+            const int ts = k * tstep;
+#pragma unroll
+            for (int r = 1; r < R; ++r) v[b][r] = twmul<INV>(v[b][r], __ldg(&tw[r * ts]));
+        }
+        butterfly<R, INV>(v[b]);
+        const int base = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[base + r * Ns] = v[b][r];
+    }
+    __syncthreads();
+}
+
+// Full transform: unnormalised, sign -1 (forward) or +1 (INV).  Every thread
+// of the CTA must call it (it synchronises the CTA); starts with a barrier so
+// that callers may fill buf just before.
+template <bool INV, typename VT>
+__device__ __forceinline__ void fft_run(VT* buf, const Dims& d, int lane, const VT* __restrict__ tw) {
+    __syncthreads();
+    int Ns = 1;
+    for (int p = 0; p < d.npass; ++p) {
+        const int R = d.radix[p];
+        if (R == 4) fft_pass<4, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+        else if (R == 3) fft_pass<3, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+        else fft_pass<2, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+        Ns *= R;
+    }
+}
+
+}  // namespace s2d

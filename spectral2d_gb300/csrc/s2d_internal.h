@@ -1,0 +1,112 @@
+// s2d_internal.h -- shared declarations of the Spectral2D GB300 library.
+//
+// Device data layout (one handle = one simulation, all buffers device-resident):
+//
+//   compact spectral state  S[kx][jc]   kx in [0,K], jc in [0,2K] with
+//                                       ky = jc (jc <= K) or jc - (2K+1);
+//                                       column pitch ldS; the retained
+//                                       rectangle of the reference's
+//                                       (cISize, nyG) array, K = nx/2.
+//   half-spectral rows      I[y][kx]    y in [0,M) (physical, after the
+//                                       y-transform), kx in [0,K]; row pitch ldI.
+//
+// M = 3*nx/2 is the padded collocation grid of the 3/2 rule.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "s2d.h"
+
+namespace s2d {
+
+constexpr int kMaxPasses = 16;
+constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
+
+// Geometry and FFT plan shared by every kernel of one handle.
+struct Dims {
+    int K;      // nx/2: largest retained |kx|, |ky|
+    int KX;     // K+1 retained kx columns
+    int KY;     // 2K+1 retained ky rows
+    int M;      // padded grid points per direction (3/2 rule)
+    int ldS;    // compact column pitch (elements)
+    int ldI;    // half-spectral row pitch (elements)
+    int Tg;     // threads per transform = M / kElemsPerThread
+    int npass;  // FFT passes
+    int radix[kMaxPasses];
+};
+
+// Terms of dW beyond the reference's (drag and a Kolmogorov source).
+struct Phys {
+    double nu;
+    double alpha;     // linear drag coefficient
+    int fk;           // forcing wavenumber (0 = none)
+    double f_re, f_im;  // coefficient at (kx=0, ky=+fk); conjugate at -fk
+};
+
+// Spectral operators applied when a column is read for the inverse y-pass.
+enum FieldOp : int {
+    OP_W = 0,    // omega
+    OP_U = 1,    // u = i ky psi
+    OP_V = 2,    // v = -i kx psi
+    OP_PSI = 3,  // psi = omega / k^2
+    OP_WX = 4,   // i kx omega
+    OP_WY = 5,   // i ky omega
+    OP_UX = 6,   // i kx u
+    OP_VY = 7,   // i ky v
+};
+
+struct FieldSet {
+    int nf;
+    int op[4];
+    void* out[4];
+};
+
+// Launch shape for one kernel: G groups of Tg threads, dynamic smem bytes.
+struct Launch {
+    int G;
+    int threads;
+    size_t smem;
+    int blocks;
+};
+
+// ---- kernel launchers (s2d_kernels.cu); T = float or double -------------
+template <typename T>
+struct Kern {
+    static cudaError_t yinv(const Dims& d, const void* S, const double* rk2, const FieldSet& fs,
+                            const void* tw, cudaStream_t st, const Launch& L);
+    static cudaError_t xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw, const void* tw,
+                                 cudaStream_t st, const Launch& L);
+    static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
+                                void* Sdw, int stage, double dt, const Phys& ph, const void* tw,
+                                unsigned int* flags, cudaStream_t st, const Launch& L);
+    static cudaError_t ref_to_compact(const Dims& d, const double* ref, int C, void* S,
+                                      cudaStream_t st);
+    static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
+                                      double* refPsi, cudaStream_t st);
+    static cudaError_t spectrum(const Dims& d, const void* S, double* Ek, cudaStream_t st);
+    static cudaError_t enstrophy_partial(const Dims& d, const void* S, double* part, int nblocks,
+                                         cudaStream_t st);
+    static cudaError_t minmax(const Dims& d, const void* S, unsigned long long* out4,
+                              cudaStream_t st);
+    static cudaError_t xinv_cfl(const Dims& d, const void* Iu, const void* Iv, const void* tw,
+                                unsigned long long* maxbits, cudaStream_t st, const Launch& L);
+    static cudaError_t fill_tg(const Dims& d, const double* sx, const double* sy, void* phys,
+                               cudaStream_t st);
+    static cudaError_t xfwd_phys(const Dims& d, const void* phys, void* Iout, const void* tw,
+                                 cudaStream_t st, const Launch& L);
+    static cudaError_t yfwd_store(const Dims& d, const void* I, void* S, const void* tw,
+                                  cudaStream_t st, const Launch& L);
+    static cudaError_t init_rk2(const Dims& d, double* rk2, cudaStream_t st);
+    static size_t smem_limit_yinv();
+};
+
+// Shared-memory attribute setup (called once per process and device).
+cudaError_t configure_kernels(int max_smem_optin);
+
+// nx of a handle (the IC generator works on host arrays of that grid).
+int handle_nx(const s2d_handle* h);
+
+cudaError_t launch_fp64_probe(double* sink, int blocks, int threads, int iters, cudaStream_t st);
+
+}  // namespace s2d

@@ -1,0 +1,741 @@
+// s2d_kernels.cu -- sm_103a kernels of the Spectral2D time step.
+//
+// One right-hand side (src/Spectral.F90:396-482) is three kernels:
+//
+//   K1 yinv      compact omega columns -> psi, u, v derived on the fly
+//                (ComputePsi :508-560, ComputeVelocity :576-610) -> inverse
+//                y-FFT of each kx column (the y half of TransformC2R :772-781,
+//                pruned to the N/2+1 non-zero columns) -> half-spectral rows.
+//   K2 xpass     per pair of physical rows: inverse x-FFTs of (u,v) and of
+//                omega (two real rows packed in one complex FFT), the
+//                products u*w and v*w (:442-447), forward x-FFTs and the
+//                real/imaginary split (the x half of TransformR2C :749-763,
+//                normalisation folded in).  Physical fields never touch HBM.
+//   K3 yfwd_rk3  forward y-FFT of each kx column of the two products, then
+//                Truncate (:457-458), i kx / i ky (:464-465), the viscous term
+//                (:479) and the TVD-RK3 stage combination with ComputePsi and
+//                Truncate (src/TimeIntegration.F90:156-209) in one epilogue.
+//
+// omega is not round-tripped through physical space (the reference does at
+// :435/:453); that changes omega by round-off only.
+#include "s2d_fft.cuh"
+#include "s2d_internal.h"
+
+#include <cuda_runtime.h>
+
+namespace s2d {
+
+__device__ __forceinline__ bool bits_nonfinite(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b & 0x7FF0000000000000ULL) == 0x7FF0000000000000ULL;
+}
+__device__ __forceinline__ bool bits_nonfinite(float x) {
+    const unsigned int b = (unsigned int)__float_as_int(x);
+    return (b & 0x7F800000u) == 0x7F800000u;
+}
+
+// compact row jc -> ky, and ky -> FFT index n in [0, M)
+__device__ __forceinline__ int ky_of_jc(const Dims& d, int jc) { return jc <= d.K ? jc : jc - d.KY; }
+
+// Apply a spectral operator to omega of mode (kx, ky); 1/k^2 is FP64.
+template <typename VT>
+__device__ __forceinline__ VT apply_op(int op, VT w, int kx, int ky, double rk2) {
+    using T = decltype(w.x);
+    switch (op) {
+        case OP_U: {  // u = i ky psi = (-ky psi.y, ky psi.x)
+            const double s = (double)ky * rk2;
+            return mk<VT>((T)(-s * (double)w.y), (T)(s * (double)w.x));
+        }
+        case OP_V: {  // v = -i kx psi = (kx psi.y, -kx psi.x)
+            const double s = (double)kx * rk2;
+            return mk<VT>((T)(s * (double)w.y), (T)(-s * (double)w.x));
+        }
+        case OP_PSI:
+            return mk<VT>((T)(rk2 * (double)w.x), (T)(rk2 * (double)w.y));
+        case OP_WX:
+            return mk<VT>((T)(-kx) * w.y, (T)kx * w.x);
+        case OP_WY:
+            return mk<VT>((T)(-ky) * w.y, (T)ky * w.x);
+        case OP_UX: {  // i kx u = -kx ky psi
+            const double s = -(double)kx * (double)ky * rk2;
+            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
+        }
+        case OP_VY: {  // i ky v = kx ky psi
+            const double s = (double)kx * (double)ky * rk2;
+            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
+        }
+        default:
+            return w;
+    }
+}
+
+// ------------------------------------------------------------------------
+// K1: inverse y-pass.  Block = G transforms of Tg threads; block b handles
+// field (b / ncg) on columns [cg*G, cg*G+G).
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
+                                               const double* __restrict__ rk2, FieldSet fs,
+                                               const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int ncg = (d.KX + G - 1) / G;
+    const int f = blockIdx.x / ncg;
+    const int cg = blockIdx.x - f * ncg;
+    const int kx0 = cg * G;
+    const int kx = kx0 + g;
+    const bool active = kx < d.KX;
+    const int op = fs.op[f];
+    VT* buf = bufs + (size_t)g * d.M;
+
+    const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
+    const double* rcol = rk2 + (size_t)(active ? kx : 0) * d.ldS;
+    for (int n = lane; n < d.M; n += d.Tg) {
+        VT val = mk<VT>((T)0, (T)0);
+        int jc = -1, ky = 0;
+        if (n <= d.K) {
+            jc = n;
+            ky = n;
+        } else if (n >= d.M - d.K) {
+            ky = n - d.M;
+            jc = ky + d.KY;
+        }
+        if (active && jc >= 0) val = apply_op(op, col[jc], kx, ky, rcol[jc]);
+        buf[n] = val;
+    }
+    fft_run<true>(buf, d, lane, tw);
+
+    VT* out = reinterpret_cast<VT*>(fs.out[f]);
+    const int gtot = min(G, d.KX - kx0);
+    for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
+        const int y = idx / G;
+        const int gg = idx - y * G;
+        if (gg < gtot) out[(size_t)y * d.ldI + kx0 + gg] = bufs[(size_t)gg * d.M + y];
+    }
+}
+
+// Hermitian extension of two half-spectrum rows X, Y (kx in [0,K]) packed as
+// Z = X + iY over the full length M; the kx=0 entries contribute their real
+// parts only (the c2r convention of FFTW, used by src/Spectral.F90:780).
+template <typename VT>
+__device__ __forceinline__ void build_pair(VT* buf, const VT* __restrict__ X, const VT* __restrict__ Y,
+                                           const Dims& d, int lane, bool active) {
+    using T = decltype(buf[0].x);
+    for (int n = lane; n < d.M; n += d.Tg) {
+        VT z = mk<VT>((T)0, (T)0);
+        if (active) {
+            if (n == 0) {
+                z = mk<VT>(X[0].x, Y[0].x);
+            } else if (n <= d.K) {
+                const VT a = X[n], b = Y[n];
+                z = mk<VT>(a.x - b.y, a.y + b.x);
+            } else if (n >= d.M - d.K) {
+                const VT a = X[d.M - n], b = Y[d.M - n];
+                z = mk<VT>(a.x + b.y, b.x - a.y);
+            }
+        }
+        buf[n] = z;
+    }
+}
+
+// Split the forward FFT P of p = a + i b (a, b real rows) into the half
+// spectra A(k) = (P(k) + conj P(M-k))/2 and B(k) = (P(k) - conj P(M-k))/(2i),
+// k in [0, K], times scale.
+template <typename VT>
+__device__ __forceinline__ void extract_pair(const VT* buf, VT* A, VT* B, const Dims& d, int lane,
+                                             bool active, decltype(buf[0].x) scale) {
+    if (!active) return;
+    for (int k = lane; k <= d.K; k += d.Tg) {
+        const VT p = buf[k];
+        const VT q = buf[k == 0 ? 0 : d.M - k];
+        A[k] = mk<VT>((p.x + q.x) * scale, (p.y - q.y) * scale);
+        B[k] = mk<VT>((p.y + q.y) * scale, (q.x - p.x) * scale);
+    }
+}
+
+// ------------------------------------------------------------------------
+// K2: x-pass of the RHS on row pairs (y1, y2) = (2p, 2p+1).  Per group two
+// buffers: W holds omega of both rows (w1 = Re, w2 = Im after the inverse
+// FFT), Z holds u + i v of one row, then u*w + i v*w, then its spectrum.
+// On exit rows y of Iu / Iv hold the normalised half spectra of u*w / v*w.
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_xpass_rhs(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+                                                    const typename Vec<T>::t* __restrict__ Iw,
+                                                    const typename Vec<T>::t* __restrict__ tw, int G,
+                                                    T scale) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int p = blockIdx.x * G + g;
+    const bool active = p < d.M / 2;
+    const int y1 = active ? 2 * p : 0;
+    const int y2 = y1 + 1;
+    VT* W = bufs + (size_t)(2 * g) * d.M;
+    VT* Z = W + d.M;
+
+    build_pair(W, Iw + (size_t)y1 * d.ldI, Iw + (size_t)y2 * d.ldI, d, lane, active);
+    fft_run<true>(W, d, lane, tw);
+
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+        const int yy = h ? y2 : y1;
+        VT* urow = Iu + (size_t)yy * d.ldI;
+        VT* vrow = Iv + (size_t)yy * d.ldI;
+        build_pair(Z, urow, vrow, d, lane, active);
+        fft_run<true>(Z, d, lane, tw);
+        for (int n = lane; n < d.M; n += d.Tg) {
+            const VT z = Z[n];
+            const T s = h ? W[n].y : W[n].x;
+            Z[n] = mk<VT>(z.x * s, z.y * s);
+        }
+        fft_run<false>(Z, d, lane, tw);
+        extract_pair(Z, urow, vrow, d, lane, active, scale);
+        __syncthreads();
+    }
+}
+
+// ------------------------------------------------------------------------
+// K3: forward y-pass of the two products + RK3 stage epilogue.
+// Block = 2G transforms (G columns x {u*w, v*w}).
+//   stage 1: S1 = S0 + dt dW                    (w_in = S0)
+//   stage 2: S1 = 3/4 S0 + 1/4 S1 + dt/4 dW      (w_in = S1)
+//   stage 3: S0 = S0/3 + 2/3 S1 + 2dt/3 dW       (w_in = S1)
+//   stage 0: Sdw = dW of w_in = S0 (ComputeRHS alone)
+// followed by Truncate (|k|^2 > K^2 -> 0).  Division by 3 is a multiply by
+// the rounded reciprocal (a <= 1 ulp difference from :198-200).
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>::t* __restrict__ Iu,
+                                                   const typename Vec<T>::t* __restrict__ Iv,
+                                                   typename Vec<T>::t* S0, typename Vec<T>::t* S1,
+                                                   typename Vec<T>::t* Sdw, int stage, double dt,
+                                                   Phys ph, const typename Vec<T>::t* __restrict__ tw,
+                                                   int G, unsigned int* flags) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int t = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - t * d.Tg;
+    const int kx0 = blockIdx.x * G;
+    const int gtot = min(G, d.KX - kx0);
+
+    for (int idx = threadIdx.x; idx < 2 * G * d.M; idx += blockDim.x) {
+        const int gg = idx % G;
+        const int rest = idx / G;
+        const int y = rest % d.M;
+        const int fld = rest / d.M;
+        VT v = mk<VT>((T)0, (T)0);
+        if (gg < gtot) v = (fld ? Iv : Iu)[(size_t)y * d.ldI + kx0 + gg];
+        bufs[(size_t)(fld * G + gg) * d.M + y] = v;
+    }
+    const int nconc = blockDim.x / d.Tg;
+    for (int t0 = 0; t0 < 2 * G; t0 += nconc) fft_run<false>(bufs + (size_t)(t0 + t) * d.M, d, lane, tw);
+    __syncthreads();
+
+    const T tdt = (T)dt;
+    const T c34 = (T)0.75, c14 = (T)0.25, c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0);
+    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * 2.0 / 3.0);
+    const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
+    const int K2 = d.K * d.K;
+    bool bad = false;
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = idx / d.KY;
+        const int jc = idx - gg * d.KY;
+        const int kx = kx0 + gg;
+        const int ky = ky_of_jc(d, jc);
+        const int n = jc <= d.K ? jc : ky + d.M;
+        const size_t off = (size_t)kx * d.ldS + jc;
+        const int kk = kx * kx + ky * ky;
+        VT out;
+        if (kk > K2) {
+            out = mk<VT>((T)0, (T)0);
+        } else {
+            const VT nx = bufs[(size_t)gg * d.M + n];
+            const VT ny = bufs[(size_t)(G + gg) * d.M + n];
+            const VT w0 = S0[off];
+            const VT win = (stage <= 1) ? w0 : S1[off];
+            const T fkx = (T)kx, fky = (T)ky;
+            const T visc = tnu * (T)kk;
+            // dW = -i kx Nx - i ky Ny - nu k^2 w   (src/Spectral.F90:464-479)
+            T dwx = fkx * nx.y + fky * ny.y - visc * win.x;
+            T dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+            if (talpha != (T)0) {
+                dwx -= talpha * win.x;
+                dwy -= talpha * win.y;
+            }
+            if (ph.fk != 0 && kx == 0 && (ky == ph.fk || ky == -ph.fk)) {
+                dwx += (T)ph.f_re;
+                dwy += (ky > 0) ? (T)ph.f_im : (T)(-ph.f_im);
+            }
+            if (stage == 0) {
+                out = mk<VT>(dwx, dwy);
+            } else if (stage == 1) {
+                out = mk<VT>(w0.x + tdt * dwx, w0.y + tdt * dwy);
+            } else if (stage == 2) {
+                out = mk<VT>(c34 * w0.x + c14 * win.x + dt4 * dwx, c34 * w0.y + c14 * win.y + dt4 * dwy);
+            } else {
+                out = mk<VT>(c13 * w0.x + c23 * win.x + dt23 * dwx, c13 * w0.y + c23 * win.y + dt23 * dwy);
+            }
+            bad |= bits_nonfinite(out.x) | bits_nonfinite(out.y);
+        }
+        if (stage == 0) Sdw[off] = out;
+        else if (stage == 3) S0[off] = out;
+        else S1[off] = out;
+    }
+    if (bad) atomicOr(flags, 1u);
+}
+
+// ------------------------------------------------------------------------
+// Layout conversion between the reference's (cISize, nyG) complex128 array
+// and the compact state.
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void k_ref_to_compact(Dims d, const double2* __restrict__ ref, int C, typename Vec<T>::t* S) {
+    using VT = typename Vec<T>::t;
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const int ky = ky_of_jc(d, jc);
+        const int n = ky >= 0 ? ky : ky + d.M;
+        VT v = mk<VT>((T)0, (T)0);
+        if (kx * kx + ky * ky <= d.K * d.K) {
+            const double2 r = ref[(size_t)n * C + kx];
+            v = mk<VT>((T)r.x, (T)r.y);
+        }
+        S[(size_t)kx * d.ldS + jc] = v;
+    }
+}
+
+// psi = w / (kx^2 + ky^2), psi(0,0) = 0 (src/Spectral.F90:508-560), written
+// with the state into full reference arrays (zeros outside the rectangle).
+template <typename T>
+__global__ void k_compact_to_ref(Dims d, const typename Vec<T>::t* __restrict__ S, int C, double2* refW,
+                                 double2* refPsi) {
+    const long total = (long)d.M * C;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const int n = (int)(idx / C);
+        const int kx = (int)(idx - (long)n * C);
+        const int ky = n <= d.M / 2 ? n : n - d.M;
+        double2 w = make_double2(0.0, 0.0);
+        if (kx <= d.K && ky >= -d.K && ky <= d.K) {
+            const int jc = ky >= 0 ? ky : ky + d.KY;
+            const auto v = S[(size_t)kx * d.ldS + jc];
+            w = make_double2((double)v.x, (double)v.y);
+        }
+        if (refW) refW[idx] = w;
+        if (refPsi) {
+            const double k2 = (double)kx * kx + (double)ky * ky;
+            refPsi[idx] = (k2 == 0.0) ? make_double2(0.0, 0.0) : make_double2(w.x / k2, w.y / k2);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------
+// Diagnostics
+// ------------------------------------------------------------------------
+__device__ __forceinline__ int isqrt_floor(int c) {
+    int r = (int)sqrtf((float)c);
+    while (r > 0 && r * r > c) --r;
+    while ((r + 1) * (r + 1) <= c) ++r;
+    return r;
+}
+
+// One warp per spectrum bin b: modes with round(|k|) == b, i.e.
+// b^2 - b + 1 <= kx^2 + ky^2 <= b^2 + b (the bins of BinarySearch with the
+// edges of src/Analysis.F90:358-362).  Energy per mode |u|^2 + |v|^2 with
+// u = i ky psi, v = -i kx psi and weight 1/2 on kx = 0 (:380-395).  Bins
+// above K hold no retained mode and are written as zero.
+template <typename T>
+__global__ void k_spectrum(Dims d, const typename Vec<T>::t* __restrict__ S, double* Ek, int nbins) {
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    const int b = warp;
+    if (b >= nbins) return;
+    double sum = 0.0;
+    if (b <= d.K) {
+        const int lo = b == 0 ? 0 : b * b - b + 1;
+        const int hi = min(b == 0 ? 0 : b * b + b, d.K * d.K);
+        for (int kx = lane; kx <= min(b, d.K); kx += 32) {
+            const int kx2 = kx * kx;
+            const int c = hi - kx2;
+            if (c < 0) continue;
+            const int a = max(lo - kx2, 0);
+            int kylo = isqrt_floor(a);
+            if (kylo * kylo < a) ++kylo;
+            const int kyhi = isqrt_floor(c);
+            for (int aky = kylo; aky <= kyhi; ++aky) {
+                for (int sgn = 0; sgn < (aky == 0 ? 1 : 2); ++sgn) {
+                    const int ky = sgn ? -aky : aky;
+                    const int jc = ky >= 0 ? ky : ky + d.KY;
+                    const auto v = S[(size_t)kx * d.ldS + jc];
+                    const double k2 = (double)kx2 + (double)ky * ky;
+                    double px = 0.0, py = 0.0;
+                    if (k2 != 0.0) {
+                        px = (double)v.x / k2;
+                        py = (double)v.y / k2;
+                    }
+                    const double ux = -(double)ky * py, uy = (double)ky * px;
+                    const double vx = (double)kx * py, vy = -(double)kx * px;
+                    const double e = ux * ux + uy * uy + vx * vx + vy * vy;
+                    sum += (kx == 0) ? 0.5 * e : e;
+                }
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) Ek[b] = sum;
+}
+
+// Partial sums of weight*|w|^2 per block (deterministic order).
+template <typename T>
+__global__ void k_enstrophy_partial(Dims d, const typename Vec<T>::t* __restrict__ S, double* part) {
+    __shared__ double red[256];
+    double s = 0.0;
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const auto v = S[(size_t)kx * d.ldS + jc];
+        const double e = (double)v.x * v.x + (double)v.y * v.y;
+        s += (kx == 0) ? e : 2.0 * e;
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// out[0] = max|w|, out[1] = min|w|, out[2] = max|psi|, out[3] = min|psi| as
+// the bit patterns of non-negative doubles (ordered like unsigned integers).
+template <typename T>
+__global__ void k_minmax(Dims d, const typename Vec<T>::t* __restrict__ S, unsigned long long* out) {
+    double mxw = 0.0, mnw = 1.0e308, mxp = 0.0, mnp = 1.0e308;
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const int ky = ky_of_jc(d, jc);
+        const auto v = S[(size_t)kx * d.ldS + jc];
+        const double aw = hypot((double)v.x, (double)v.y);
+        const double k2 = (double)kx * kx + (double)ky * ky;
+        const double ap = (k2 == 0.0) ? 0.0 : hypot((double)v.x / k2, (double)v.y / k2);
+        mxw = fmax(mxw, aw);
+        mnw = fmin(mnw, aw);
+        mxp = fmax(mxp, ap);
+        mnp = fmin(mnp, ap);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        mxw = fmax(mxw, __shfl_xor_sync(0xffffffffu, mxw, o));
+        mnw = fmin(mnw, __shfl_xor_sync(0xffffffffu, mnw, o));
+        mxp = fmax(mxp, __shfl_xor_sync(0xffffffffu, mxp, o));
+        mnp = fmin(mnp, __shfl_xor_sync(0xffffffffu, mnp, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicMax(&out[0], (unsigned long long)__double_as_longlong(mxw));
+        atomicMin(&out[1], (unsigned long long)__double_as_longlong(mnw));
+        atomicMax(&out[2], (unsigned long long)__double_as_longlong(mxp));
+        atomicMin(&out[3], (unsigned long long)__double_as_longlong(mnp));
+    }
+}
+
+// Physical u, v of each row (one complex inverse FFT of u + i v), then
+// max(|u|/dx + |v|/dy) with dx = dy = 2 pi / M.
+template <typename T>
+__global__ void __launch_bounds__(512) k_xinv_cfl(Dims d, const typename Vec<T>::t* __restrict__ Iu,
+                                                   const typename Vec<T>::t* __restrict__ Iv,
+                                                   const typename Vec<T>::t* __restrict__ tw, int G,
+                                                   unsigned long long* maxbits) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    __shared__ double red[32];
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    VT* Z = bufs + (size_t)g * d.M;
+    const int yy = active ? y : 0;
+    build_pair(Z, Iu + (size_t)yy * d.ldI, Iv + (size_t)yy * d.ldI, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);
+    const double inv_dx = (double)d.M / (2.0 * 3.14159265358979323846);
+    double m = 0.0;
+    if (active)
+        for (int n = lane; n < d.M; n += d.Tg) {
+            const VT z = Z[n];
+            m = fmax(m, fabs((double)z.x) * inv_dx + fabs((double)z.y) * inv_dx);
+        }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < (blockDim.x + 31) / 32 ? red[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) atomicMax(maxbits, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+// Taylor-Green vorticity on the physical grid, 2 sin(x_i) sin(y_j) with the
+// 1-based coordinates of src/SetIC.F90:88-96 (sx, sy precomputed on the host
+// with the same FP64 sin as the reference).
+template <typename T>
+__global__ void k_fill_tg(Dims d, const double* __restrict__ sx, const double* __restrict__ sy, T* phys) {
+    const long total = (long)d.M * d.M;
+    for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total; idx += (long)gridDim.x * blockDim.x) {
+        const int j = (int)(idx / d.M);
+        const int i = (int)(idx - (long)j * d.M);
+        phys[idx] = (T)((2.0 * sx[i]) * sy[j]);
+    }
+}
+
+// Forward x-transform of physical rows (pitch M) in pairs: one complex FFT
+// of r1 + i r2, split into two normalised half spectra (kx in [0,K]).
+template <typename T>
+__global__ void __launch_bounds__(512) k_xfwd_phys(Dims d, const T* __restrict__ phys,
+                                                    typename Vec<T>::t* Iout,
+                                                    const typename Vec<T>::t* __restrict__ tw, int G,
+                                                    T scale) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int p = blockIdx.x * G + g;
+    const bool active = p < d.M / 2;
+    const int y1 = active ? 2 * p : 0;
+    VT* Z = bufs + (size_t)g * d.M;
+    const T* r1 = phys + (size_t)y1 * d.M;
+    const T* r2 = r1 + d.M;
+    for (int n = lane; n < d.M; n += d.Tg) Z[n] = active ? mk<VT>(r1[n], r2[n]) : mk<VT>((T)0, (T)0);
+    fft_run<false>(Z, d, lane, tw);
+    extract_pair(Z, Iout + (size_t)y1 * d.ldI, Iout + (size_t)(y1 + 1) * d.ldI, d, lane, active, scale);
+}
+
+// Forward y-transform of half-spectral columns into the compact state, with
+// Truncate.
+template <typename T>
+__global__ void __launch_bounds__(512) k_yfwd_store(Dims d, const typename Vec<T>::t* __restrict__ I,
+                                                     typename Vec<T>::t* S,
+                                                     const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int kx0 = blockIdx.x * G;
+    const int gtot = min(G, d.KX - kx0);
+    for (int idx = threadIdx.x; idx < G * d.M; idx += blockDim.x) {
+        const int gg = idx % G;
+        const int y = idx / G;
+        bufs[(size_t)gg * d.M + y] = gg < gtot ? I[(size_t)y * d.ldI + kx0 + gg] : mk<VT>((T)0, (T)0);
+    }
+    fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = idx / d.KY;
+        const int jc = idx - gg * d.KY;
+        const int kx = kx0 + gg;
+        const int ky = ky_of_jc(d, jc);
+        const int n = jc <= d.K ? jc : ky + d.M;
+        VT v = bufs[(size_t)gg * d.M + n];
+        if (kx * kx + ky * ky > d.K * d.K) v = mk<VT>((T)0, (T)0);
+        S[(size_t)kx * d.ldS + jc] = v;
+    }
+}
+
+// 1/(kx^2+ky^2) per compact mode, 0 at the mean mode (FP64 in every variant).
+__global__ void k_init_rk2(Dims d, double* rk2) {
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const int ky = ky_of_jc(d, jc);
+        const double k2 = (double)kx * kx + (double)ky * ky;
+        rk2[(size_t)kx * d.ldS + jc] = (k2 == 0.0) ? 0.0 : 1.0 / k2;
+    }
+}
+
+// FP64 throughput probe: 8 independent FMA chains per thread.
+__global__ void k_fp64_probe(double* sink, int iters) {
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+    double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+    const double b = 0.999999, c = 1e-7;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c); a1 = fma(a1, b, c); a2 = fma(a2, b, c); a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c); a5 = fma(a5, b, c); a6 = fma(a6, b, c); a7 = fma(a7, b, c);
+    }
+    const double s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (s == 12345.678) sink[threadIdx.x] = s;
+}
+
+// ------------------------------------------------------------------------
+// Host-side launchers
+// ------------------------------------------------------------------------
+static int grid_for(long work, int threads) {
+    long b = (work + threads - 1) / threads;
+    if (b > 152L * 32) b = 152L * 32;
+    if (b < 1) b = 1;
+    return (int)b;
+}
+
+template <typename T>
+cudaError_t Kern<T>::yinv(const Dims& d, const void* S, const double* rk2, const FieldSet& fs, const void* tw,
+                          cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    const int ncg = (d.KX + L.G - 1) / L.G;
+    k_yinv<T><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw, const void* tw,
+                               cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    const int pairs = d.M / 2;
+    const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
+    k_xpass_rhs<T><<<(pairs + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)Iw,
+                                                                         (const VT*)tw, L.G, scale);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1, void* Sdw,
+                              int stage, double dt, const Phys& ph, const void* tw, unsigned int* flags,
+                              cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    k_yfwd_rk3<T><<<(d.KX + L.G - 1) / L.G, L.threads, L.smem, st>>>(
+        d, (const VT*)Iu, (const VT*)Iv, (VT*)S0, (VT*)S1, (VT*)Sdw, stage, dt, ph, (const VT*)tw, L.G, flags);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::ref_to_compact(const Dims& d, const double* ref, int C, void* S, cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    k_ref_to_compact<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const double2*)ref, C, (VT*)S);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::compact_to_ref(const Dims& d, const void* S, int C, double* refW, double* refPsi,
+                                    cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    k_compact_to_ref<T><<<grid_for((long)d.M * C, 256), 256, 0, st>>>(d, (const VT*)S, C, (double2*)refW,
+                                                                     (double2*)refPsi);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::spectrum(const Dims& d, const void* S, double* Ek, cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    // bins 0..K get a warp each; the caller zeroes the rest
+    const int nb = d.K + 1;
+    k_spectrum<T><<<(nb * 32 + 255) / 256, 256, 0, st>>>(d, (const VT*)S, Ek, nb);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::enstrophy_partial(const Dims& d, const void* S, double* part, int nblocks,
+                                       cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    k_enstrophy_partial<T><<<nblocks, 256, 0, st>>>(d, (const VT*)S, part);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::minmax(const Dims& d, const void* S, unsigned long long* out4, cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    k_minmax<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const VT*)S, out4);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::xinv_cfl(const Dims& d, const void* Iu, const void* Iv, const void* tw,
+                              unsigned long long* maxbits, cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    k_xinv_cfl<T><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv,
+                                                                     (const VT*)tw, L.G, maxbits);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::fill_tg(const Dims& d, const double* sx, const double* sy, void* phys, cudaStream_t st) {
+    k_fill_tg<T><<<grid_for((long)d.M * d.M, 256), 256, 0, st>>>(d, sx, sy, (T*)phys);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::xfwd_phys(const Dims& d, const void* phys, void* Iout, const void* tw, cudaStream_t st,
+                               const Launch& L) {
+    using VT = typename Vec<T>::t;
+    const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
+    k_xfwd_phys<T><<<(d.M / 2 + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (const T*)phys, (VT*)Iout,
+                                                                         (const VT*)tw, L.G, scale);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::yfwd_store(const Dims& d, const void* I, void* S, const void* tw, cudaStream_t st,
+                                const Launch& L) {
+    using VT = typename Vec<T>::t;
+    k_yfwd_store<T><<<(d.KX + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (const VT*)I, (VT*)S,
+                                                                       (const VT*)tw, L.G);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::init_rk2(const Dims& d, double* rk2, cudaStream_t st) {
+    k_init_rk2<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2);
+    return cudaGetLastError();
+}
+
+template <typename T>
+size_t Kern<T>::smem_limit_yinv() {
+    return 0;
+}
+
+template struct Kern<double>;
+template struct Kern<float>;
+
+template <typename K>
+static cudaError_t set_smem(K kernel, int bytes) {
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+cudaError_t configure_kernels(int max_smem_optin) {
+    cudaError_t e = cudaSuccess;
+#define S2D_SET(k)                                          \
+    do {                                                    \
+        cudaError_t e2 = set_smem(k, max_smem_optin);       \
+        if (e2 != cudaSuccess && e == cudaSuccess) e = e2;  \
+    } while (0)
+    S2D_SET(k_yinv<double>);
+    S2D_SET(k_yinv<float>);
+    S2D_SET(k_xpass_rhs<double>);
+    S2D_SET(k_xpass_rhs<float>);
+    S2D_SET(k_yfwd_rk3<double>);
+    S2D_SET(k_yfwd_rk3<float>);
+    S2D_SET(k_xinv_cfl<double>);
+    S2D_SET(k_xinv_cfl<float>);
+    S2D_SET(k_xfwd_phys<double>);
+    S2D_SET(k_xfwd_phys<float>);
+    S2D_SET(k_yfwd_store<double>);
+    S2D_SET(k_yfwd_store<float>);
+#undef S2D_SET
+    return e;
+}
+
+cudaError_t launch_fp64_probe(double* sink, int blocks, int threads, int iters, cudaStream_t st) {
+    k_fp64_probe<<<blocks, threads, 0, st>>>(sink, iters);
+    return cudaGetLastError();
+}
+
+}  // namespace s2d

@@ -1,0 +1,188 @@
+"""Python host interface over the C-ABI, named after the reference's routines.
+
+The reference is a Fortran program whose modules expose ``GetGridSize``,
+``SetTaylorGreen``, ``SetTurbulentVelocity``, ``IntegrateOneStep``,
+``ComputeRHS``, ``ComputeSpectrum`` and the driver's min/max print
+(src/Spectral.F90, src/SetIC.F90, src/TimeIntegration.F90,
+src/Analysis.F90, src/Spectral2D.F90).  :class:`Spectral2D` offers the same
+operations on a device-resident state; spectral arrays crossing this
+interface use the reference layout: complex128 of shape ``(nyG, cISize)``
+(C order), which is the Fortran ``(cISize, nyG)`` array.
+
+Every call goes through ``libspectral2d_gb300.so``; there is no CPU path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+_FP = {"fp64": L.S2D_FP64, "fp32": L.S2D_FP32}
+_SPEC = {"schumann": L.S2D_SPECTRUM_SCHUMANN, "k4gauss": L.S2D_SPECTRUM_K4_GAUSS}
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def get_grid_size(nx: int, ny: int, dealias: int = L.S2D_DEALIAS_3_2_RULE) -> L.S2DGrid:
+    """``GetGridSize`` (src/Spectral.F90:117-219)."""
+    g = L.S2DGrid()
+    L.check(L.lib().s2d_get_grid_size(nx, ny, dealias, C.byref(g)))
+    return g
+
+
+def turbulent_ic_host(nx: int, seed: int, spectrum: str = "k4gauss", k0: float = 10.0,
+                      urms: float = 1.0, tke: float = 0.5) -> np.ndarray:
+    """The library's turbulent-IC generator evaluated on the host (no GPU)."""
+    g = get_grid_size(nx, nx)
+    w = np.zeros((g.nyG, g.cISize), dtype=np.complex128)
+    L.check(L.lib().s2d_turbulent_ic_host(nx, seed, _SPEC[spectrum], k0, urms, tke,
+                                          _dptr(w.view(np.float64))))
+    return w
+
+
+def probe_fp64_peak(device: int = 0) -> float:
+    """Measured FP64 FMA throughput of the GPU, TFLOP/s."""
+    v = C.c_double()
+    L.check(L.lib().s2d_probe_fp64_peak(device, C.byref(v)))
+    return v.value
+
+
+class Spectral2D:
+    """One vorticity-streamfunction simulation on one GPU."""
+
+    def __init__(self, nx: int, ny: int | None = None, nu: float = 0.005,
+                 precision: str = "fp64", alpha: float = 0.0, forcing_amp: float = 0.0,
+                 forcing_k: int = 0, device: int = 0,
+                 dealias: int = L.S2D_DEALIAS_3_2_RULE):
+        self._L = L.lib()
+        cfg = L.S2DConfig(nx=nx, ny=ny if ny is not None else nx, dealias=dealias,
+                          precision=_FP[precision], nu=nu, alpha=alpha,
+                          forcing_amp=forcing_amp, forcing_k=forcing_k, device=device)
+        h = C.c_void_p()
+        L.check(self._L.s2d_create(C.byref(cfg), C.byref(h)))
+        self._h = h
+        self.nx = nx
+        self.nu = nu
+        self.precision = precision
+        self.grid = get_grid_size(nx, cfg.ny, dealias)
+        self.shape = (self.grid.nyG, self.grid.cISize)
+
+    # -- lifetime -----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.s2d_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover - best effort
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- state ----------------------------------------------------------------
+    def _new(self) -> np.ndarray:
+        return np.zeros(self.shape, dtype=np.complex128)
+
+    def set_state(self, wC: np.ndarray) -> None:
+        w = np.ascontiguousarray(wC, dtype=np.complex128)
+        assert w.shape == self.shape, (w.shape, self.shape)
+        L.check(self._L.s2d_set_state(self._h, _dptr(w.view(np.float64)), *self.shape[::-1]))
+
+    def get_state(self):
+        """Return ``(wC, psiC)`` in the reference layout."""
+        w, p = self._new(), self._new()
+        L.check(self._L.s2d_get_state(self._h, _dptr(w.view(np.float64)),
+                                      _dptr(p.view(np.float64)), *self.shape[::-1]))
+        return w, p
+
+    # -- initial conditions --------------------------------------------------
+    def set_taylor_green(self) -> None:
+        """``SetTaylorGreen`` (src/SetIC.F90:70-101)."""
+        L.check(self._L.s2d_set_taylor_green(self._h))
+
+    def set_turbulent_velocity(self, seed: int, spectrum: str = "k4gauss", k0: float = 10.0,
+                               urms: float = 1.0, tke: float = 0.5) -> None:
+        """``SetTurbulentVelocity`` (src/SetIC.F90:125-151) with a seeded phase."""
+        L.check(self._L.s2d_set_turbulent(self._h, seed, _SPEC[spectrum], k0, urms, tke))
+
+    # -- time stepping -------------------------------------------------------
+    def integrate_one_step(self, dt: float) -> None:
+        """``IntegrateOneStep`` (src/TimeIntegration.F90:130-210)."""
+        L.check(self._L.s2d_integrate_one_step(self._h, dt))
+
+    def integrate_steps(self, n: int, dt: float) -> None:
+        L.check(self._L.s2d_integrate_steps(self._h, n, dt))
+
+    def integrate_one_step_host(self, wC: np.ndarray, dt: float):
+        """``IntegrateOneStep`` on host arrays: returns the new ``(wC, psiC)``."""
+        w = np.array(wC, dtype=np.complex128, order="C", copy=True)
+        p = self._new()
+        L.check(self._L.s2d_integrate_one_step_host(self._h, _dptr(w.view(np.float64)),
+                                                    _dptr(p.view(np.float64)),
+                                                    *self.shape[::-1], dt))
+        return w, p
+
+    def compute_rhs(self) -> np.ndarray:
+        """``ComputeRHS`` (src/Spectral.F90:396-482) of the current state."""
+        d = self._new()
+        L.check(self._L.s2d_compute_rhs(self._h, _dptr(d.view(np.float64)), *self.shape[::-1]))
+        return d
+
+    def compute_time_step(self, cfl: float) -> float:
+        """CFL time step (fills ``ComputeTimeStep``, src/TimeIntegration.F90:213-215)."""
+        v = C.c_double()
+        L.check(self._L.s2d_cfl_dt(self._h, cfl, C.byref(v)))
+        return v.value
+
+    def synchronize(self) -> None:
+        L.check(self._L.s2d_synchronize(self._h))
+
+    def check_finite(self) -> None:
+        L.check(self._L.s2d_check_finite(self._h))
+
+    # -- diagnostics ---------------------------------------------------------
+    def compute_spectrum(self):
+        """``ComputeSpectrum`` (src/Analysis.F90:267-460):
+        ``(kBin, Ek, tke, eps, enstDiss)``."""
+        nb = L.check(self._L.s2d_spectrum_bins(self._h))
+        Ek = np.zeros(nb)
+        t, e, z = C.c_double(), C.c_double(), C.c_double()
+        L.check(self._L.s2d_spectrum(self._h, _dptr(Ek), nb, C.byref(t), C.byref(e), C.byref(z)))
+        return np.arange(nb, dtype=np.float64), Ek, t.value, e.value, z.value
+
+    def enstrophy(self) -> float:
+        v = C.c_double()
+        L.check(self._L.s2d_enstrophy(self._h, C.byref(v)))
+        return v.value
+
+    def minmax_abs(self):
+        """(max|w|, min|w|, max|psi|, min|psi|) as printed by src/Spectral2D.F90:358-377."""
+        out = np.zeros(4)
+        L.check(self._L.s2d_minmax_abs(self._h, _dptr(out)))
+        return tuple(float(x) for x in out)
+
+    # -- timing ----------------------------------------------------------------
+    def time_steps(self, n: int, dt: float, per_kernel: bool = False):
+        """Device time of n steps on the handle's stream (CUDA events).
+        Returns ``ms`` or ``(ms, [yinv_ms, xpass_ms, yfwd_ms])``."""
+        ms = C.c_double()
+        if per_kernel:
+            k = np.zeros(3)
+            L.check(self._L.s2d_time_steps(self._h, n, dt, C.byref(ms), _dptr(k)))
+            return ms.value, k
+        L.check(self._L.s2d_time_steps(self._h, n, dt, C.byref(ms), None))
+        return ms.value
+
+    def kernels_per_step(self) -> int:
+        return L.check(self._L.s2d_kernels_per_step(self._h))

@@ -1,0 +1,79 @@
+"""CPU tests of the C-ABI library: it loads without a GPU, exports every
+symbol include/*.h declares, and its host-only entry points agree with the
+oracle.  No compute call here touches a GPU."""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle as O
+from spectral2d_gb300 import _lib as L
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    names = L.header_symbols()
+    assert len(names) >= 25
+    lib = C.CDLL(built_lib)
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the ctypes table covers the header exactly
+    assert sorted(names) == sorted(L.SIGNATURES)
+
+
+@pytest.mark.parametrize("nx", [8, 96, 256, 2048, 4096])
+def test_get_grid_size_matches_oracle(gpu_lib, nx):
+    g = L.S2DGrid()
+    assert gpu_lib.s2d_get_grid_size(nx, nx, 1, C.byref(g)) == 0
+    o = O.get_grid_size(nx, nx)
+    for f in ("nxG", "nyG", "kxLG", "kyLG", "kxMG", "kyMG", "kxLU", "kyLU", "kxMU", "kyMU",
+              "rISize", "cISize"):
+        assert getattr(g, f) == getattr(o, f), f
+    assert g.kMax == o.kMax
+
+
+def test_grid_size_rejects_unimplemented_dealiasing(gpu_lib):
+    g = L.S2DGrid()
+    assert gpu_lib.s2d_get_grid_size(16, 16, 2, C.byref(g)) == L.S2D_ERR_UNSUPPORTED
+    assert "empty case" in L.last_error()
+
+
+@pytest.mark.parametrize("kind,k0", [(1, 10.0), (0, 1.5)])
+def test_turbulent_ic_host_matches_oracle(gpu_lib, kind, k0):
+    from spectral2d_gb300.solver import turbulent_ic_host
+    nx = 64
+    w = turbulent_ic_host(nx, 7, "k4gauss" if kind == 1 else "schumann", k0, 1.0, 0.5)
+    g = O.get_grid_size(nx, nx)
+    wo, _ = O.set_turbulent(g, 7, kind=kind, k0=k0, urms=1.0, tke_target=0.5)
+    assert O.rel_l2(w, wo) < 1e-13
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(nx=0), dict(nx=12), dict(nx=16, ny=32), dict(nx=16, dealias=0),
+    dict(nx=16, precision=7), dict(nx=16, nu=float("nan")), dict(nx=16, forcing_amp=1.0, forcing_k=99),
+])
+def test_create_rejects_bad_config_before_touching_a_gpu(gpu_lib, cfg):
+    c = L.S2DConfig(nx=cfg.get("nx", 16), ny=cfg.get("ny", cfg.get("nx", 16)),
+                    dealias=cfg.get("dealias", 1), precision=cfg.get("precision", 0),
+                    nu=cfg.get("nu", 0.01), alpha=0.0, forcing_amp=cfg.get("forcing_amp", 0.0),
+                    forcing_k=cfg.get("forcing_k", 0), device=0)
+    h = C.c_void_p()
+    r = gpu_lib.s2d_create(C.byref(c), C.byref(h))
+    assert r in (L.S2D_ERR_INVALID, L.S2D_ERR_UNSUPPORTED), (r, L.last_error())
+    assert not h.value
+
+
+def test_null_arguments_are_rejected(gpu_lib):
+    assert gpu_lib.s2d_get_grid_size(16, 16, 1, None) == L.S2D_ERR_INVALID
+    assert gpu_lib.s2d_create(None, None) == L.S2D_ERR_INVALID
+    assert gpu_lib.s2d_integrate_one_step(None, 0.1) == L.S2D_ERR_INVALID
+    assert gpu_lib.s2d_set_state(None, None, 0, 0) == L.S2D_ERR_INVALID
+    assert gpu_lib.s2d_turbulent_ic_host(16, 1, 1, 10.0, 1.0, 0.5, None) == L.S2D_ERR_INVALID
+
+
+def test_product_package_does_not_import_the_oracle():
+    import pathlib
+    pkg = pathlib.Path(L.PKG)
+    for p in pkg.rglob("*"):
+        if p.suffix in (".py", ".cu", ".cpp", ".h", ".cuh"):
+            assert "oracle" not in p.read_text().replace("the oracle", ""), p

@@ -1,0 +1,263 @@
+"""GPU parity tests: the sm_103a path through the C-ABI against the oracle
+(the FP64 numpy restatement of the reference) and the exact golden vectors.
+
+Tolerances (relative L2 in omega unless stated):
+  * one RHS: 1e-13; one RK3 step: 1e-12 (the reference's one-step bar);
+  * 1000 steps of decaying turbulence: 1e-9 (the reference's 1000-step bar);
+  * Taylor-Green after 1000 steps vs exp(-2 nu t): 1e-10;
+  * FP32 variant vs FP64 oracle: stated per test (round-off of FP32 FFTs).
+"""
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module")
+def S2D(built_lib):
+    from spectral2d_gb300 import Spectral2D
+    return Spectral2D
+
+
+def _oracle_state(w, g):
+    w = O.truncate(w, g)
+    return w, O.truncate(O.compute_psi(w, g), g)
+
+
+@pytest.mark.parametrize("n", [8, 16])
+def test_rhs_exact_golden(S2D, n):
+    d = np.load(os.path.join(GOLD, f"rhs_exact_n{n}.npz"))
+    with S2D(n, nu=float(d["nu"])) as s:
+        s.set_state(d["w"])
+        dW = s.compute_rhs()
+    assert O.rel_l2(dW, d["dW"]) < 1e-14
+
+
+def test_step_exact_golden(S2D):
+    d = np.load(os.path.join(GOLD, "step_exact_n8.npz"))
+    with S2D(8, nu=float(d["nu"])) as s:
+        s.set_state(d["w"])
+        s.integrate_one_step(float(d["dt"]))
+        w, p = s.get_state()
+    assert O.rel_l2(w, d["w_new"]) < 1e-14
+    assert O.rel_l2(p, d["psi_new"]) < 1e-14
+
+
+@pytest.mark.parametrize("n", [8, 32, 64, 96, 128, 256, 512])
+def test_rhs_vs_oracle(S2D, n):
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 100 + n)
+    with S2D(n, nu=0.01) as s:
+        s.set_state(w)
+        dW = s.compute_rhs()
+        w_back, psi_back = s.get_state()
+    wo, po = _oracle_state(w, g)
+    assert np.array_equal(w_back, wo)
+    assert O.rel_l2(psi_back, po) < 1e-15
+    ref, _ = O.compute_rhs(wo, po, g, 0.01, round_trip=False)
+    assert O.rel_l2(dW, O.truncate(ref, g)) < 1e-13
+
+
+@pytest.mark.parametrize("n", [16, 64, 256])
+def test_one_step_vs_oracle(S2D, n):
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 7 + n, decay=0.05)
+    nu, dt = 0.005, 1e-3
+    with S2D(n, nu=nu) as s:
+        s.set_state(w)
+        s.integrate_one_step(dt)
+        wg, pg = s.get_state()
+    wo, po = _oracle_state(w, g)
+    for rt in (False, True):   # with and without the reference's omega round trip
+        w1, p1 = O.integrate_one_step(wo, po, g, nu, dt, round_trip=rt)
+        assert O.rel_l2(wg, w1) < 1e-12
+        assert O.rel_l2(pg, p1) < 1e-12
+
+
+def test_taylor_green_ic_matches_oracle(S2D):
+    g = O.get_grid_size(64, 64)
+    with S2D(64, nu=0.01) as s:
+        s.set_taylor_green()
+        w, p = s.get_state()
+    wo, po = O.set_taylor_green(g)
+    assert O.rel_l2(w, O.truncate(wo, g)) < 1e-14
+    assert O.rel_l2(p, O.truncate(po, g)) < 1e-14
+
+
+def test_taylor_green_1000_steps_analytic(S2D):
+    """The Taylor-Green workload: N=256 (384^2 padded), nu=0.01, dt=1e-3,
+    1000 steps, against the analytic decay exp(-2 nu t)."""
+    n, nu, dt, steps = 256, 0.01, 1e-3, 1000
+    g = O.get_grid_size(n, n)
+    with S2D(n, nu=nu) as s:
+        s.set_taylor_green()
+        w0, _ = s.get_state()
+        s.integrate_steps(steps, dt)
+        w, p = s.get_state()
+    F = math.exp(-2.0 * nu * steps * dt)
+    assert O.rel_l2(w, w0 * F) < 1e-10
+    psiE, wE, uE, vE = O.taylor_green_exact(g, nu, steps * dt)
+    dx = 2 * np.pi / g.nxG
+    wN = O.transform_c2r(w, g)
+    pN = O.transform_c2r(p, g)
+    # the error norms of analysis/TaylorGreen.py:43-60
+    assert O.l2_error(dx, dx, wE, wN) < 1e-10 * 2 * np.pi
+    assert O.linf_error(wE, wN) < 1e-10
+    assert O.linf_error(psiE, pN) < 1e-10
+
+
+def test_turbulence_1000_steps_vs_oracle(S2D):
+    """Decaying turbulence from the seeded k^4 exp(-2(k/10)^2) spectrum,
+    N=128, nu=1e-3, CFL dt, 1000 steps: GPU vs oracle."""
+    n, nu, steps = 128, 1e-3, 1000
+    g = O.get_grid_size(n, n)
+    with S2D(n, nu=nu) as s:
+        s.set_turbulent_velocity(seed=1, spectrum="k4gauss", k0=10.0, tke=0.5)
+        w0, _ = s.get_state()
+        dt = s.compute_time_step(0.5)
+        s.integrate_steps(steps, dt)
+        s.check_finite()
+        wg, _ = s.get_state()
+    wo, po = _oracle_state(w0, g)
+    assert abs(dt - O.cfl_dt(wo, g, 0.5)) < 1e-12 * dt
+    for _ in range(steps):
+        wo, po = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False)
+    err = O.rel_l2(wg, wo)
+    print(f"turbulence N={n}, {steps} steps: rel-L2 = {err:.3e}")
+    assert err < 1e-9
+
+
+def test_graph_replay_equals_single_steps(S2D):
+    n = 64
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 3, decay=0.1)
+    with S2D(n, nu=0.01) as a, S2D(n, nu=0.01) as b:
+        a.set_state(w)
+        b.set_state(w)
+        for _ in range(5):
+            a.integrate_one_step(1e-3)
+        b.integrate_steps(5, 1e-3)
+        wa, _ = a.get_state()
+        wb, _ = b.get_state()
+    assert np.array_equal(wa, wb)
+
+
+def test_host_array_step_equals_device_step(S2D):
+    n = 64
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 4, decay=0.1)
+    with S2D(n, nu=0.01) as s:
+        w1, p1 = s.integrate_one_step_host(w, 1e-3)
+        s.set_state(w)
+        s.integrate_one_step(1e-3)
+        w2, p2 = s.get_state()
+    assert np.array_equal(w1, w2) and np.array_equal(p1, p2)
+
+
+def test_spectrum_minmax_enstrophy_vs_oracle(S2D):
+    n = 128
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 9, decay=0.05)
+    nu = 0.002
+    with S2D(n, nu=nu) as s:
+        s.set_state(w)
+        kb, Ek, tke, eps, enst = s.compute_spectrum()
+        mm = s.minmax_abs()
+        Z = s.enstrophy()
+    wo, po = _oracle_state(w, g)
+    kbo, Eko, tkeo, epso, ensto = O.spectrum_of_vorticity(wo, g, nu)
+    assert len(Ek) == len(Eko) == 2 * 0 + int(math.sqrt(2 * (3 * n // 4) ** 2) + 1.0) + 1
+    assert np.allclose(Ek, Eko, rtol=1e-13, atol=1e-300)
+    for a, b in ((tke, tkeo), (eps, epso), (enst, ensto)):
+        assert abs(a - b) <= 1e-13 * abs(b)
+    mo = O.minmax_abs(wo, po)
+    assert np.allclose(mm, mo, rtol=1e-15, atol=0)
+    assert abs(Z - O.enstrophy(wo, g)) <= 1e-13 * Z
+
+
+def test_forcing_and_drag_vs_oracle(S2D):
+    n, nu, alpha, amp, kf, dt = 64, 1e-3, 0.1, 4.0, 4, 1e-3
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 11, decay=0.1)
+    with S2D(n, nu=nu, alpha=alpha, forcing_amp=amp, forcing_k=kf) as s:
+        s.set_state(w)
+        s.integrate_steps(3, dt)
+        wg, _ = s.get_state()
+    wo, po = _oracle_state(w, g)
+    F = O.kolmogorov_forcing(g, amp, kf)
+    for _ in range(3):
+        wo, po = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False, forcing=F, alpha=alpha)
+    assert O.rel_l2(wg, wo) < 1e-12
+
+
+@pytest.mark.parametrize("n", [64, 256])
+def test_fp32_variant_error_vs_fp64_oracle(S2D, n):
+    """FP32 FFTs and products (1/k^2 in FP64): one RHS within 1e-5 and ten
+    steps within 1e-5 of the FP64 oracle."""
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 21, decay=0.05)
+    nu, dt = 0.005, 1e-3
+    with S2D(n, nu=nu, precision="fp32") as s:
+        s.set_state(w)
+        dW = s.compute_rhs()
+        s.integrate_steps(10, dt)
+        wg, _ = s.get_state()
+    wo, po = _oracle_state(w, g)
+    ref, _ = O.compute_rhs(wo, po, g, nu, round_trip=False)
+    e_rhs = O.rel_l2(dW, O.truncate(ref, g))
+    for _ in range(10):
+        wo, po = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False)
+    e_step = O.rel_l2(wg, wo)
+    print(f"fp32 N={n}: rhs rel-L2 {e_rhs:.2e}, 10 steps rel-L2 {e_step:.2e}")
+    assert e_rhs < 1e-5 and e_step < 1e-5
+
+
+def test_nonfinite_state_is_reported(S2D):
+    from spectral2d_gb300 import S2DError
+    n = 32
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 2)
+    w[1, 1] = np.nan
+    with S2D(n, nu=0.01) as s:
+        s.set_state(w)
+        s.integrate_one_step(1e-3)
+        with pytest.raises(S2DError) as ei:
+            s.check_finite()
+        assert ei.value.code == -3
+        s.check_finite()   # flag was cleared
+
+
+def test_full_size_one_step_vs_oracle(S2D):
+    """The 2048^2 (3072^2 padded) FP64 decaying-turbulence workload: one RK3
+    step from the seeded IC against the oracle, and size-independent checks
+    (energy and enstrophy decay, Hermitian kx=0 column)."""
+    n, nu = 2048, 1e-4
+    g = O.get_grid_size(n, n)
+    O.set_workers(O.cpu_count())
+    with S2D(n, nu=nu) as s:
+        s.set_turbulent_velocity(seed=0, spectrum="k4gauss", k0=10.0, tke=0.5)
+        w0, _ = s.get_state()
+        dt = s.compute_time_step(0.5)
+        _, _, e0, _, _ = s.compute_spectrum()
+        z0 = s.enstrophy()
+        s.integrate_one_step(dt)
+        s.check_finite()
+        w1, _ = s.get_state()
+        _, _, e1, _, _ = s.compute_spectrum()
+        z1 = s.enstrophy()
+    assert abs(e0 - 0.5) < 1e-13
+    assert e1 < e0 and z1 < z0
+    assert np.allclose(w1[1:n // 2 + 1, 0], np.conj(w1[(-np.arange(1, n // 2 + 1)) % g.nyG, 0]),
+                       rtol=0, atol=1e-14 * np.abs(w1).max())
+    wo, po = _oracle_state(w0, g)
+    wr, _ = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False)
+    err = O.rel_l2(w1, wr)
+    print(f"2048^2 one step: rel-L2 {err:.3e}")
+    assert err < 1e-12
