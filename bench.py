@@ -50,25 +50,35 @@ FALLBACK_HBM_GBS = 6800.0
 # ---------------------------------------------------------------------------
 # byte and flop model of one step (shared with the design notes)
 # ---------------------------------------------------------------------------
-def byte_model(n: int, wbytes: int) -> dict:
+def byte_model(n: int, wbytes: int, form: str = "basdevant") -> dict:
     """Compulsory HBM bytes of the fused two-pass step.
     I = (N/2+1)*M*w (half-spectral intermediate), S = (N/2+1)*(N+1)*w
-    (compact state).  Per RHS: K1 reads S, writes 3I; K2 reads 3I, writes 2I;
-    K3 reads 2I and 2S (stage input, w^n), writes S.  B_rhs = 10I + 4S."""
+    (compact state).
+    Conservative form (the reference's): K1 reads S, writes 3I (u, v, w);
+    K2 reads 3I, writes 2I; K3 reads 2I and 2S (stage input, w^n), writes S:
+    B_rhs = 10I + 4S.
+    Basdevant form: K1 writes 2I (u, v); K2 reads 2I, writes 2I:
+    B_rhs = 8I + 4S."""
     m = 3 * n // 2
     I = (n // 2 + 1) * m * wbytes
     S = (n // 2 + 1) * (n + 1) * wbytes
-    per = {"yinv": S + 3 * I, "xpass": 5 * I, "yfwd": 2 * I + 3 * S}
-    return {"I": I, "S": S, "per_kernel": per, "rhs": 10 * I + 4 * S, "step": 3 * (10 * I + 4 * S)}
+    nf = 2 if form == "basdevant" else 3
+    per = {"yinv": S + nf * I, "xpass": (nf + 2) * I, "yfwd": 2 * I + 3 * S}
+    rhs = sum(per.values())
+    return {"I": I, "S": S, "per_kernel": per, "rhs": rhs, "step": 3 * rhs,
+            "step_reference_form": 3 * (10 * I + 4 * S)}
 
 
-def flop_model(n: int) -> dict:
+def flop_model(n: int, form: str = "basdevant") -> dict:
     """benchFFT convention: 2.5*M*log2(M) flops per real 1-D transform of
     length M, i.e. 2.5*M^2*log2(M) per field per direction of an M x M real
-    2-D FFT.  K1: 3 fields (y), K2: 5 fields (x), K3: 2 fields (y)."""
+    2-D FFT.  Basdevant: K1 2 fields (y), K2 4 (x), K3 2 (y); conservative:
+    3, 5, 2."""
     m = 3 * n // 2
     f = 2.5 * m * m * math.log2(m)
-    return {"yinv": 3 * f, "xpass": 5 * f, "yfwd": 2 * f, "rhs": 10 * f, "step": 30 * f}
+    a, b = (2, 4) if form == "basdevant" else (3, 5)
+    return {"yinv": a * f, "xpass": b * f, "yfwd": 2 * f, "rhs": (a + b + 2) * f,
+            "step": 3 * (a + b + 2) * f}
 
 
 # ---------------------------------------------------------------------------
@@ -88,6 +98,22 @@ def hbm_peak(peaks: dict):
         if k in peaks and peaks[k]:
             return float(peaks[k]), "measured"
     return FALLBACK_HBM_GBS, "fallback"
+
+
+def read_traffic(kernel: str, form: str, n: int, precision: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary of that kernel, if there is one."""
+    name = {"yinv": "yinv", "yfwd": "yfwd_rk3",
+            "xpass": "xpass_bas" if form == "basdevant" else "xpass_rhs"}[kernel]
+    p = os.path.join(ROOT, "profiles", f"{name}_n{n}_{precision}.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if "traffic_bytes_per_launch" in line:
+            digits = [c for c in line.split("|") if c.strip().isdigit()]
+            if digits:
+                return int(digits[0].strip())
+    return None
 
 
 class Clocks:
@@ -242,6 +268,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--form", default="basdevant", choices=["basdevant", "conservative"])
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
@@ -265,7 +292,7 @@ def main():
 
     D = Dist(world, local)
     n = args.n
-    s = Spectral2D(n, nu=NU, precision=args.precision, device=local)
+    s = Spectral2D(n, nu=NU, precision=args.precision, device=local, nonlinear_form=args.form)
     s.set_turbulent_velocity(seed=SEED + rank, spectrum="k4gauss", k0=10.0, tke=0.5)
     dt = s.compute_time_step(CFL)
 
@@ -289,8 +316,8 @@ def main():
     ksteps = max(3, min(args.steps, 10))
     launches_per_kernel = 3 * ksteps
     wbytes = 16 if args.precision == "fp64" else 8
-    bm = byte_model(n, wbytes)
-    fm = flop_model(n)
+    bm = byte_model(n, wbytes, args.form)
+    fm = flop_model(n, args.form)
     names = ["yinv", "xpass", "yfwd"]
     avg = {k: kms[i] / launches_per_kernel for i, k in enumerate(names)}
     dom = max(names, key=lambda k: avg[k])
@@ -299,30 +326,30 @@ def main():
     achieved = bm["per_kernel"][dom] / (avg[dom] * 1e-3) / 1e9
     fp64 = probe_fp64_peak(local) if rank == 0 else None
     alu = fm[dom] / (avg[dom] * 1e-3) / 1e12
-    traffic = None
-    tp = os.path.join(ROOT, "profiles", f"traffic_{dom}_n{n}_{args.precision}.json")
-    if os.path.exists(tp):
-        try:
-            traffic = json.load(open(tp)).get("bytes_per_launch")
-        except Exception:
-            traffic = None
+    traffic = read_traffic(dom, args.form, n, args.precision)
 
     # e2e through the reference-facing C-ABI with host arrays
     e2e = None
     if args.e2e_steps > 0:
-        w_host, _ = s.get_state()
+        from spectral2d_gb300.solver import pinned_array
+        w0, _ = s.get_state()
+        w_host = pinned_array(w0.shape)
+        p_host = pinned_array(w0.shape)
+        w_host[...] = w0
+        s.integrate_one_step_host(w_host, dt, p_host, inplace=True)   # warm-up
         s.synchronize()
         D.barrier()
         t0 = time.perf_counter()
         for _ in range(args.e2e_steps):
-            w_host, p_host = s.integrate_one_step_host(w_host, dt)
+            s.integrate_one_step_host(w_host, dt, p_host, inplace=True)
         t1 = time.perf_counter()
         el = D.reduce(t1 - t0, "MAX")
         nbytes = w_host.nbytes
         e2e = {"value": D.reduce(n * n * args.e2e_steps / el / 1e6, "SUM"), "unit": "Mpt*steps/s",
                "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
                "steps": args.e2e_steps,
-               "path": "s2d_integrate_one_step_host (reference-layout wC in; wC, psiC out)"}
+               "path": "s2d_integrate_one_step_host on pinned host arrays "
+                       "(reference-layout wC in; wC, psiC out)"}
 
     if rank == 0:
         line = {
@@ -345,6 +372,8 @@ def main():
                                       "peak_source": "measured FP64 FMA loop on this GPU",
                                       "flops_per_launch": fm[dom]},
                          "step_hbm_frac": bm["step"] / (ms_per_step * 1e-3) / 1e9 / hbm,
+                         "step_hbm_frac_reference_form_bytes": bm["step_reference_form"] / (ms_per_step * 1e-3) / 1e9 / hbm,
+                         "nonlinear_form": args.form,
                          "kernel_ms_per_step": {k: kms[i] / ksteps for i, k in enumerate(names)}},
             "cpu_baseline": cpu,
             "e2e": e2e,

@@ -55,6 +55,16 @@ extern "C" {
 #define S2D_FP64               0   /* the reference's precision (RWPC=C_DOUBLE) */
 #define S2D_FP32               1   /* FP32 FFTs/products; 1/k^2 stays FP64      */
 
+/* ---- form of the nonlinear term ---------------------------------------- *
+ * BASDEVANT: N = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2]  (4 FFTs per RHS).
+ * CONSERVATIVE: N = -i kx F[u w] - i ky F[v w]         (5 FFTs per RHS), the
+ * reference's form (src/Spectral.F90:424-479).  The two are the same
+ * polynomial identity for divergence-free fields, and on the 3/2 grid the
+ * only aliased products that reach retained modes (|k| = nx/2 on an axis)
+ * are multiplied by zero in both, so they agree to round-off.            */
+#define S2D_NL_BASDEVANT       0
+#define S2D_NL_CONSERVATIVE    1
+
 /* ---- initial-condition spectra ----------------------------------------- */
 #define S2D_SPECTRUM_SCHUMANN  0   /* 1.5 urms^2 (k/k0) exp(-k/k0), SetIC.F90:374-381 */
 #define S2D_SPECTRUM_K4_GAUSS  1   /* k^4 exp(-2 (k/k0)^2)                             */
@@ -80,6 +90,7 @@ typedef struct s2d_config {
     double  forcing_amp;     /* vorticity source amp*cos(kf*y) (0 = off)       */
     int32_t forcing_k;       /* kf                                             */
     int32_t device;          /* CUDA device ordinal                            */
+    int32_t nonlinear_form;  /* S2D_NL_BASDEVANT (default) or S2D_NL_CONSERVATIVE */
 } s2d_config;
 
 typedef struct s2d_handle s2d_handle;

@@ -29,6 +29,8 @@ S2D_FP64 = 0
 S2D_FP32 = 1
 S2D_SPECTRUM_SCHUMANN = 0
 S2D_SPECTRUM_K4_GAUSS = 1
+S2D_NL_BASDEVANT = 0
+S2D_NL_CONSERVATIVE = 1
 
 
 class S2DGrid(C.Structure):
@@ -40,7 +42,8 @@ class S2DGrid(C.Structure):
 class S2DConfig(C.Structure):
     _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("dealias", C.c_int32),
                 ("precision", C.c_int32), ("nu", C.c_double), ("alpha", C.c_double),
-                ("forcing_amp", C.c_double), ("forcing_k", C.c_int32), ("device", C.c_int32)]
+                ("forcing_amp", C.c_double), ("forcing_k", C.c_int32), ("device", C.c_int32),
+                ("nonlinear_form", C.c_int32)]
 
 
 class S2DError(RuntimeError):

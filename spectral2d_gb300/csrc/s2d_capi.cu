@@ -148,8 +148,9 @@ int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_gro
 template <typename T>
 int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
     const Dims& d = h->d;
+    const bool bas = h->ph.form == S2D_NL_BASDEVANT;
     FieldSet fs{};
-    fs.nf = 3;
+    fs.nf = bas ? 2 : 3;
     fs.op[0] = OP_U;
     fs.op[1] = OP_V;
     fs.op[2] = OP_W;
@@ -160,7 +161,8 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
     if (ev) S2D_CUDA(cudaEventRecord(ev[0], h->stream));
     S2D_CUDA(Kern<T>::yinv(d, win, h->rk2, fs, h->tw, h->stream, h->L_yinv));
     if (ev) S2D_CUDA(cudaEventRecord(ev[1], h->stream));
-    S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
+    if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow));
+    else S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
     if (ev) S2D_CUDA(cudaEventRecord(ev[2], h->stream));
     S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, stage, dt, h->ph, h->tw, h->flags,
                                h->stream, h->L_yfwd));
@@ -337,6 +339,11 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
     d.Tg = d.M / kElemsPerThread;
     h->ph.nu = cfg->nu;
     h->ph.alpha = cfg->alpha;
+    h->ph.form = cfg->nonlinear_form;
+    if (h->ph.form != S2D_NL_BASDEVANT && h->ph.form != S2D_NL_CONSERVATIVE) {
+        delete h;
+        return fail(S2D_ERR_INVALID, "nonlinear_form must be S2D_NL_BASDEVANT or S2D_NL_CONSERVATIVE");
+    }
     h->ph.fk = cfg->forcing_amp != 0.0 ? cfg->forcing_k : 0;
     if (h->ph.fk < 0 || h->ph.fk > d.K) {
         delete h;
@@ -407,23 +414,24 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess)
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
-    // launch shapes
+    // launch shapes: about 256 threads per CTA so that at least two CTAs
+    // share an SM and one CTA's barrier phases overlap the other's FP64 work
     const size_t tb = (size_t)d.M * h->vsz;
+    const int tgt = 256;
     int rr;
-    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_yinv, "inverse y-pass")) != S2D_OK) return bail(rr);
-    if ((rr = pick_launch(h, d.Tg, 2 * tb, 512, &h->L_xpass, "x-pass")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_yinv, "inverse y-pass")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, &h->L_xpass, "x-pass")) != S2D_OK) return bail(rr);
     {
-        // forward y-pass: G columns x 2 fields; up to two transforms at a time
+        // forward y-pass: G columns x 2 fields, run in rounds of c transforms
         Launch L{};
-        if ((rr = pick_launch(h, d.Tg, 2 * tb, 512, &L, "forward y-pass")) != S2D_OK) return bail(rr);
-        const int conc = std::max(1, std::min(2 * L.G, 512 / d.Tg));
-        int c = conc;
+        if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, &L, "forward y-pass")) != S2D_OK) return bail(rr);
+        int c = std::max(1, std::min(2 * L.G, tgt / d.Tg));
         while ((2 * L.G) % c) --c;
         L.threads = c * d.Tg;
         h->L_yfwd = L;
     }
-    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
-    if ((rr = pick_launch(h, d.Tg, tb, 512, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
     *out = h;

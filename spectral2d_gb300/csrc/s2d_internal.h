@@ -42,6 +42,7 @@ struct Phys {
     double alpha;     // linear drag coefficient
     int fk;           // forcing wavenumber (0 = none)
     double f_re, f_im;  // coefficient at (kx=0, ky=+fk); conjugate at -fk
+    int form;         // S2D_NL_BASDEVANT or S2D_NL_CONSERVATIVE
 };
 
 // Spectral operators applied when a column is read for the inverse y-pass.
@@ -77,6 +78,8 @@ struct Kern {
                             const void* tw, cudaStream_t st, const Launch& L);
     static cudaError_t xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw, const void* tw,
                                  cudaStream_t st, const Launch& L);
+    static cudaError_t xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw, cudaStream_t st,
+                                 const Launch& L);
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
                                 void* Sdw, int stage, double dt, const Phys& ph, const void* tw,
                                 unsigned int* flags, cudaStream_t st, const Launch& L);

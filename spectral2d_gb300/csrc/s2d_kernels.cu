@@ -88,7 +88,15 @@ __global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* 
     const int kx0 = cg * G;
     const int kx = kx0 + g;
     const bool active = kx < d.KX;
-    const int op = fs.op[f];
+    // select without dynamic indexing of the parameter struct
+    int op;
+    void* outp;
+    switch (f) {
+        case 0: op = fs.op[0]; outp = fs.out[0]; break;
+        case 1: op = fs.op[1]; outp = fs.out[1]; break;
+        case 2: op = fs.op[2]; outp = fs.out[2]; break;
+        default: op = fs.op[3]; outp = fs.out[3]; break;
+    }
     VT* buf = bufs + (size_t)g * d.M;
 
     const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
@@ -108,7 +116,7 @@ __global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* 
     }
     fft_run<true>(buf, d, lane, tw);
 
-    VT* out = reinterpret_cast<VT*>(fs.out[f]);
+    VT* out = reinterpret_cast<VT*>(outp);
     const int gtot = min(G, d.KX - kx0);
     for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
         const int y = idx / G;
@@ -201,8 +209,40 @@ __global__ void __launch_bounds__(512) k_xpass_rhs(Dims d, typename Vec<T>::t* I
 }
 
 // ------------------------------------------------------------------------
+// K2 (Basdevant form): one physical row per transform.  z = u + i v from
+// one inverse FFT, then p = u v + i (v^2 - u^2), one forward FFT, split into
+// the normalised half spectra of u v (-> Iu row) and v^2 - u^2 (-> Iv row).
+// Two complex FFTs per row instead of 2.5; omega is not needed in physical
+// space.
+// ------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(512) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+                                                    const typename Vec<T>::t* __restrict__ tw, int G,
+                                                    T scale) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    VT* Z = bufs + (size_t)g * d.M;
+    VT* urow = Iu + (size_t)(active ? y : 0) * d.ldI;
+    VT* vrow = Iv + (size_t)(active ? y : 0) * d.ldI;
+    build_pair(Z, urow, vrow, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);
+    for (int n = lane; n < d.M; n += d.Tg) {
+        const VT z = Z[n];
+        Z[n] = mk<VT>(z.x * z.y, z.y * z.y - z.x * z.x);
+    }
+    fft_run<false>(Z, d, lane, tw);
+    extract_pair(Z, urow, vrow, d, lane, active, scale);
+}
+
+// ------------------------------------------------------------------------
 // K3: forward y-pass of the two products + RK3 stage epilogue.
-// Block = 2G transforms (G columns x {u*w, v*w}).
+// Block = 2G transforms (G columns x two product fields: {u v, v^2 - u^2}
+// in the Basdevant form, {u w, v w} in the conservative form).
 //   stage 1: S1 = S0 + dt dW                    (w_in = S0)
 //   stage 2: S1 = 3/4 S0 + 1/4 S1 + dt/4 dW      (w_in = S1)
 //   stage 3: S0 = S0/3 + 2/3 S1 + 2dt/3 dW       (w_in = S1)
@@ -262,9 +302,17 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
             const VT win = (stage <= 1) ? w0 : S1[off];
             const T fkx = (T)kx, fky = (T)ky;
             const T visc = tnu * (T)kk;
-            // dW = -i kx Nx - i ky Ny - nu k^2 w   (src/Spectral.F90:464-479)
-            T dwx = fkx * nx.y + fky * ny.y - visc * win.x;
-            T dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+            T dwx, dwy;
+            if (ph.form == S2D_NL_BASDEVANT) {
+                // dW = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2] - nu k^2 w
+                const T c1 = (T)(kx * kx - ky * ky), c2 = (T)(kx * ky);
+                dwx = c1 * nx.x + c2 * ny.x - visc * win.x;
+                dwy = c1 * nx.y + c2 * ny.y - visc * win.y;
+            } else {
+                // dW = -i kx F[uw] - i ky F[vw] - nu k^2 w  (src/Spectral.F90:464-479)
+                dwx = fkx * nx.y + fky * ny.y - visc * win.x;
+                dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+            }
             if (talpha != (T)0) {
                 dwx -= talpha * win.x;
                 dwy -= talpha * win.y;
@@ -608,6 +656,16 @@ cudaError_t Kern<T>::xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw
 }
 
 template <typename T>
+cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw, cudaStream_t st,
+                               const Launch& L) {
+    using VT = typename Vec<T>::t;
+    const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
+    k_xpass_bas<T><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G,
+                                                                       scale);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1, void* Sdw,
                               int stage, double dt, const Phys& ph, const void* tw, unsigned int* flags,
                               cudaStream_t st, const Launch& L) {
@@ -721,6 +779,8 @@ cudaError_t configure_kernels(int max_smem_optin) {
     S2D_SET(k_yinv<float>);
     S2D_SET(k_xpass_rhs<double>);
     S2D_SET(k_xpass_rhs<float>);
+    S2D_SET(k_xpass_bas<double>);
+    S2D_SET(k_xpass_bas<float>);
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
     S2D_SET(k_xinv_cfl<double>);

@@ -15,6 +15,7 @@ Every call goes through ``libspectral2d_gb300.so``; there is no CPU path.
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -22,6 +23,7 @@ from . import _lib as L
 
 _FP = {"fp64": L.S2D_FP64, "fp32": L.S2D_FP32}
 _SPEC = {"schumann": L.S2D_SPECTRUM_SCHUMANN, "k4gauss": L.S2D_SPECTRUM_K4_GAUSS}
+_FORM = {"basdevant": L.S2D_NL_BASDEVANT, "conservative": L.S2D_NL_CONSERVATIVE}
 
 
 def _dptr(a: np.ndarray):
@@ -45,6 +47,18 @@ def turbulent_ic_host(nx: int, seed: int, spectrum: str = "k4gauss", k0: float =
     return w
 
 
+def pinned_array(shape, dtype=np.complex128) -> np.ndarray:
+    """Zeroed page-locked host array (freed when the array is collected)."""
+    nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+    ptr = C.c_void_p()
+    L.check(L.lib().s2d_host_alloc(nbytes, C.byref(ptr)))
+    buf = (C.c_byte * nbytes).from_address(ptr.value)
+    weakref.finalize(buf, L.lib().s2d_host_free, C.c_void_p(ptr.value))
+    arr = np.frombuffer(buf, dtype=dtype).reshape(shape)
+    arr[...] = 0
+    return arr
+
+
 def probe_fp64_peak(device: int = 0) -> float:
     """Measured FP64 FMA throughput of the GPU, TFLOP/s."""
     v = C.c_double()
@@ -58,11 +72,12 @@ class Spectral2D:
     def __init__(self, nx: int, ny: int | None = None, nu: float = 0.005,
                  precision: str = "fp64", alpha: float = 0.0, forcing_amp: float = 0.0,
                  forcing_k: int = 0, device: int = 0,
-                 dealias: int = L.S2D_DEALIAS_3_2_RULE):
+                 dealias: int = L.S2D_DEALIAS_3_2_RULE, nonlinear_form: str = "basdevant"):
         self._L = L.lib()
         cfg = L.S2DConfig(nx=nx, ny=ny if ny is not None else nx, dealias=dealias,
                           precision=_FP[precision], nu=nu, alpha=alpha,
-                          forcing_amp=forcing_amp, forcing_k=forcing_k, device=device)
+                          forcing_amp=forcing_amp, forcing_k=forcing_k, device=device,
+                          nonlinear_form=_FORM[nonlinear_form])
         h = C.c_void_p()
         L.check(self._L.s2d_create(C.byref(cfg), C.byref(h)))
         self._h = h
@@ -124,10 +139,18 @@ class Spectral2D:
     def integrate_steps(self, n: int, dt: float) -> None:
         L.check(self._L.s2d_integrate_steps(self._h, n, dt))
 
-    def integrate_one_step_host(self, wC: np.ndarray, dt: float):
-        """``IntegrateOneStep`` on host arrays: returns the new ``(wC, psiC)``."""
-        w = np.array(wC, dtype=np.complex128, order="C", copy=True)
-        p = self._new()
+    def integrate_one_step_host(self, wC: np.ndarray, dt: float, psiC: np.ndarray | None = None,
+                                inplace: bool = False):
+        """``IntegrateOneStep`` on host arrays: returns the new ``(wC, psiC)``.
+        With ``inplace`` the arrays given (e.g. from :func:`pinned_array`) are
+        updated directly, as the reference updates its wC/psiC."""
+        if inplace:
+            assert wC.flags.c_contiguous and wC.dtype == np.complex128 and wC.shape == self.shape
+            w = wC
+        else:
+            w = np.array(wC, dtype=np.complex128, order="C", copy=True)
+        p = psiC if psiC is not None else self._new()
+        assert p.flags.c_contiguous and p.dtype == np.complex128 and p.shape == self.shape
         L.check(self._L.s2d_integrate_one_step_host(self._h, _dptr(w.view(np.float64)),
                                                     _dptr(p.view(np.float64)),
                                                     *self.shape[::-1], dt))

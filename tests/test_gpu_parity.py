@@ -65,6 +65,27 @@ def test_rhs_vs_oracle(S2D, n):
     assert O.rel_l2(dW, O.truncate(ref, g)) < 1e-13
 
 
+@pytest.mark.parametrize("n", [8, 64, 256])
+def test_conservative_form_vs_oracle_and_basdevant(S2D, n):
+    """The reference's own form of the nonlinear term on the GPU, and its
+    agreement with the default (Basdevant) form."""
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 300 + n)
+    with S2D(n, nu=0.01, nonlinear_form="conservative") as a, S2D(n, nu=0.01) as b:
+        a.set_state(w)
+        b.set_state(w)
+        da, db = a.compute_rhs(), b.compute_rhs()
+        a.integrate_steps(3, 1e-3)
+        b.integrate_steps(3, 1e-3)
+        wa, _ = a.get_state()
+        wb, _ = b.get_state()
+    wo, po = _oracle_state(w, g)
+    ref, _ = O.compute_rhs(wo, po, g, 0.01, round_trip=False)
+    assert O.rel_l2(da, O.truncate(ref, g)) < 1e-13
+    assert O.rel_l2(db, da) < 1e-13
+    assert O.rel_l2(wb, wa) < 1e-13
+
+
 @pytest.mark.parametrize("n", [16, 64, 256])
 def test_one_step_vs_oracle(S2D, n):
     g = O.get_grid_size(n, n)
