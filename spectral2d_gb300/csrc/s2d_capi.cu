@@ -74,6 +74,51 @@ void twiddle(long long r, long long M, double* c, double* s) {
     *s = -(double)S;  // forward sign
 }
 
+// exp(-2 pi i m / M) = i^q * c * (1 + i t) with |t| <= 1 (needs 4 | M):
+// q0 = nearest quarter turn of m, residual angle th in [-pi/4, pi/4].
+void twiddle_fma(long long m, long long M, int* q, long double* c, long double* t) {
+    const long double PI = 3.141592653589793238462643383279502884L;
+    m %= M;
+    if (m < 0) m += M;
+    const long long q0 = (4 * m + M / 2) / M;
+    const long long mr = m - q0 * (M / 4);
+    const long double th = 2.0L * PI * (long double)mr / (long double)M;
+    *q = (int)((4 - (q0 % 4)) % 4);   // (-i)^q0 = i^-q0
+    *c = cosl(th);
+    *t = -sinl(th) / cosl(th);
+}
+
+// TwEnt blocks of every pass after the first with radix 4 or 2.
+template <typename T>
+std::vector<TwEnt<T>> fma_tables(Dims* d) {
+    std::vector<TwEnt<T>> tab;
+    int Ns = 1;
+    for (int p = 0; p < d->npass; ++p) {
+        const int R = d->radix[p];
+        d->twoff[p] = -1;
+        if (p > 0 && (R == 4 || R == 2)) {
+            d->twoff[p] = (int)tab.size();
+            const long long step = d->M / (Ns * R);
+            for (int k = 0; k < Ns; ++k) {
+                TwEnt<T> e{};
+                int qs[4] = {0, 0, 0, 0};
+                long double cs[4] = {1, 1, 1, 1}, ts[4] = {0, 0, 0, 0};
+                for (int r = 1; r < R; ++r) twiddle_fma((long long)r * k * step, d->M, &qs[r], &cs[r], &ts[r]);
+                e.t1 = (T)ts[1];
+                e.t2 = (T)ts[2];
+                e.t3 = (T)ts[3];
+                e.c1 = (T)cs[1];
+                e.c2 = (T)cs[2];
+                e.r31 = (T)(cs[3] / cs[1]);
+                e.q = qs[1] | (qs[2] << 2) | (qs[3] << 4);
+                tab.push_back(e);
+            }
+        }
+        Ns *= R;
+    }
+    return tab;
+}
+
 bool factor_plan(int M, Dims* d) {
     int m = M, a = 0, b = 0;
     while (m % 2 == 0) { m /= 2; ++a; }
@@ -390,7 +435,15 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
     h->I[1] = (char*)h->Ibase + h->Ibytes;
     h->I[2] = (char*)h->Ibase + 2 * h->Ibytes;
     S2D_ALLOC(h->rk2, (size_t)d.KX * d.ldS * sizeof(double));
-    S2D_ALLOC(h->tw, (size_t)d.M * h->vsz);
+    // complex twiddles (M entries) followed by the FMA-form blocks
+    std::vector<TwEnt<double>> tabd;
+    std::vector<TwEnt<float>> tabf;
+    if (h->prec == S2D_FP64) tabd = fma_tables<double>(&d);
+    else tabf = fma_tables<float>(&d);
+    d.tab_bytes = (long long)(((size_t)d.M * h->vsz + 63) / 64 * 64);
+    const size_t tab_size = h->prec == S2D_FP64 ? tabd.size() * sizeof(TwEnt<double>)
+                                                : tabf.size() * sizeof(TwEnt<float>);
+    S2D_ALLOC(h->tw, (size_t)d.tab_bytes + tab_size + 64);
     S2D_ALLOC(h->flags, 64);
     S2D_ALLOC(h->red64, 8 * sizeof(unsigned long long));
     h->dscratch_n = std::max<size_t>(d.K + 1, 4096);
@@ -410,6 +463,9 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
             if (cudaMemcpy(h->tw, twf.data(), twf.size() * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
                 return bail(fail(S2D_ERR_CUDA, "twiddle upload failed"));
         }
+        const void* src = h->prec == S2D_FP64 ? (const void*)tabd.data() : (const void*)tabf.data();
+        if (tab_size && cudaMemcpy((char*)h->tw + d.tab_bytes, src, tab_size, cudaMemcpyHostToDevice) != cudaSuccess)
+            return bail(fail(S2D_ERR_CUDA, "twiddle table upload failed"));
     }
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess)
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));

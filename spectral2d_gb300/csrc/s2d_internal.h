@@ -23,6 +23,19 @@ namespace s2d {
 constexpr int kMaxPasses = 16;
 constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
 
+// Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
+// w_r = i^q_r * c_r * (1 + i t_r) with |t_r| <= 1, so that x*w_r costs two
+// FMAs on (x*i^q_r) and the scale c_r is folded into the butterfly's
+// additions (t0 = a + c2*C, E = B + (c3/c1)*D, y = t + c1*E ...).
+// q packs q_1 | q_2 << 2 | q_3 << 4.
+template <typename T>
+struct __align__(16) TwEnt {
+    T t1, t2, t3;
+    T c1, c2, r31;  // c_1, c_2, c_3 / c_1
+    int q;
+    int pad;
+};
+
 // Geometry and FFT plan shared by every kernel of one handle.
 struct Dims {
     int K;      // nx/2: largest retained |kx|, |ky|
@@ -34,6 +47,10 @@ struct Dims {
     int Tg;     // threads per transform = M / kElemsPerThread
     int npass;  // FFT passes
     int radix[kMaxPasses];
+    // per pass: offset (entries) of its TwEnt block, -1 if the pass uses the
+    // plain complex table (first pass, or a radix-3 pass after the first)
+    int twoff[kMaxPasses];
+    long long tab_bytes;  // byte offset of the TwEnt table after the complex table
 };
 
 // Terms of dW beyond the reference's (drag and a Kolmogorov source).
