@@ -207,6 +207,36 @@ S2D_API int s2d_host_free(void* ptr);
  * in TFLOP/s (2 flops per FMA). */
 S2D_API int s2d_probe_fp64_peak(int32_t device, double* tflops);
 
+/* ---- allocation-free right-hand side ----------------------------------- *
+ * No counterpart in the reference.  For callers that must not allocate
+ * device memory -- host codes whose device memory belongs to another
+ * runtime or a fixed pool, plug-ins that may only use the buffers they are
+ * handed, or code paths where an allocation (and the device synchronisation
+ * it can bring) is not allowed.
+ *
+ * dW = ComputeRHS(wC) (src/Spectral.F90:396-482, Basdevant form, viscosity
+ * nu, no drag or forcing) for one grid of nx = ny points, on the current CUDA
+ * device.  wC_dev and dW_dev are DEVICE arrays in the reference layout
+ * (cISize, nyG) complex128, owned by the caller; modes of wC outside
+ * |k| <= nx/2 are ignored, modes of dW outside it are written as zero.
+ * stream is a cudaStream_t (NULL = the legacy default stream); the call is
+ * asynchronous on it.
+ *
+ * All scratch lives in one static device array of
+ * S2D_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * the process exits; the call makes no cudaMalloc, cudaFree or other
+ * allocation.  nx must be a multiple of 8 and at most S2D_NOALLOC_MAX_NX,
+ * else S2D_ERR_INVALID.  The first call on a device resolves the array's
+ * device address (cudaGetSymbolAddress) and sets kernel attributes: make it
+ * before any stream capture.  Every call shares the one array, so calls that
+ * overlap on the GPU (other streams, other host threads) race; serialise
+ * them.  Errors are reported by the return code only.
+ */
+#define S2D_NOALLOC_MAX_NX          256
+#define S2D_NOALLOC_SCRATCH_BYTES   (3u << 20)
+S2D_API int s2d_compute_rhs_noalloc(int32_t nx, double nu, const double* wC_dev, double* dW_dev,
+                                    void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -86,6 +86,7 @@ SIGNATURES = {
     "s2d_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "s2d_host_free": (C.c_int, [C.c_void_p]),
     "s2d_probe_fp64_peak": (C.c_int, [C.c_int32, _dp]),
+    "s2d_compute_rhs_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
 _lib = None
