@@ -207,6 +207,34 @@ S2D_API int s2d_host_free(void* ptr);
  * in TFLOP/s (2 flops per FMA). */
 S2D_API int s2d_probe_fp64_peak(int32_t device, double* tflops);
 
+/* ---- ensembles of independent runs (no reference counterpart) ----------- *
+ * A batch advances nruns independent simulations of uneven sizes (nx a power
+ * of two in [16, 2048]; each run its own nu, drag and forcing; one precision
+ * and device for all) with one persistent kernel launch per RK3 stage, the
+ * three launches of a step replayed from a CUDA graph.  Each run is an
+ * ordinary handle (s2d_batch_run) on the batch's stream, so the single-run
+ * calls (set/get state, ICs, CFL, spectrum) work on it; they are ordered
+ * with the batch's launches. */
+typedef struct s2d_batch s2d_batch;
+S2D_API int s2d_batch_create(int32_t nruns, const s2d_config* cfgs, s2d_batch** out);
+S2D_API void s2d_batch_destroy(s2d_batch* b);
+S2D_API int s2d_batch_size(const s2d_batch* b);
+S2D_API int s2d_batch_run(s2d_batch* b, int32_t i, s2d_handle** h);
+/* per-run time steps dt[nruns] used by the following steps */
+S2D_API int s2d_batch_set_dt(s2d_batch* b, const double* dt);
+/* n RK3 steps of every run (asynchronous) */
+S2D_API int s2d_batch_integrate_steps(s2d_batch* b, int32_t n);
+/* n steps timed with CUDA events on the batch stream */
+S2D_API int s2d_batch_time_steps(s2d_batch* b, int32_t n, double* ms);
+/* S2D_ERR_TIMEOUT if a dependency wait of the persistent kernel gave up,
+ * S2D_ERR_NONFINITE if a run produced NaN/Inf; clears the flags. */
+S2D_API int s2d_batch_status(s2d_batch* b);
+S2D_API int s2d_batch_synchronize(s2d_batch* b);
+/* Autotuner: times the candidate tile schedules (128/256/512 threads per CTA,
+ * i.e. transforms per tile, and 1-4 CTAs per SM) on this ensemble, keeps the
+ * fastest and restores every run's state.  Any output may be NULL. */
+S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm, double* ms_per_step);
+
 /* ---- allocation-free right-hand side ----------------------------------- *
  * No counterpart in the reference.  For callers that must not allocate
  * device memory -- host codes whose device memory belongs to another

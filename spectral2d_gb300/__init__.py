@@ -6,6 +6,6 @@ hand-written CUDA kernels in ``libspectral2d_gb300.so`` behind the C-ABI of
 """
 
 from ._lib import S2DError, lib  # noqa: F401
-from .solver import Spectral2D, get_grid_size, probe_fp64_peak, turbulent_ic_host  # noqa: F401
+from .solver import Ensemble, Spectral2D, get_grid_size, probe_fp64_peak, turbulent_ic_host  # noqa: F401
 
-__all__ = ["Spectral2D", "get_grid_size", "turbulent_ic_host", "probe_fp64_peak", "S2DError", "lib"]
+__all__ = ["Spectral2D", "Ensemble", "get_grid_size", "turbulent_ic_host", "probe_fp64_peak", "S2DError", "lib"]

@@ -87,6 +87,16 @@ SIGNATURES = {
     "s2d_host_free": (C.c_int, [C.c_void_p]),
     "s2d_probe_fp64_peak": (C.c_int, [C.c_int32, _dp]),
     "s2d_compute_rhs_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "s2d_batch_create": (C.c_int, [C.c_int32, C.POINTER(S2DConfig), C.POINTER(C.c_void_p)]),
+    "s2d_batch_destroy": (None, [C.c_void_p]),
+    "s2d_batch_size": (C.c_int, [C.c_void_p]),
+    "s2d_batch_run": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "s2d_batch_set_dt": (C.c_int, [C.c_void_p, _dp]),
+    "s2d_batch_integrate_steps": (C.c_int, [C.c_void_p, C.c_int32]),
+    "s2d_batch_time_steps": (C.c_int, [C.c_void_p, C.c_int32, _dp]),
+    "s2d_batch_status": (C.c_int, [C.c_void_p]),
+    "s2d_batch_synchronize": (C.c_int, [C.c_void_p]),
+    "s2d_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
 }
 
 _lib = None

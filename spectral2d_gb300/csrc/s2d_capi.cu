@@ -141,35 +141,6 @@ int kIntMaxBins(int kxMG, int kyMG) {
 
 }  // namespace
 
-struct s2d_handle {
-    s2d_config cfg;
-    s2d_grid grid;
-    Dims d;
-    Phys ph;
-    int prec;            // S2D_FP64 / S2D_FP32
-    size_t vsz;          // bytes of one complex element of the state
-    int device;
-    cudaStream_t stream = nullptr;
-    void* S0 = nullptr;  // w^n
-    void* S1 = nullptr;  // stage vorticity
-    void* Sdw = nullptr; // dW for compute_rhs (lazily allocated)
-    void* Ibase = nullptr;
-    void* I[3] = {nullptr, nullptr, nullptr};
-    size_t Ibytes = 0;
-    double* rk2 = nullptr;
-    void* tw = nullptr;
-    double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
-    size_t ref_bytes = 0;          // bytes of one reference-layout array
-    unsigned int* flags = nullptr;
-    unsigned long long* red64 = nullptr;  // 8 reduction words
-    double* dscratch = nullptr;           // spectrum / partial sums
-    size_t dscratch_n = 0;
-    Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    double graph_dt = 0.0;
-    int max_smem = 0;
-};
 
 namespace {
 
@@ -209,7 +180,7 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
     if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow));
     else S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
     if (ev) S2D_CUDA(cudaEventRecord(ev[2], h->stream));
-    S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, stage, dt, h->ph, h->tw, h->flags,
+    S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->tw, h->flags,
                                h->stream, h->L_yfwd));
     if (ev) S2D_CUDA(cudaEventRecord(ev[3], h->stream));
     return S2D_OK;
@@ -306,6 +277,8 @@ int spectrum_impl(s2d_handle* h, std::vector<double>& Ek) {
 
 int s2d::handle_nx(const s2d_handle* h) { return h->cfg.nx; }
 
+int s2d::set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 // ============================================================================
 // C-ABI
 // ============================================================================
@@ -346,7 +319,11 @@ S2D_API int s2d_get_grid_size(int32_t nx, int32_t ny, int32_t dealias, s2d_grid*
     return S2D_OK;
 }
 
-S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
+S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) { return s2d::create_handle(cfg, nullptr, out); }
+
+}  // extern "C"
+
+int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handle** out) {
     if (!cfg || !out) return fail(S2D_ERR_INVALID, "null argument");
     *out = nullptr;
     if (cfg->dealias != S2D_DEALIAS_3_2_RULE)
@@ -419,8 +396,12 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
             configured[h->device] = true;
         }
     }
-    if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess)
+    if (ext_stream) {
+        h->stream = ext_stream;
+        h->own_stream = false;
+    } else if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
         return bail(fail(S2D_ERR_CUDA, "stream creation failed"));
+    }
 
     const size_t state_bytes = (size_t)d.KX * d.ldS * h->vsz;
     h->Ibytes = (size_t)d.M * d.ldI * h->vsz;
@@ -494,6 +475,8 @@ S2D_API int s2d_create(const s2d_config* cfg, s2d_handle** out) {
     return S2D_OK;
 }
 
+extern "C" {
+
 S2D_API void s2d_destroy(s2d_handle* h) {
     if (!h) return;
     cudaSetDevice(h->device);
@@ -502,7 +485,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     void* ptrs[] = {h->S0, h->S1, h->Sdw, h->Ibase, h->rk2, h->tw, h->ref_stage, h->flags, h->red64, h->dscratch};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
 }
 

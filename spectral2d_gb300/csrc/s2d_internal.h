@@ -98,8 +98,8 @@ struct Kern {
     static cudaError_t xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw, cudaStream_t st,
                                  const Launch& L);
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
-                                void* Sdw, int stage, double dt, const Phys& ph, const void* tw,
-                                unsigned int* flags, cudaStream_t st, const Launch& L);
+                                void* Sdw, const void* src, int stage, double dt, const Phys& ph,
+                                const void* tw, unsigned int* flags, cudaStream_t st, const Launch& L);
     static cudaError_t ref_to_compact(const Dims& d, const double* ref, int C, void* S,
                                       cudaStream_t st);
     static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
@@ -121,8 +121,51 @@ struct Kern {
     static size_t smem_limit_yinv();
 };
 
+}  // namespace s2d
+
+// One simulation: configuration, plan, launch shapes and device buffers.
+struct s2d_handle {
+    s2d_config cfg;
+    s2d_grid grid;
+    s2d::Dims d;
+    s2d::Phys ph;
+    int prec;            // S2D_FP64 / S2D_FP32
+    size_t vsz;          // bytes of one complex element of the state
+    int device;
+    cudaStream_t stream = nullptr;
+    bool own_stream = true;
+    void* S0 = nullptr;  // w^n
+    void* S1 = nullptr;  // stage vorticity
+    void* Sdw = nullptr; // dW for compute_rhs (lazily allocated)
+    void* src = nullptr; // optional additive source of dW (compact layout), e.g. a closure term
+    void* Ibase = nullptr;
+    void* I[3] = {nullptr, nullptr, nullptr};
+    size_t Ibytes = 0;
+    double* rk2 = nullptr;
+    void* tw = nullptr;
+    double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
+    size_t ref_bytes = 0;          // bytes of one reference-layout array
+    unsigned int* flags = nullptr;
+    unsigned long long* red64 = nullptr;  // 8 reduction words
+    double* dscratch = nullptr;           // spectrum / partial sums
+    size_t dscratch_n = 0;
+    s2d::Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    double graph_dt = 0.0;
+    int max_smem = 0;
+};
+
+namespace s2d {
+
+// s2d_create with an optional external stream (not owned by the handle).
+int create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handle** out);
+
 // Shared-memory attribute setup (called once per process and device).
 cudaError_t configure_kernels(int max_smem_optin);
+
+// Record msg as this thread's last error (s2d_last_error) and return code.
+int set_error(int code, const char* msg);
 
 // nx of a handle (the IC generator works on host arrays of that grid).
 int handle_nx(const s2d_handle* h);

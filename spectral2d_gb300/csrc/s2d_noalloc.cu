@@ -241,7 +241,7 @@ S2D_API int s2d_compute_rhs_noalloc(int32_t nx, double nu, const double* wC_dev,
     if (Kern<double>::ref_to_compact(d, wC_dev, C, B + c.S, st) != cudaSuccess ||
         Kern<double>::yinv(d, B + c.S, (const double*)(B + c.rk2), fs, B + c.tw, st, Ly) != cudaSuccess ||
         Kern<double>::xpass_bas(d, B + c.I0, B + c.I1, B + c.tw, st, Lx) != cudaSuccess ||
-        Kern<double>::yfwd_rk3(d, B + c.I0, B + c.I1, B + c.S, B + c.S, B + c.Sdw, 0, 0.0, ph, B + c.tw,
+        Kern<double>::yfwd_rk3(d, B + c.I0, B + c.I1, B + c.S, B + c.S, B + c.Sdw, nullptr, 0, 0.0, ph, B + c.tw,
                                (unsigned int*)(B + c.flags), st, Lf) != cudaSuccess ||
         Kern<double>::compact_to_ref(d, B + c.Sdw, C, dW_dev, nullptr, st) != cudaSuccess)
         return err(S2D_ERR_CUDA, "kernel launch failed");

@@ -1,0 +1,287 @@
+// s2d_step.cuh -- bodies of the three right-hand-side kernels, shared by the
+// single-run kernels (s2d_kernels.cu) and the persistent ensemble kernel
+// (s2d_batch.cu).  A body processes one "block" (a tile of columns or rows)
+// with all threads of the calling CTA and the shared memory it is given.
+//
+// Intermediates are read with ld.global.cg (L2, not L1): in the persistent
+// kernel they were written by other CTAs of the same launch.
+#pragma once
+
+#include "s2d_fft.cuh"
+#include "s2d_internal.h"
+
+namespace s2d {
+
+__device__ __forceinline__ bool bits_nonfinite(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b & 0x7FF0000000000000ULL) == 0x7FF0000000000000ULL;
+}
+__device__ __forceinline__ bool bits_nonfinite(float x) {
+    const unsigned int b = (unsigned int)__float_as_int(x);
+    return (b & 0x7F800000u) == 0x7F800000u;
+}
+
+// compact row jc -> ky
+__device__ __forceinline__ int ky_of_jc(const Dims& d, int jc) { return jc <= d.K ? jc : jc - d.KY; }
+
+// Apply a spectral operator to omega of mode (kx, ky); 1/k^2 is FP64.
+template <typename VT>
+__device__ __forceinline__ VT apply_op(int op, VT w, int kx, int ky, double rk2) {
+    using T = decltype(w.x);
+    switch (op) {
+        case OP_U: {  // u = i ky psi = (-ky psi.y, ky psi.x)
+            const double s = (double)ky * rk2;
+            return mk<VT>((T)(-s * (double)w.y), (T)(s * (double)w.x));
+        }
+        case OP_V: {  // v = -i kx psi = (kx psi.y, -kx psi.x)
+            const double s = (double)kx * rk2;
+            return mk<VT>((T)(s * (double)w.y), (T)(-s * (double)w.x));
+        }
+        case OP_PSI:
+            return mk<VT>((T)(rk2 * (double)w.x), (T)(rk2 * (double)w.y));
+        case OP_WX:
+            return mk<VT>((T)(-kx) * w.y, (T)kx * w.x);
+        case OP_WY:
+            return mk<VT>((T)(-ky) * w.y, (T)ky * w.x);
+        case OP_UX: {  // i kx u = -kx ky psi
+            const double s = -(double)kx * (double)ky * rk2;
+            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
+        }
+        case OP_VY: {  // i ky v = kx ky psi
+            const double s = (double)kx * (double)ky * rk2;
+            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
+        }
+        default:
+            return w;
+    }
+}
+
+// ------------------------------------------------------------------------
+// K1: inverse y-pass.  blk selects field (blk / ncg) and the column tile
+// [cg*G, cg*G+G); G transforms of Tg threads each.
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::t* __restrict__ S,
+                                          const double* __restrict__ rk2, const FieldSet& fs,
+                                          const typename Vec<T>::t* __restrict__ tw, int G, int blk,
+                                          typename Vec<T>::t* bufs) {
+    using VT = typename Vec<T>::t;
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int ncg = (d.KX + G - 1) / G;
+    const int f = blk / ncg;
+    const int cg = blk - f * ncg;
+    const int kx0 = cg * G;
+    const int kx = kx0 + g;
+    const bool active = kx < d.KX && g < G;
+    // select without dynamic indexing of the parameter struct
+    int op;
+    void* outp;
+    switch (f) {
+        case 0: op = fs.op[0]; outp = fs.out[0]; break;
+        case 1: op = fs.op[1]; outp = fs.out[1]; break;
+        case 2: op = fs.op[2]; outp = fs.out[2]; break;
+        default: op = fs.op[3]; outp = fs.out[3]; break;
+    }
+    VT* buf = bufs + (size_t)g * d.M;
+
+    const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
+    const double* rcol = rk2 + (size_t)(active ? kx : 0) * d.ldS;
+    for (int n = lane; n < d.M; n += d.Tg) {
+        VT val = mk<VT>((T)0, (T)0);
+        int jc = -1, ky = 0;
+        if (n <= d.K) {
+            jc = n;
+            ky = n;
+        } else if (n >= d.M - d.K) {
+            ky = n - d.M;
+            jc = ky + d.KY;
+        }
+        if (active && jc >= 0) val = apply_op(op, __ldcg(&col[jc]), kx, ky, rcol[jc]);
+        buf[n] = val;
+    }
+    fft_run<true>(buf, d, lane, tw);
+
+    VT* out = reinterpret_cast<VT*>(outp);
+    const int gtot = min(G, d.KX - kx0);
+    for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
+        const int y = idx / G;
+        const int gg = idx - y * G;
+        if (gg < gtot) out[(size_t)y * d.ldI + kx0 + gg] = bufs[(size_t)gg * d.M + y];
+    }
+}
+
+// Hermitian extension of two half-spectrum rows X, Y (kx in [0,K]) packed as
+// Z = X + iY over the full length M; the kx=0 entries contribute their real
+// parts only (the c2r convention of FFTW, used by src/Spectral.F90:780).
+template <typename VT>
+__device__ __forceinline__ void build_pair(VT* buf, const VT* __restrict__ X, const VT* __restrict__ Y,
+                                           const Dims& d, int lane, bool active) {
+    using T = decltype(buf[0].x);
+    for (int n = lane; n < d.M; n += d.Tg) {
+        VT z = mk<VT>((T)0, (T)0);
+        if (active) {
+            if (n == 0) {
+                z = mk<VT>(__ldcg(&X[0]).x, __ldcg(&Y[0]).x);
+            } else if (n <= d.K) {
+                const VT a = __ldcg(&X[n]), b = __ldcg(&Y[n]);
+                z = mk<VT>(a.x - b.y, a.y + b.x);
+            } else if (n >= d.M - d.K) {
+                const VT a = __ldcg(&X[d.M - n]), b = __ldcg(&Y[d.M - n]);
+                z = mk<VT>(a.x + b.y, b.x - a.y);
+            }
+        }
+        buf[n] = z;
+    }
+}
+
+// Split the forward FFT P of p = a + i b (a, b real rows) into the half
+// spectra A(k) = (P(k) + conj P(M-k))/2 and B(k) = (P(k) - conj P(M-k))/(2i),
+// k in [0, K], times scale.
+template <typename VT>
+__device__ __forceinline__ void extract_pair(const VT* buf, VT* A, VT* B, const Dims& d, int lane,
+                                             bool active, decltype(buf[0].x) scale) {
+    if (!active) return;
+    for (int k = lane; k <= d.K; k += d.Tg) {
+        const VT p = buf[k];
+        const VT q = buf[k == 0 ? 0 : d.M - k];
+        A[k] = mk<VT>((p.x + q.x) * scale, (p.y - q.y) * scale);
+        B[k] = mk<VT>((p.y + q.y) * scale, (q.x - p.x) * scale);
+    }
+}
+
+// ------------------------------------------------------------------------
+// K2 (Basdevant form): one physical row per transform, rows [blk*G, blk*G+G).
+// z = u + i v from one inverse FFT, then p = u v + i (v^2 - u^2), one forward
+// FFT, split into the normalised half spectra of u v (-> Iu row) and
+// v^2 - u^2 (-> Iv row).  Two complex FFTs per row.
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ void xpass_bas_body(const Dims& d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+                                               const typename Vec<T>::t* __restrict__ tw, int G, T scale,
+                                               int blk, typename Vec<T>::t* bufs) {
+    using VT = typename Vec<T>::t;
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blk * G + g;
+    const bool active = y < d.M && g < G;
+    VT* Z = bufs + (size_t)g * d.M;
+    VT* urow = Iu + (size_t)(active ? y : 0) * d.ldI;
+    VT* vrow = Iv + (size_t)(active ? y : 0) * d.ldI;
+    build_pair(Z, urow, vrow, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);
+    for (int n = lane; n < d.M; n += d.Tg) {
+        const VT z = Z[n];
+        Z[n] = mk<VT>(z.x * z.y, z.y * z.y - z.x * z.x);
+    }
+    fft_run<false>(Z, d, lane, tw);
+    extract_pair(Z, urow, vrow, d, lane, active, scale);
+}
+
+// ------------------------------------------------------------------------
+// K3: forward y-pass of the two products + RK3 stage epilogue on columns
+// [blk*G, blk*G+G): 2G transforms (G columns x two product fields: {u v,
+// v^2 - u^2} in the Basdevant form, {u w, v w} in the conservative form),
+// run blockDim/Tg at a time.
+//   stage 1: S1 = S0 + dt dW                    (w_in = S0)
+//   stage 2: S1 = 3/4 S0 + 1/4 S1 + dt/4 dW      (w_in = S1)
+//   stage 3: S0 = S0/3 + 2/3 S1 + 2dt/3 dW       (w_in = S1)
+//   stage 0: Sdw = dW of w_in = S0 (ComputeRHS alone)
+// followed by Truncate (|k|^2 > K^2 -> 0).  Division by 3 is a multiply by
+// the rounded reciprocal (a <= 1 ulp difference from
+// src/TimeIntegration.F90:198-200).  src, when not null, is an additive
+// spectral source in the compact layout (added to dW).
+// ------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ bool yfwd_body(const Dims& d, const typename Vec<T>::t* __restrict__ Iu,
+                                          const typename Vec<T>::t* __restrict__ Iv, typename Vec<T>::t* S0,
+                                          typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
+                                          const typename Vec<T>::t* __restrict__ src, int stage, double dt,
+                                          const Phys& ph, const typename Vec<T>::t* __restrict__ tw, int G,
+                                          int blk, typename Vec<T>::t* bufs) {
+    using VT = typename Vec<T>::t;
+    const int t = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - t * d.Tg;
+    const int kx0 = blk * G;
+    const int gtot = min(G, d.KX - kx0);
+
+    for (int idx = threadIdx.x; idx < 2 * G * d.M; idx += blockDim.x) {
+        const int gg = idx % G;
+        const int rest = idx / G;
+        const int y = rest % d.M;
+        const int fld = rest / d.M;
+        VT v = mk<VT>((T)0, (T)0);
+        if (gg < gtot) v = __ldcg(&(fld ? Iv : Iu)[(size_t)y * d.ldI + kx0 + gg]);
+        bufs[(size_t)(fld * G + gg) * d.M + y] = v;
+    }
+    const int nconc = blockDim.x / d.Tg;
+    for (int t0 = 0; t0 < 2 * G; t0 += nconc) fft_run<false>(bufs + (size_t)(t0 + t) * d.M, d, lane, tw);
+    __syncthreads();
+
+    const T tdt = (T)dt;
+    const T c34 = (T)0.75, c14 = (T)0.25, c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0);
+    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * 2.0 / 3.0);
+    const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
+    const int K2 = d.K * d.K;
+    bool bad = false;
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = idx / d.KY;
+        const int jc = idx - gg * d.KY;
+        const int kx = kx0 + gg;
+        const int ky = ky_of_jc(d, jc);
+        const int n = jc <= d.K ? jc : ky + d.M;
+        const size_t off = (size_t)kx * d.ldS + jc;
+        const int kk = kx * kx + ky * ky;
+        VT out;
+        if (kk > K2) {
+            out = mk<VT>((T)0, (T)0);
+        } else {
+            const VT nx = bufs[(size_t)gg * d.M + n];
+            const VT ny = bufs[(size_t)(G + gg) * d.M + n];
+            const VT w0 = S0[off];
+            const VT win = (stage <= 1) ? w0 : S1[off];
+            const T fkx = (T)kx, fky = (T)ky;
+            const T visc = tnu * (T)kk;
+            T dwx, dwy;
+            if (ph.form == S2D_NL_BASDEVANT) {
+                // dW = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2] - nu k^2 w
+                const T c1 = (T)(kx * kx - ky * ky), c2 = (T)(kx * ky);
+                dwx = c1 * nx.x + c2 * ny.x - visc * win.x;
+                dwy = c1 * nx.y + c2 * ny.y - visc * win.y;
+            } else {
+                // dW = -i kx F[uw] - i ky F[vw] - nu k^2 w  (src/Spectral.F90:464-479)
+                dwx = fkx * nx.y + fky * ny.y - visc * win.x;
+                dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+            }
+            if (talpha != (T)0) {
+                dwx -= talpha * win.x;
+                dwy -= talpha * win.y;
+            }
+            if (ph.fk != 0 && kx == 0 && (ky == ph.fk || ky == -ph.fk)) {
+                dwx += (T)ph.f_re;
+                dwy += (ky > 0) ? (T)ph.f_im : (T)(-ph.f_im);
+            }
+            if (src) {
+                const VT e = src[off];
+                dwx += e.x;
+                dwy += e.y;
+            }
+            if (stage == 0) {
+                out = mk<VT>(dwx, dwy);
+            } else if (stage == 1) {
+                out = mk<VT>(w0.x + tdt * dwx, w0.y + tdt * dwy);
+            } else if (stage == 2) {
+                out = mk<VT>(c34 * w0.x + c14 * win.x + dt4 * dwx, c34 * w0.y + c14 * win.y + dt4 * dwy);
+            } else {
+                out = mk<VT>(c13 * w0.x + c23 * win.x + dt23 * dwx, c13 * w0.y + c23 * win.y + dt23 * dwy);
+            }
+            bad |= bits_nonfinite(out.x) | bits_nonfinite(out.y);
+        }
+        if (stage == 0) Sdw[off] = out;
+        else if (stage == 3) S0[off] = out;
+        else S1[off] = out;
+    }
+    return bad;
+}
+
+}  // namespace s2d

@@ -87,10 +87,23 @@ class Spectral2D:
         self.grid = get_grid_size(nx, cfg.ny, dealias)
         self.shape = (self.grid.nyG, self.grid.cISize)
 
+    @classmethod
+    def _borrow(cls, handle: C.c_void_p, nx: int, nu: float, precision: str) -> "Spectral2D":
+        """Wrap a handle owned elsewhere (a run of an :class:`Ensemble`)."""
+        self = cls.__new__(cls)
+        self._L = L.lib()
+        self._h = handle
+        self._owned = False
+        self.nx, self.nu, self.precision = nx, nu, precision
+        self.grid = get_grid_size(nx, nx)
+        self.shape = (self.grid.nyG, self.grid.cISize)
+        return self
+
     # -- lifetime -----------------------------------------------------------
     def close(self) -> None:
         if getattr(self, "_h", None):
-            self._L.s2d_destroy(self._h)
+            if getattr(self, "_owned", True):
+                self._L.s2d_destroy(self._h)
             self._h = None
 
     def __enter__(self):
@@ -209,3 +222,75 @@ class Spectral2D:
 
     def kernels_per_step(self) -> int:
         return L.check(self._L.s2d_kernels_per_step(self._h))
+
+
+class Ensemble:
+    """Independent runs of uneven sizes advanced together: one persistent
+    kernel launch per RK3 stage for all runs, replayed from a CUDA graph.
+    ``runs[i]`` is a :class:`Spectral2D` view of run i (set/get state, ICs,
+    CFL, spectrum), ordered with the ensemble's launches."""
+
+    def __init__(self, nxs, nus, precision: str = "fp64", device: int = 0, alpha=None,
+                 forcing_amp=None, forcing_k=None):
+        self._L = L.lib()
+        n = len(nxs)
+        cfgs = (L.S2DConfig * n)()
+        for i in range(n):
+            cfgs[i] = L.S2DConfig(nx=nxs[i], ny=nxs[i], dealias=L.S2D_DEALIAS_3_2_RULE,
+                                  precision=_FP[precision], nu=nus[i],
+                                  alpha=(alpha[i] if alpha is not None else 0.0),
+                                  forcing_amp=(forcing_amp[i] if forcing_amp is not None else 0.0),
+                                  forcing_k=(forcing_k[i] if forcing_k is not None else 0),
+                                  device=device, nonlinear_form=L.S2D_NL_BASDEVANT)
+        b = C.c_void_p()
+        L.check(self._L.s2d_batch_create(n, cfgs, C.byref(b)))
+        self._b = b
+        self.runs = []
+        for i in range(n):
+            h = C.c_void_p()
+            L.check(self._L.s2d_batch_run(b, i, C.byref(h)))
+            self.runs.append(Spectral2D._borrow(h, nxs[i], nus[i], precision))
+        self.nxs = list(nxs)
+
+    def close(self) -> None:
+        if getattr(self, "_b", None):
+            for r in self.runs:
+                r._h = None
+            self._L.s2d_batch_destroy(self._b)
+            self._b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_dt(self, dts) -> None:
+        a = np.ascontiguousarray(dts, dtype=np.float64)
+        L.check(self._L.s2d_batch_set_dt(self._b, _dptr(a)))
+
+    def integrate_steps(self, n: int) -> None:
+        L.check(self._L.s2d_batch_integrate_steps(self._b, n))
+
+    def time_steps(self, n: int) -> float:
+        ms = C.c_double()
+        L.check(self._L.s2d_batch_time_steps(self._b, n, C.byref(ms)))
+        return ms.value
+
+    def status(self) -> None:
+        L.check(self._L.s2d_batch_status(self._b))
+
+    def synchronize(self) -> None:
+        L.check(self._L.s2d_batch_synchronize(self._b))
+
+    def tune(self):
+        """Autotune the tile schedule; returns (threads, ctas_per_sm, ms_per_step)."""
+        t, c, ms = C.c_int32(), C.c_int32(), C.c_double()
+        L.check(self._L.s2d_batch_tune(self._b, C.byref(t), C.byref(c), C.byref(ms)))
+        return t.value, c.value, ms.value
