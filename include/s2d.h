@@ -235,6 +235,53 @@ S2D_API int s2d_batch_synchronize(s2d_batch* b);
  * fastest and restores every run's state.  Any output may be NULL. */
 S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm, double* ms_per_step);
 
+/* ---- learned subgrid closure for coarse LES (no reference counterpart) -- *
+ * Sharp spectral filter of a DNS state to an LES grid (a Truncate-style mask
+ * of radius nx_les/2, src/Spectral.F90:788-802), the subgrid vorticity flux
+ * Pi^ = T[N_dns(w)] - N_les(T w) (N = F[u . grad w]), and a 6-layer circular
+ * 3x3 CNN (2 -> 32 x 5 -> 1 channels, GELU, BF16 activations and weights,
+ * FP32 accumulation, Adam) that predicts Pi from the filtered (w, psi) on the
+ * LES collocation grid.  Closure handles must be FP64. */
+typedef struct s2d_cnn s2d_cnn;
+/* grid = LES collocation grid (3*nx_les/2); max_batch = largest batch */
+S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32_t device, s2d_cnn** out);
+S2D_API void s2d_cnn_destroy(s2d_cnn* c);
+S2D_API int s2d_cnn_num_params(const s2d_cnn* c);
+/* parameters per layer: W[co][tap][ci] (tap = 3(dy+1)+(dx+1)) then b[co], FP32 */
+S2D_API int s2d_cnn_get_params(s2d_cnn* c, float* params);
+S2D_API int s2d_cnn_set_params(s2d_cnn* c, const float* params);
+/* normalisation: rms of w, psi and Pi (inputs divided, output multiplied) */
+S2D_API int s2d_cnn_set_scales(s2d_cnn* c, const double* rms3);
+S2D_API int s2d_cnn_get_scales(const s2d_cnn* c, double* rms3);
+/* x: batch x grid x grid x 2 (w, psi); y: batch x grid x grid (Pi) */
+S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t batch, float* y);
+/* MSE loss of the normalised output against target/rms_Pi and its gradient
+ * (same layout as the parameters) */
+S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, int32_t batch, float* grads,
+                              double* loss);
+/* device-resident training set of (w, psi, Pi) snapshots */
+S2D_API int s2d_cnn_dataset_reserve(s2d_cnn* c, int32_t capacity);
+S2D_API int s2d_cnn_dataset_size(const s2d_cnn* c);
+S2D_API int s2d_cnn_dataset_add(s2d_cnn* c, s2d_handle* les);   /* after s2d_subgrid_flux */
+S2D_API int s2d_cnn_dataset_stats(s2d_cnn* c, double* rms3);
+/* one epoch over samples [first, first+count) in seeded random order */
+S2D_API int s2d_cnn_train_epoch(s2d_cnn* c, int32_t first, int32_t count, int32_t batch, double lr,
+                                uint64_t seed, double* mean_loss);
+S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_loss);
+/* les state := sharp-filtered dns state */
+S2D_API int s2d_filter_state(s2d_handle* dns, s2d_handle* les);
+/* les state := filtered dns state, and the subgrid flux of the DNS state on
+ * the LES grid is kept in the LES handle (and written to pi_host in the
+ * reference layout when not NULL) */
+S2D_API int s2d_subgrid_flux(s2d_handle* dns, s2d_handle* les, double* pi_host);
+/* attach (c != NULL) or detach the closure network of an LES handle */
+S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c);
+/* the closure source -Pi^ of the current LES state (asynchronous) */
+S2D_API int s2d_les_closure_term(s2d_handle* les);
+/* n steps; with a closure attached, -Pi^ of the state at the start of each
+ * step is added to dW in its three RK3 stages */
+S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt);
+
 /* ---- allocation-free right-hand side ----------------------------------- *
  * No counterpart in the reference.  For callers that must not allocate
  * device memory -- host codes whose device memory belongs to another

@@ -55,6 +55,7 @@ class S2DError(RuntimeError):
 
 
 _dp = C.POINTER(C.c_double)
+_fp = C.POINTER(C.c_float)
 _h = C.c_void_p
 
 # name -> (restype, argtypes)
@@ -97,6 +98,27 @@ SIGNATURES = {
     "s2d_batch_status": (C.c_int, [C.c_void_p]),
     "s2d_batch_synchronize": (C.c_int, [C.c_void_p]),
     "s2d_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "s2d_cnn_create": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_void_p)]),
+    "s2d_cnn_destroy": (None, [C.c_void_p]),
+    "s2d_cnn_num_params": (C.c_int, [C.c_void_p]),
+    "s2d_cnn_get_params": (C.c_int, [C.c_void_p, _fp]),
+    "s2d_cnn_set_params": (C.c_int, [C.c_void_p, _fp]),
+    "s2d_cnn_set_scales": (C.c_int, [C.c_void_p, _dp]),
+    "s2d_cnn_get_scales": (C.c_int, [C.c_void_p, _dp]),
+    "s2d_cnn_forward_host": (C.c_int, [C.c_void_p, _fp, C.c_int32, _fp]),
+    "s2d_cnn_grad_host": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int32, _fp, _dp]),
+    "s2d_cnn_dataset_reserve": (C.c_int, [C.c_void_p, C.c_int32]),
+    "s2d_cnn_dataset_size": (C.c_int, [C.c_void_p]),
+    "s2d_cnn_dataset_add": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "s2d_cnn_dataset_stats": (C.c_int, [C.c_void_p, _dp]),
+    "s2d_cnn_train_epoch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
+                                      _dp]),
+    "s2d_cnn_eval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _dp]),
+    "s2d_filter_state": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "s2d_subgrid_flux": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
+    "s2d_les_set_closure": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "s2d_les_closure_term": (C.c_int, [C.c_void_p]),
+    "s2d_les_integrate_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
 }
 
 _lib = None

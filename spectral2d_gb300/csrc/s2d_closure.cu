@@ -1,0 +1,1042 @@
+// s2d_closure.cu -- learned subgrid closure for coarse LES (no counterpart in
+// the reference).
+//
+// Data: the DNS state is sharp-spectrally filtered to the LES's retained
+// modes |k| <= nx_les/2 (a Truncate-style mask with a smaller radius,
+// src/Spectral.F90:788-802), and the subgrid vorticity flux
+//     Pi^ = T[N_dns(w)] - N_les(T w),   N(w) = F[u . grad w] (dealiased),
+// is formed in spectral space from the two solvers' right-hand sides
+// (N = -(dW + nu k^2 w)).  Fields go to the LES collocation grid (3/2 rule,
+// M = 3 nx_les / 2) for the network.
+//
+// Network: 6 circular 3x3 convolutions, 2 -> 32 -> 32 -> 32 -> 32 -> 32 -> 1
+// channels, GELU (erf) after the first five; activations and working weights
+// in BF16, accumulation FP32, FP32 master weights, Adam.  Convolutions are
+// implicit GEMMs (pixels x out-channels x 9*in-channels): the forward pass and
+// the data gradient on the tensor cores with mma.sync m16n8k16 BF16->FP32,
+// the weight gradient on the FP32 pipes with a deterministic two-stage
+// reduction over pixels.  Channel counts are padded to multiples of 16
+// (input 2 -> 16, output 1 -> 16) with zero weights.
+//
+// LES with closure: each step the network maps (w, psi) of the LES state to
+// Pi on the collocation grid; -Pi^ (truncated) is added to dW in all three
+// RK3 stages of the step.
+#include "s2d.h"
+#include "s2d_internal.h"
+#include "s2d_step.cuh"
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace s2d {
+
+constexpr int kLayers = 6;
+constexpr int kCinP[kLayers] = {16, 32, 32, 32, 32, 32};
+constexpr int kCoutP[kLayers] = {32, 32, 32, 32, 32, 16};
+constexpr int kCin[kLayers] = {2, 32, 32, 32, 32, 32};
+constexpr int kCout[kLayers] = {32, 32, 32, 32, 32, 1};
+
+__device__ __forceinline__ uint32_t ld32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+__device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
+    __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&u);
+    return __bfloat1622float2(h);
+}
+__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad_f(float x) {
+    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// Periodic neighbour of pixel p shifted by (dy, dx).
+__device__ __forceinline__ long nbr(long p, int dy, int dx, int H, int Wd) {
+    const long HW = (long)H * Wd;
+    const long b = p / HW;
+    const int rem = (int)(p - b * HW);
+    int y = rem / Wd, x = rem - (rem / Wd) * Wd;
+    y += dy;
+    x += dx;
+    y += (y < 0) ? H : ((y >= H) ? -H : 0);
+    x += (x < 0) ? Wd : ((x >= Wd) ? -Wd : 0);
+    return b * HW + (long)y * Wd + x;
+}
+
+// Implicit-GEMM convolution on the tensor cores.  A warp owns 16 pixels x
+// NC channels; the K loop runs over 9 taps x KC/16 chunks of 16 channels.
+//   FWD (SIGN = +1): out[p, n] = sum_{t,k} in[p + off_t, k] W[n, t, k]
+//   data gradient (SIGN = -1): out[q, n] = sum_{t,k} in[q - off_t, k] W^T[n, t, k]
+// Epilogue EPI: 0 = + bias, store z and gelu(z) (BF16); 1 = + bias, store
+// channel 0 as FP32; 2 = multiply by gelu'(zprev), store BF16.
+template <int KC, int NC, int SIGN, int EPI>
+__global__ void __launch_bounds__(256) k_conv_mma(const __nv_bfloat16* __restrict__ in,
+                                                  const __nv_bfloat16* __restrict__ W,
+                                                  const float* __restrict__ bias,
+                                                  const __nv_bfloat16* __restrict__ zprev, __nv_bfloat16* z,
+                                                  __nv_bfloat16* a, float* yout, long P, int H, int Wd) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int g = lane >> 2, tg = lane & 3;
+    const long p0 = ((long)blockIdx.x * 8 + warp) * 16;
+    if (p0 >= P) return;
+    const long pA = p0 + g, pB = pA + 8;
+    const bool vA = pA < P, vB = pB < P;
+    constexpr int NT = NC / 8;
+    float acc[NT][4];
+#pragma unroll
+    for (int i = 0; i < NT; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t) {
+        const int dy = SIGN * (t / 3 - 1), dx = SIGN * (t % 3 - 1);
+        const __nv_bfloat16* rA = in + nbr(vA ? pA : 0, dy, dx, H, Wd) * KC;
+        const __nv_bfloat16* rB = in + nbr(vB ? pB : 0, dy, dx, H, Wd) * KC;
+#pragma unroll
+        for (int c = 0; c < KC; c += 16) {
+            const uint32_t a0 = vA ? ld32(rA + c + tg * 2) : 0u;
+            const uint32_t a1 = vB ? ld32(rB + c + tg * 2) : 0u;
+            const uint32_t a2 = vA ? ld32(rA + c + tg * 2 + 8) : 0u;
+            const uint32_t a3 = vB ? ld32(rB + c + tg * 2 + 8) : 0u;
+#pragma unroll
+            for (int nt = 0; nt < NT; ++nt) {
+                const __nv_bfloat16* wr = W + ((long)(nt * 8 + g) * 9 + t) * KC + c;
+                mma_bf16(acc[nt], a0, a1, a2, a3, ld32(wr + tg * 2), ld32(wr + tg * 2 + 8));
+            }
+        }
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt) {
+        const int n0 = nt * 8 + tg * 2;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const long p = h ? pB : pA;
+            if (!(h ? vB : vA)) continue;
+            float v0 = acc[nt][2 * h], v1 = acc[nt][2 * h + 1];
+            if (EPI == 0) {
+                v0 += bias[n0];
+                v1 += bias[n0 + 1];
+                *reinterpret_cast<uint32_t*>(z + p * NC + n0) = pack_bf16(v0, v1);
+                *reinterpret_cast<uint32_t*>(a + p * NC + n0) = pack_bf16(gelu_f(v0), gelu_f(v1));
+            } else if (EPI == 1) {
+                if (n0 == 0) yout[p] = v0 + bias[0];
+            } else {
+                const float2 zz = unpack_bf16(ld32(zprev + p * NC + n0));
+                *reinterpret_cast<uint32_t*>(z + p * NC + n0) =
+                    pack_bf16(v0 * gelu_grad_f(zz.x), v1 * gelu_grad_f(zz.y));
+            }
+        }
+    }
+}
+
+// Weight and bias gradient of one layer on the FP32 pipes:
+//   dW[co, t, ci] = sum_p dz[p, co] in[p + off_t, ci],   db[co] = sum_p dz[p, co].
+// A CTA walks image rows, staging dz of the row and in of rows y-1, y, y+1 in
+// shared memory; thread = (co, group of CI/8 input channels); partial sums per
+// CTA go to part[blockIdx] and are summed by k_reduce_rows in a fixed order.
+template <int CI, int CO>
+__global__ void __launch_bounds__(256) k_conv_wgrad(const __nv_bfloat16* __restrict__ dz,
+                                                    const __nv_bfloat16* __restrict__ in, float* part, int B,
+                                                    int H, int Wd) {
+    constexpr int CIG = CI / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* rows = reinterpret_cast<__nv_bfloat16*>(smem_raw);   // [3][Wd][CI]
+    __nv_bfloat16* drow = rows + 3 * Wd * CI;                            // [Wd][CO]
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int co = warp * 4 + (lane >> 3);
+    const int ci0 = (lane & 7) * CIG;
+    float acc[9][CIG];
+    float accb = 0.f;
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int c = 0; c < CIG; ++c) acc[t][c] = 0.f;
+    const long HW = (long)H * Wd;
+    for (int r = blockIdx.x; r < B * H; r += gridDim.x) {
+        const int b = r / H, y = r - (r / H) * H;
+        __syncthreads();
+        for (int i = threadIdx.x; i < 3 * Wd * CI / 2; i += blockDim.x) {
+            const int e = 2 * i;
+            const int rr = e / (Wd * CI);
+            const int rem = e - rr * Wd * CI;
+            int yy = y + rr - 1;
+            yy += (yy < 0) ? H : ((yy >= H) ? -H : 0);
+            reinterpret_cast<uint32_t*>(rows)[i] = ld32(in + ((long)b * HW + (long)yy * Wd) * CI + rem);
+        }
+        for (int i = threadIdx.x; i < Wd * CO / 2; i += blockDim.x)
+            reinterpret_cast<uint32_t*>(drow)[i] = ld32(dz + ((long)b * HW + (long)y * Wd) * CO + 2 * i);
+        __syncthreads();
+        for (int x = 0; x < Wd; ++x) {
+            const float d = __bfloat162float(drow[x * CO + co]);
+            accb += d;
+#pragma unroll
+            for (int t = 0; t < 9; ++t) {
+                int xs = x + (t % 3) - 1;
+                xs += (xs < 0) ? Wd : ((xs >= Wd) ? -Wd : 0);
+                const __nv_bfloat16* v = rows + ((t / 3) * Wd + xs) * CI + ci0;
+#pragma unroll
+                for (int c = 0; c < CIG; c += 2) {
+                    const float2 f = unpack_bf16(ld32(v + c));
+                    acc[t][c] += d * f.x;
+                    acc[t][c + 1] += d * f.y;
+                }
+            }
+        }
+    }
+    const long stride = (long)CO * 9 * CI + CO;
+    float* out = part + (long)blockIdx.x * stride;
+#pragma unroll
+    for (int t = 0; t < 9; ++t)
+#pragma unroll
+        for (int c = 0; c < CIG; ++c) out[((long)co * 9 + t) * CI + ci0 + c] = acc[t][c];
+    if ((lane & 7) == 0) out[(long)CO * 9 * CI + co] = accb;
+}
+
+// out[i] = sum_b part[b * n + i], b in order.
+__global__ void k_reduce_rows(const float* __restrict__ part, int nblk, long n, float* out) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        float s = 0.f;
+        for (int b = 0; b < nblk; ++b) s += part[(long)b * n + i];
+        out[i] = s;
+    }
+}
+
+// MSE loss: dz[p, 0] = 2 (y - t) / n, other channels 0; per-block loss sums.
+__global__ void k_mse(const float* __restrict__ y, const float* __restrict__ tgt, long P, float inv_n,
+                      __nv_bfloat16* dz, int CO, double* part) {
+    __shared__ double red[256];
+    double s = 0.0;
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
+        const float e = y[p] - tgt[p];
+        s += (double)e * e;
+        dz[p * CO] = __float2bfloat16_rn(2.f * e * inv_n);
+        for (int c = 1; c < CO; ++c) dz[p * CO + c] = __float2bfloat16_rn(0.f);
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters.
+__global__ void k_adam(float* p, const float* __restrict__ g, float* m, float* v, long n, float lr, float b1, float b2,
+                       float eps, float c1, float c2) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    }
+}
+
+// BF16 working copies of one layer: W[co][t][ci] and W^T[ci][t][co].
+__global__ void k_refresh(const float* __restrict__ Wm, int CO, int CI, __nv_bfloat16* W, __nv_bfloat16* WT) {
+    const int n = CO * 9 * CI;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int co = i / (9 * CI), rem = i - co * 9 * CI, t = rem / CI, ci = rem - t * CI;
+        const __nv_bfloat16 h = __float2bfloat16_rn(Wm[i]);
+        W[i] = h;
+        WT[((long)ci * 9 + t) * CO + co] = h;
+    }
+}
+
+// Network input (channels 0, 1 = w / s0, psi / s1; 2..15 = 0) and target
+// (Pi / s2) of a batch, from dataset samples idx[b] (FP32 [HW][3]).
+__global__ void k_pack(const float* __restrict__ data, const int* __restrict__ idx, int B, long HW, float r0,
+                       float r1, float r2, __nv_bfloat16* x, float* tgt) {
+    const long P = (long)B * HW;
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
+        const long b = p / HW, q = p - b * HW;
+        const float* s = data + ((long)idx[b] * HW + q) * 3;
+        uint32_t* xr = reinterpret_cast<uint32_t*>(x + p * 16);
+        xr[0] = pack_bf16(s[0] * r0, s[1] * r1);
+        for (int c = 1; c < 8; ++c) xr[c] = 0u;
+        if (tgt) tgt[p] = s[2] * r2;
+    }
+}
+
+// ---- LES-side kernels ---------------------------------------------------
+
+// Sharp filter DNS -> LES (|k| <= K_les) of w, and N_dns = -(dW + nu k^2 w).
+__global__ void k_filter_gather(Dims dd, Dims dl, const double2* __restrict__ wd, const double2* __restrict__ dWd,
+                                double nu_d, double2* wl, double2* pil) {
+    const int total = dl.KX * dl.KY;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int kx = i / dl.KY, jc = i - kx * dl.KY;
+        const int ky = ky_of_jc(dl, jc);
+        double2 w = make_double2(0.0, 0.0), nl = make_double2(0.0, 0.0);
+        if (kx * kx + ky * ky <= dl.K * dl.K) {
+            const int jd = ky >= 0 ? ky : ky + dd.KY;
+            const size_t od = (size_t)kx * dd.ldS + jd;
+            w = wd[od];
+            if (dWd) {
+                const double2 d = dWd[od];
+                const double visc = nu_d * (double)(kx * kx + ky * ky);
+                nl = make_double2(-(d.x + visc * w.x), -(d.y + visc * w.y));
+            }
+        }
+        const size_t ol = (size_t)kx * dl.ldS + jc;
+        wl[ol] = w;
+        if (pil) pil[ol] = nl;
+    }
+}
+
+// Pi = N_dns_filtered - N_les with N_les = -(dW_les + nu k^2 w): pi += dW + nu k^2 w.
+__global__ void k_pi_finish(Dims dl, const double2* __restrict__ w, const double2* __restrict__ dW, double nu,
+                            double2* pi) {
+    const int total = dl.KX * dl.KY;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+        const int kx = i / dl.KY, jc = i - kx * dl.KY;
+        const int ky = ky_of_jc(dl, jc);
+        const size_t o = (size_t)kx * dl.ldS + jc;
+        if (kx * kx + ky * ky > dl.K * dl.K) {
+            pi[o] = make_double2(0.0, 0.0);
+            continue;
+        }
+        const double visc = nu * (double)(kx * kx + ky * ky);
+        const double2 a = pi[o], d = dW[o], ww = w[o];
+        pi[o] = make_double2(a.x + d.x + visc * ww.x, a.y + d.y + visc * ww.y);
+    }
+}
+
+// Physical rows of two spectral fields X, Y (half-spectral rows, Y may be
+// null): one inverse FFT of X + iY per row, real part -> ox, imaginary -> oy.
+__global__ void __launch_bounds__(512) k_xinv_phys2(Dims d, const double2* __restrict__ X,
+                                                    const double2* __restrict__ Y, const double2* __restrict__ tw,
+                                                    int G, double* ox, double* oy) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double2* bufs = reinterpret_cast<double2*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    double2* Z = bufs + (size_t)g * d.M;
+    const int yy = active ? y : 0;
+    if (Y) {
+        build_pair(Z, X + (size_t)yy * d.ldI, Y + (size_t)yy * d.ldI, d, lane, active);
+    } else {
+        // X alone: Z = X Hermitian-extended
+        for (int n = lane; n < d.M; n += d.Tg) {
+            double2 z = make_double2(0.0, 0.0);
+            if (active) {
+                const double2* Xr = X + (size_t)yy * d.ldI;
+                if (n == 0) z = make_double2(__ldcg(&Xr[0]).x, 0.0);
+                else if (n <= d.K) z = __ldcg(&Xr[n]);
+                else if (n >= d.M - d.K) {
+                    const double2 a = __ldcg(&Xr[d.M - n]);
+                    z = make_double2(a.x, -a.y);
+                }
+            }
+            Z[n] = z;
+        }
+    }
+    fft_run<true>(Z, d, lane, tw);
+    if (active)
+        for (int n = lane; n < d.M; n += d.Tg) {
+            ox[(size_t)y * d.M + n] = Z[n].x;
+            if (oy) oy[(size_t)y * d.M + n] = Z[n].y;
+        }
+}
+
+// Dataset sample (FP32 [HW][3]) from physical w, psi, Pi (FP64).
+__global__ void k_to_sample(const double* __restrict__ w, const double* __restrict__ p, const double* __restrict__ pi,
+                            long HW, float* out) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
+        out[3 * i] = (float)w[i];
+        out[3 * i + 1] = (float)p[i];
+        out[3 * i + 2] = (float)pi[i];
+    }
+}
+
+// Network input of one LES state: channels (w / s0, psi / s1).
+__global__ void k_pack_les(const double* __restrict__ w, const double* __restrict__ p, long HW, float r0, float r1,
+                           __nv_bfloat16* x) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
+        uint32_t* xr = reinterpret_cast<uint32_t*>(x + i * 16);
+        xr[0] = pack_bf16((float)(w[i] * r0), (float)(p[i] * r1));
+        for (int c = 1; c < 8; ++c) xr[c] = 0u;
+    }
+}
+
+// phys = scale * y (network output, FP32) as FP64.
+__global__ void k_scale_out(const float* __restrict__ y, long n, double scale, double* phys) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        phys[i] = scale * (double)y[i];
+}
+
+// Moments of the dataset: per-block sums of squares of the 3 channels.
+__global__ void k_moments(const float* __restrict__ data, long n, double* part) {
+    __shared__ double red[3][256];
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        s0 += (double)data[3 * i] * data[3 * i];
+        s1 += (double)data[3 * i + 1] * data[3 * i + 1];
+        s2 += (double)data[3 * i + 2] * data[3 * i + 2];
+    }
+    red[0][threadIdx.x] = s0;
+    red[1][threadIdx.x] = s1;
+    red[2][threadIdx.x] = s2;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w)
+            for (int c = 0; c < 3; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int c = 0; c < 3; ++c) part[3 * blockIdx.x + c] = red[c][0];
+}
+
+}  // namespace s2d
+
+using namespace s2d;
+
+struct s2d_cnn {
+    int device = 0;
+    int H = 0, Wd = 0, maxB = 0;
+    cudaStream_t stream = nullptr;
+    long poff[kLayers + 1];            // offsets of each layer's (W, b) in the padded FP32 arrays
+    long nparam_pad = 0;
+    float *master = nullptr, *grad = nullptr, *m = nullptr, *v = nullptr;
+    __nv_bfloat16 *Wb[kLayers] = {}, *WTb[kLayers] = {};
+    __nv_bfloat16* X0 = nullptr;
+    __nv_bfloat16 *Z[kLayers - 1] = {}, *A[kLayers - 1] = {};
+    __nv_bfloat16 *dZ6 = nullptr, *dZa = nullptr, *dZb = nullptr;
+    float *Y = nullptr, *tgt = nullptr;
+    float* part = nullptr;
+    long part_n = 0;
+    int wg_blocks = 0;
+    double* lpart = nullptr;
+    int* idx = nullptr;
+    float* data = nullptr;
+    int data_cap = 0, data_n = 0;
+    double scale[3] = {1.0, 1.0, 1.0};
+    long step = 0;
+};
+
+namespace {
+
+int cerr(int code, const char* m) { return set_error(code, m); }
+
+#define C_CUDA(call)                                                               \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e_));  \
+    } while (0)
+
+int nblocks(long n, int threads) { return (int)std::min<long>((n + threads - 1) / threads, 152L * 16); }
+
+int refresh_all(s2d_cnn* c) {
+    for (int l = 0; l < kLayers; ++l) {
+        const int n = kCoutP[l] * 9 * kCinP[l];
+        k_refresh<<<nblocks(n, 256), 256, 0, c->stream>>>(c->master + c->poff[l], kCoutP[l], kCinP[l], c->Wb[l],
+                                                           c->WTb[l]);
+        C_CUDA(cudaGetLastError());
+    }
+    return S2D_OK;
+}
+
+// forward of the batch in X0 (B images)
+int forward(s2d_cnn* c, int B) {
+    const long P = (long)B * c->H * c->Wd;
+    const int grid = (int)((P + 127) / 128);
+    const float* bias[kLayers];
+    for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
+    k_conv_mma<16, 32, 1, 0><<<grid, 256, 0, c->stream>>>(c->X0, c->Wb[0], bias[0], nullptr, c->Z[0], c->A[0],
+                                                           nullptr, P, c->H, c->Wd);
+    for (int l = 1; l < kLayers - 1; ++l)
+        k_conv_mma<32, 32, 1, 0><<<grid, 256, 0, c->stream>>>(c->A[l - 1], c->Wb[l], bias[l], nullptr, c->Z[l],
+                                                               c->A[l], nullptr, P, c->H, c->Wd);
+    k_conv_mma<32, 16, 1, 1><<<grid, 256, 0, c->stream>>>(c->A[kLayers - 2], c->Wb[kLayers - 1], bias[kLayers - 1],
+                                                           nullptr, nullptr, nullptr, c->Y, P, c->H, c->Wd);
+    C_CUDA(cudaGetLastError());
+    return S2D_OK;
+}
+
+// loss of the batch (targets in tgt) and, with grads, the full backward pass
+int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
+    const long P = (long)B * c->H * c->Wd;
+    const int grid = (int)((P + 127) / 128);
+    const int lb = 256;
+    k_mse<<<lb, 256, 0, c->stream>>>(c->Y, c->tgt, P, 1.0f / (float)P, c->dZ6, 16, c->lpart);
+    C_CUDA(cudaGetLastError());
+    std::vector<double> lp(lb);
+    C_CUDA(cudaMemcpyAsync(lp.data(), c->lpart, sizeof(double) * lb, cudaMemcpyDeviceToHost, c->stream));
+    if (grads) {
+        const __nv_bfloat16* dz = c->dZ6;
+        __nv_bfloat16* bufs[2] = {c->dZa, c->dZb};
+        for (int l = kLayers - 1; l >= 0; --l) {
+            const __nv_bfloat16* in = l == 0 ? c->X0 : c->A[l - 1];
+            const int CI = kCinP[l], CO = kCoutP[l];
+            const size_t sm = (size_t)(3 * c->Wd * CI + c->Wd * CO) * sizeof(__nv_bfloat16);
+            const long n = (long)CO * 9 * CI + CO;
+            if (CI == 16)
+                k_conv_wgrad<16, 32><<<c->wg_blocks, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+            else if (CO == 16)
+                k_conv_wgrad<32, 16><<<c->wg_blocks, 16 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+            else
+                k_conv_wgrad<32, 32><<<c->wg_blocks, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+            C_CUDA(cudaGetLastError());
+            k_reduce_rows<<<nblocks(n, 256), 256, 0, c->stream>>>(c->part, c->wg_blocks, n, c->grad + c->poff[l]);
+            C_CUDA(cudaGetLastError());
+            if (l > 0) {
+                __nv_bfloat16* out = bufs[l & 1];
+                if (CO == 16)
+                    k_conv_mma<16, 32, -1, 2><<<grid, 256, 0, c->stream>>>(dz, c->WTb[l], nullptr, c->Z[l - 1], out,
+                                                                            nullptr, nullptr, P, c->H, c->Wd);
+                else
+                    k_conv_mma<32, 32, -1, 2><<<grid, 256, 0, c->stream>>>(dz, c->WTb[l], nullptr, c->Z[l - 1], out,
+                                                                            nullptr, nullptr, P, c->H, c->Wd);
+                C_CUDA(cudaGetLastError());
+                dz = out;
+            }
+        }
+    }
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    double s = 0.0;
+    for (double x : lp) s += x;
+    if (loss) *loss = s / (double)P;
+    return S2D_OK;
+}
+
+int adam_step(s2d_cnn* c, double lr) {
+    c->step += 1;
+    const double b1 = 0.9, b2 = 0.999;
+    const float c1 = (float)(1.0 - std::pow(b1, (double)c->step));
+    const float c2 = (float)(1.0 - std::pow(b2, (double)c->step));
+    k_adam<<<nblocks(c->nparam_pad, 256), 256, 0, c->stream>>>(c->master, c->grad, c->m, c->v, c->nparam_pad,
+                                                                (float)lr, (float)b1, (float)b2, 1e-8f, c1, c2);
+    C_CUDA(cudaGetLastError());
+    return refresh_all(c);
+}
+
+// logical (Cout x 9 x Cin + Cout per layer) <-> padded layout
+void logical_to_padded(const float* lg, std::vector<float>& pad, const long* poff) {
+    long o = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        for (int co = 0; co < kCout[l]; ++co)
+            for (int t = 0; t < 9; ++t)
+                for (int ci = 0; ci < kCin[l]; ++ci)
+                    pad[poff[l] + ((long)co * 9 + t) * kCinP[l] + ci] = lg[o++];
+        for (int co = 0; co < kCout[l]; ++co) pad[poff[l] + (long)kCoutP[l] * 9 * kCinP[l] + co] = lg[o++];
+    }
+}
+
+void padded_to_logical(const std::vector<float>& pad, float* lg, const long* poff) {
+    long o = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        for (int co = 0; co < kCout[l]; ++co)
+            for (int t = 0; t < 9; ++t)
+                for (int ci = 0; ci < kCin[l]; ++ci)
+                    lg[o++] = pad[poff[l] + ((long)co * 9 + t) * kCinP[l] + ci];
+        for (int co = 0; co < kCout[l]; ++co) lg[o++] = pad[poff[l] + (long)kCoutP[l] * 9 * kCinP[l] + co];
+    }
+}
+
+long logical_count() {
+    long n = 0;
+    for (int l = 0; l < kLayers; ++l) n += (long)kCout[l] * 9 * kCin[l] + kCout[l];
+    return n;
+}
+
+uint64_t mix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ULL;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBULL;
+    return x ^ (x >> 31);
+}
+
+int upload_host_batch(s2d_cnn* c, const float* x, const float* target, int B) {
+    // host (omega, psi) pairs -> temporary dataset slots at the end of a
+    // private staging area, then the packing kernel
+    const long HW = (long)c->H * c->Wd;
+    std::vector<float> s((size_t)B * HW * 3);
+    for (long i = 0; i < (long)B * HW; ++i) {
+        s[3 * i] = x[2 * i];
+        s[3 * i + 1] = x[2 * i + 1];
+        s[3 * i + 2] = target ? target[i] : 0.f;
+    }
+    float* tmp = nullptr;
+    int* idx = nullptr;
+    C_CUDA(cudaMalloc(&tmp, s.size() * sizeof(float)));
+    C_CUDA(cudaMalloc(&idx, sizeof(int) * B));
+    std::vector<int> id(B);
+    for (int b = 0; b < B; ++b) id[b] = b;
+    C_CUDA(cudaMemcpyAsync(tmp, s.data(), s.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    C_CUDA(cudaMemcpyAsync(idx, id.data(), sizeof(int) * B, cudaMemcpyHostToDevice, c->stream));
+    k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(tmp, idx, B, HW, (float)(1.0 / c->scale[0]),
+                                                              (float)(1.0 / c->scale[1]), (float)(1.0 / c->scale[2]),
+                                                              c->X0, c->tgt);
+    cudaError_t e = cudaGetLastError();
+    cudaStreamSynchronize(c->stream);
+    cudaFree(tmp);
+    cudaFree(idx);
+    if (e != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    return S2D_OK;
+}
+
+// Physical w and psi of an FP64 handle's state on its collocation grid (into h->phys, h->phys + M*M).
+int state_to_phys(s2d_handle* h, const void* S, double* ow, double* op, bool with_psi) {
+    FieldSet fs{};
+    fs.nf = with_psi ? 2 : 1;
+    fs.op[0] = OP_W;
+    fs.op[1] = OP_PSI;
+    fs.out[0] = h->I[0];
+    fs.out[1] = h->I[1];
+    C_CUDA(Kern<double>::yinv(h->d, S, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    const Launch& L = h->L_xrow;
+    k_xinv_phys2<<<(h->d.M + L.G - 1) / L.G, L.threads, L.smem, h->stream>>>(
+        h->d, (const double2*)h->I[0], with_psi ? (const double2*)h->I[1] : nullptr, (const double2*)h->tw, L.G, ow,
+        with_psi ? op : nullptr);
+    C_CUDA(cudaGetLastError());
+    return S2D_OK;
+}
+
+int ensure_les_buffers(s2d_handle* h) {
+    if (h->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "closure LES handles must be FP64");
+    static bool attr[64] = {false};
+    if (h->device >= 0 && h->device < 64 && !attr[h->device]) {
+        C_CUDA(cudaFuncSetAttribute(k_xinv_phys2, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
+        attr[h->device] = true;
+    }
+    const size_t cs = (size_t)h->d.KX * h->d.ldS * sizeof(double2);
+    if (!h->pi) C_CUDA(cudaMalloc(&h->pi, cs));
+    if (!h->Sdw) C_CUDA(cudaMalloc(&h->Sdw, cs));
+    if (!h->phys) C_CUDA(cudaMalloc(&h->phys, 3 * (size_t)h->d.M * h->d.M * sizeof(double)));
+    return S2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32_t device, s2d_cnn** out) {
+    if (!out || grid < 8 || max_batch < 1) return cerr(S2D_ERR_INVALID, "bad network arguments");
+    *out = nullptr;
+    s2d_cnn* c = new (std::nothrow) s2d_cnn();
+    if (!c) return cerr(S2D_ERR_NOMEM, "host allocation failed");
+    c->device = device;
+    c->H = c->Wd = grid;
+    c->maxB = max_batch;
+    auto bail = [&](int code) {
+        s2d_cnn_destroy(c);
+        return code;
+    };
+    if (cudaSetDevice(device) != cudaSuccess) return bail(cerr(S2D_ERR_CUDA, "cudaSetDevice failed"));
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(cerr(S2D_ERR_CUDA, "stream creation failed"));
+    long off = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        c->poff[l] = off;
+        off += (long)kCoutP[l] * 9 * kCinP[l] + kCoutP[l];
+    }
+    c->poff[kLayers] = off;
+    c->nparam_pad = off;
+    const long P = (long)max_batch * grid * grid;
+    int dev_sms = 152;
+    cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, device);
+    c->wg_blocks = std::max(1, std::min(2 * dev_sms, max_batch * grid));
+    c->part_n = (long)c->wg_blocks * (32 * 9 * 32 + 32);
+    bool ok = cudaMalloc(&c->master, off * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->grad, off * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->m, off * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->v, off * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->X0, P * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->dZ6, P * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->dZa, P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->dZb, P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->Y, P * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->tgt, P * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->part, c->part_n * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&c->lpart, 256 * sizeof(double)) == cudaSuccess &&
+              cudaMalloc(&c->idx, max_batch * sizeof(int)) == cudaSuccess;
+    for (int l = 0; l < kLayers && ok; ++l) {
+        const size_t n = (size_t)kCoutP[l] * 9 * kCinP[l] * sizeof(__nv_bfloat16);
+        ok = cudaMalloc(&c->Wb[l], n) == cudaSuccess && cudaMalloc(&c->WTb[l], n) == cudaSuccess;
+    }
+    for (int l = 0; l < kLayers - 1 && ok; ++l)
+        ok = cudaMalloc(&c->Z[l], P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+             cudaMalloc(&c->A[l], P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess;
+    if (!ok) return bail(cerr(S2D_ERR_NOMEM, "cudaMalloc failed"));
+    {
+        const int smax = 3 * grid * 32 * 2 + grid * 32 * 2;
+        cudaFuncSetAttribute(k_conv_wgrad<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(k_conv_wgrad<32, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(k_conv_wgrad<32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+    }
+    // He-uniform initialisation from a seeded counter-based generator
+    std::vector<float> pad(off, 0.f);
+    uint64_t ctr = 0;
+    for (int l = 0; l < kLayers; ++l) {
+        const double bound = std::sqrt(6.0 / (9.0 * kCin[l])) * (l == kLayers - 1 ? 0.5 : 1.0);
+        for (int co = 0; co < kCout[l]; ++co)
+            for (int t = 0; t < 9; ++t)
+                for (int ci = 0; ci < kCin[l]; ++ci) {
+                    const double u = (double)(mix64(seed * 0x100000001B3ULL + (ctr++)) >> 11) * (1.0 / 9007199254740992.0);
+                    pad[c->poff[l] + ((long)co * 9 + t) * kCinP[l] + ci] = (float)((2.0 * u - 1.0) * bound);
+                }
+    }
+    if (cudaMemcpy(c->master, pad.data(), off * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess)
+        return bail(cerr(S2D_ERR_CUDA, "parameter upload failed"));
+    cudaMemset(c->m, 0, off * sizeof(float));
+    cudaMemset(c->v, 0, off * sizeof(float));
+    cudaMemset(c->grad, 0, off * sizeof(float));
+    if (refresh_all(c) != S2D_OK) return bail(S2D_ERR_CUDA);
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) return bail(cerr(S2D_ERR_CUDA, "setup failed"));
+    *out = c;
+    return S2D_OK;
+}
+
+S2D_API void s2d_cnn_destroy(s2d_cnn* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    void* ptrs[] = {c->master, c->grad, c->m, c->v, c->X0, c->dZ6, c->dZa, c->dZb, c->Y, c->tgt, c->part,
+                    c->lpart, c->idx, c->data};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    for (int l = 0; l < kLayers; ++l) {
+        if (c->Wb[l]) cudaFree(c->Wb[l]);
+        if (c->WTb[l]) cudaFree(c->WTb[l]);
+    }
+    for (int l = 0; l < kLayers - 1; ++l) {
+        if (c->Z[l]) cudaFree(c->Z[l]);
+        if (c->A[l]) cudaFree(c->A[l]);
+    }
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+S2D_API int s2d_cnn_num_params(const s2d_cnn* c) {
+    if (!c) return cerr(S2D_ERR_INVALID, "null network");
+    return (int)logical_count();
+}
+
+S2D_API int s2d_cnn_get_params(s2d_cnn* c, float* p) {
+    if (!c || !p) return cerr(S2D_ERR_INVALID, "null argument");
+    C_CUDA(cudaSetDevice(c->device));
+    std::vector<float> pad(c->nparam_pad);
+    C_CUDA(cudaMemcpy(pad.data(), c->master, pad.size() * sizeof(float), cudaMemcpyDeviceToHost));
+    padded_to_logical(pad, p, c->poff);
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_set_params(s2d_cnn* c, const float* p) {
+    if (!c || !p) return cerr(S2D_ERR_INVALID, "null argument");
+    C_CUDA(cudaSetDevice(c->device));
+    std::vector<float> pad(c->nparam_pad, 0.f);
+    logical_to_padded(p, pad, c->poff);
+    C_CUDA(cudaMemcpy(c->master, pad.data(), pad.size() * sizeof(float), cudaMemcpyHostToDevice));
+    C_CUDA(cudaMemset(c->m, 0, pad.size() * sizeof(float)));
+    C_CUDA(cudaMemset(c->v, 0, pad.size() * sizeof(float)));
+    c->step = 0;
+    const int r = refresh_all(c);
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    return r;
+}
+
+S2D_API int s2d_cnn_set_scales(s2d_cnn* c, const double* s) {
+    if (!c || !s || !(s[0] > 0) || !(s[1] > 0) || !(s[2] > 0)) return cerr(S2D_ERR_INVALID, "scales must be > 0");
+    for (int i = 0; i < 3; ++i) c->scale[i] = s[i];
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_get_scales(const s2d_cnn* c, double* s) {
+    if (!c || !s) return cerr(S2D_ERR_INVALID, "null argument");
+    for (int i = 0; i < 3; ++i) s[i] = c->scale[i];
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t B, float* y) {
+    if (!c || !x || !y || B < 1 || B > c->maxB) return cerr(S2D_ERR_INVALID, "bad batch");
+    C_CUDA(cudaSetDevice(c->device));
+    int r = upload_host_batch(c, x, nullptr, B);
+    if (r != S2D_OK) return r;
+    r = forward(c, B);
+    if (r != S2D_OK) return r;
+    const long P = (long)B * c->H * c->Wd;
+    std::vector<float> out(P);
+    C_CUDA(cudaMemcpyAsync(out.data(), c->Y, P * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    for (long i = 0; i < P; ++i) y[i] = (float)(out[i] * c->scale[2]);
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, int32_t B, float* grads,
+                              double* loss) {
+    if (!c || !x || !target || B < 1 || B > c->maxB) return cerr(S2D_ERR_INVALID, "bad batch");
+    C_CUDA(cudaSetDevice(c->device));
+    int r = upload_host_batch(c, x, target, B);
+    if (r != S2D_OK) return r;
+    if ((r = forward(c, B)) != S2D_OK) return r;
+    if ((r = loss_backward(c, B, true, loss)) != S2D_OK) return r;
+    if (grads) {
+        std::vector<float> pad(c->nparam_pad);
+        C_CUDA(cudaMemcpy(pad.data(), c->grad, pad.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        padded_to_logical(pad, grads, c->poff);
+    }
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_dataset_reserve(s2d_cnn* c, int32_t capacity) {
+    if (!c || capacity < 1) return cerr(S2D_ERR_INVALID, "bad capacity");
+    C_CUDA(cudaSetDevice(c->device));
+    if (c->data) cudaFree(c->data);
+    c->data = nullptr;
+    C_CUDA(cudaMalloc(&c->data, (size_t)capacity * c->H * c->Wd * 3 * sizeof(float)));
+    c->data_cap = capacity;
+    c->data_n = 0;
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_dataset_size(const s2d_cnn* c) {
+    if (!c) return cerr(S2D_ERR_INVALID, "null network");
+    return c->data_n;
+}
+
+S2D_API int s2d_cnn_dataset_stats(s2d_cnn* c, double* rms) {
+    if (!c || !rms || c->data_n < 1) return cerr(S2D_ERR_INVALID, "empty dataset");
+    C_CUDA(cudaSetDevice(c->device));
+    const long n = (long)c->data_n * c->H * c->Wd;
+    double* part = nullptr;
+    C_CUDA(cudaMalloc(&part, 3 * 256 * sizeof(double)));
+    k_moments<<<256, 256, 0, c->stream>>>(c->data, n, part);
+    std::vector<double> h(3 * 256);
+    cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(part);
+    if (e != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    for (int k = 0; k < 3; ++k) {
+        double s = 0.0;
+        for (int b = 0; b < 256; ++b) s += h[3 * b + k];
+        rms[k] = std::sqrt(s / (double)n);
+    }
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_train_epoch(s2d_cnn* c, int32_t first, int32_t count, int32_t batch, double lr, uint64_t seed,
+                                double* mean_loss) {
+    if (!c || batch < 1 || batch > c->maxB || first < 0 || count < batch || first + count > c->data_n)
+        return cerr(S2D_ERR_INVALID, "bad training range");
+    C_CUDA(cudaSetDevice(c->device));
+    std::vector<int> order(count);
+    for (int i = 0; i < count; ++i) order[i] = first + i;
+    for (int i = count - 1; i > 0; --i) {   // Fisher-Yates with a seeded generator
+        const int j = (int)(mix64(seed * 1315423911ULL + (uint64_t)i) % (uint64_t)(i + 1));
+        std::swap(order[i], order[j]);
+    }
+    const long HW = (long)c->H * c->Wd;
+    double tot = 0.0;
+    int nb = 0;
+    for (int s = 0; s + batch <= count; s += batch) {
+        C_CUDA(cudaMemcpyAsync(c->idx, order.data() + s, sizeof(int) * batch, cudaMemcpyHostToDevice, c->stream));
+        k_pack<<<nblocks((long)batch * HW, 256), 256, 0, c->stream>>>(
+            c->data, c->idx, batch, HW, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]),
+            (float)(1.0 / c->scale[2]), c->X0, c->tgt);
+        C_CUDA(cudaGetLastError());
+        int r = forward(c, batch);
+        double l = 0.0;
+        if (r == S2D_OK) r = loss_backward(c, batch, true, &l);
+        if (r == S2D_OK) r = adam_step(c, lr);
+        if (r != S2D_OK) return r;
+        tot += l;
+        ++nb;
+    }
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    if (mean_loss) *mean_loss = nb ? tot / nb : 0.0;
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_loss) {
+    if (!c || first < 0 || count < 1 || first + count > c->data_n) return cerr(S2D_ERR_INVALID, "bad range");
+    C_CUDA(cudaSetDevice(c->device));
+    const long HW = (long)c->H * c->Wd;
+    double tot = 0.0;
+    int nb = 0;
+    for (int s = 0; s < count; s += c->maxB) {
+        const int B = std::min(c->maxB, count - s);
+        std::vector<int> id(B);
+        for (int b = 0; b < B; ++b) id[b] = first + s + b;
+        C_CUDA(cudaMemcpyAsync(c->idx, id.data(), sizeof(int) * B, cudaMemcpyHostToDevice, c->stream));
+        k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(c->data, c->idx, B, HW, (float)(1.0 / c->scale[0]),
+                                                                  (float)(1.0 / c->scale[1]),
+                                                                  (float)(1.0 / c->scale[2]), c->X0, c->tgt);
+        int r = forward(c, B);
+        double l = 0.0;
+        if (r == S2D_OK) r = loss_backward(c, B, false, &l);
+        if (r != S2D_OK) return r;
+        tot += l * B;
+        nb += B;
+    }
+    if (mean_loss) *mean_loss = tot / nb;
+    return S2D_OK;
+}
+
+S2D_API int s2d_filter_state(s2d_handle* dns, s2d_handle* les) {
+    if (!dns || !les) return cerr(S2D_ERR_INVALID, "null handle");
+    if (dns->prec != S2D_FP64 || les->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "filtering needs FP64 handles");
+    if (les->d.K > dns->d.K) return cerr(S2D_ERR_INVALID, "the LES grid must be coarser than the DNS grid");
+    C_CUDA(cudaSetDevice(dns->device));
+    C_CUDA(cudaStreamSynchronize(les->stream));
+    const int total = les->d.KX * les->d.KY;
+    k_filter_gather<<<nblocks(total, 256), 256, 0, dns->stream>>>(dns->d, les->d, (const double2*)dns->S0, nullptr,
+                                                                   0.0, (double2*)les->S0, nullptr);
+    C_CUDA(cudaGetLastError());
+    C_CUDA(cudaStreamSynchronize(dns->stream));
+    return S2D_OK;
+}
+
+S2D_API int s2d_subgrid_flux(s2d_handle* dns, s2d_handle* les, double* pi_host) {
+    if (!dns || !les) return cerr(S2D_ERR_INVALID, "null handle");
+    if (dns->prec != S2D_FP64 || les->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "needs FP64 handles");
+    if (les->d.K > dns->d.K) return cerr(S2D_ERR_INVALID, "the LES grid must be coarser than the DNS grid");
+    C_CUDA(cudaSetDevice(dns->device));
+    int r = ensure_les_buffers(les);
+    if (r != S2D_OK) return r;
+    // N_dns: the DNS right-hand side of its current state
+    const size_t cs = (size_t)dns->d.KX * dns->d.ldS * dns->vsz;
+    if (!dns->Sdw) C_CUDA(cudaMalloc(&dns->Sdw, cs));
+    {
+        FieldSet fs{};
+        fs.nf = 2;
+        fs.op[0] = OP_U;
+        fs.op[1] = OP_V;
+        fs.out[0] = dns->I[0];
+        fs.out[1] = dns->I[1];
+        if (dns->ph.form != S2D_NL_BASDEVANT) return cerr(S2D_ERR_UNSUPPORTED, "DNS must use the Basdevant form");
+        C_CUDA(Kern<double>::yinv(dns->d, dns->S0, dns->rk2, fs, dns->tw, dns->stream, dns->L_yinv));
+        C_CUDA(Kern<double>::xpass_bas(dns->d, dns->I[0], dns->I[1], dns->tw, dns->stream, dns->L_xrow));
+        C_CUDA(Kern<double>::yfwd_rk3(dns->d, dns->I[0], dns->I[1], dns->S0, dns->S1, dns->Sdw, nullptr, 0, 0.0,
+                                      dns->ph, dns->tw, dns->flags, dns->stream, dns->L_yfwd));
+    }
+    C_CUDA(cudaStreamSynchronize(les->stream));
+    const int total = les->d.KX * les->d.KY;
+    k_filter_gather<<<nblocks(total, 256), 256, 0, dns->stream>>>(dns->d, les->d, (const double2*)dns->S0,
+                                                                   (const double2*)dns->Sdw, dns->ph.nu,
+                                                                   (double2*)les->S0, (double2*)les->pi);
+    C_CUDA(cudaGetLastError());
+    C_CUDA(cudaStreamSynchronize(dns->stream));
+    // N_les of the filtered state
+    {
+        FieldSet fs{};
+        fs.nf = 2;
+        fs.op[0] = OP_U;
+        fs.op[1] = OP_V;
+        fs.out[0] = les->I[0];
+        fs.out[1] = les->I[1];
+        C_CUDA(Kern<double>::yinv(les->d, les->S0, les->rk2, fs, les->tw, les->stream, les->L_yinv));
+        C_CUDA(Kern<double>::xpass_bas(les->d, les->I[0], les->I[1], les->tw, les->stream, les->L_xrow));
+        Phys ph = les->ph;
+        ph.alpha = 0.0;
+        ph.fk = 0;
+        C_CUDA(Kern<double>::yfwd_rk3(les->d, les->I[0], les->I[1], les->S0, les->S1, les->Sdw, nullptr, 0, 0.0, ph,
+                                      les->tw, les->flags, les->stream, les->L_yfwd));
+        k_pi_finish<<<nblocks(total, 256), 256, 0, les->stream>>>(les->d, (const double2*)les->S0,
+                                                                   (const double2*)les->Sdw, ph.nu, (double2*)les->pi);
+        C_CUDA(cudaGetLastError());
+    }
+    if (pi_host) {
+        double* d = nullptr;
+        const size_t rb = (size_t)les->grid.cISize * les->grid.nyG * 2 * sizeof(double);
+        C_CUDA(cudaMalloc(&d, rb));
+        C_CUDA(Kern<double>::compact_to_ref(les->d, les->pi, les->grid.cISize, d, nullptr, les->stream));
+        C_CUDA(cudaMemcpyAsync(pi_host, d, rb, cudaMemcpyDeviceToHost, les->stream));
+        cudaStreamSynchronize(les->stream);
+        cudaFree(d);
+    }
+    C_CUDA(cudaStreamSynchronize(les->stream));
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_dataset_add(s2d_cnn* c, s2d_handle* les) {
+    if (!c || !les || !les->pi) return cerr(S2D_ERR_INVALID, "no subgrid flux computed for this LES handle");
+    if (les->d.M != c->H) return cerr(S2D_ERR_INVALID, "network grid differs from the LES collocation grid");
+    if (c->data_n >= c->data_cap) return cerr(S2D_ERR_INVALID, "dataset full");
+    C_CUDA(cudaSetDevice(c->device));
+    const long HW = (long)les->d.M * les->d.M;
+    double* pw = les->phys;
+    double* pp = les->phys + HW;
+    double* ppi = les->phys + 2 * HW;
+    int r = state_to_phys(les, les->S0, pw, pp, true);
+    if (r == S2D_OK) r = state_to_phys(les, les->pi, ppi, nullptr, false);
+    if (r != S2D_OK) return r;
+    k_to_sample<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, ppi, HW, c->data + (size_t)c->data_n * HW * 3);
+    C_CUDA(cudaGetLastError());
+    C_CUDA(cudaStreamSynchronize(les->stream));
+    c->data_n += 1;
+    return S2D_OK;
+}
+
+S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
+    if (!les) return cerr(S2D_ERR_INVALID, "null handle");
+    if (c && les->d.M != c->H) return cerr(S2D_ERR_INVALID, "network grid differs from the LES collocation grid");
+    C_CUDA(cudaSetDevice(les->device));
+    if (c) {
+        int r = ensure_les_buffers(les);
+        if (r != S2D_OK) return r;
+        if (!les->src) C_CUDA(cudaMalloc(&les->src, (size_t)les->d.KX * les->d.ldS * sizeof(double2)));
+    } else if (les->src) {
+        C_CUDA(cudaStreamSynchronize(les->stream));
+        cudaFree(les->src);
+        les->src = nullptr;
+    }
+    les->cnn = c;
+    return S2D_OK;
+}
+
+S2D_API int s2d_les_closure_term(s2d_handle* les) {
+    if (!les || !les->cnn || !les->src) return cerr(S2D_ERR_INVALID, "no closure set");
+    s2d_cnn* c = les->cnn;
+    C_CUDA(cudaSetDevice(les->device));
+    const long HW = (long)les->d.M * les->d.M;
+    double* pw = les->phys;
+    double* pp = les->phys + HW;
+    double* ppi = les->phys + 2 * HW;
+    int r = state_to_phys(les, les->S0, pw, pp, true);
+    if (r != S2D_OK) return r;
+    k_pack_les<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, HW, (float)(1.0 / c->scale[0]),
+                                                          (float)(1.0 / c->scale[1]), c->X0);
+    C_CUDA(cudaGetLastError());
+    // the network runs on the LES stream: borrow it for the forward pass
+    cudaStream_t saved = c->stream;
+    c->stream = les->stream;
+    r = forward(c, 1);
+    c->stream = saved;
+    if (r != S2D_OK) return r;
+    k_scale_out<<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], ppi);
+    C_CUDA(cudaGetLastError());
+    C_CUDA(Kern<double>::xfwd_phys(les->d, ppi, les->I[2], les->tw, les->stream, les->L_xrow));
+    C_CUDA(Kern<double>::yfwd_store(les->d, les->I[2], les->src, les->tw, les->stream, les->L_ystore));
+    return S2D_OK;
+}
+
+S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {
+    if (!les || n < 0) return cerr(S2D_ERR_INVALID, "bad argument");
+    for (int i = 0; i < n; ++i) {
+        if (les->cnn) {
+            const int r = s2d_les_closure_term(les);
+            if (r != S2D_OK) return r;
+        }
+        const int r = s2d_integrate_one_step(les, dt);
+        if (r != S2D_OK) return r;
+    }
+    return S2D_OK;
+}
+
+}  // extern "C"

@@ -123,6 +123,8 @@ struct Kern {
 
 }  // namespace s2d
 
+struct s2d_cnn;
+
 // One simulation: configuration, plan, launch shapes and device buffers.
 struct s2d_handle {
     s2d_config cfg;
@@ -138,6 +140,9 @@ struct s2d_handle {
     void* S1 = nullptr;  // stage vorticity
     void* Sdw = nullptr; // dW for compute_rhs (lazily allocated)
     void* src = nullptr; // optional additive source of dW (compact layout), e.g. a closure term
+    void* pi = nullptr;  // subgrid flux of the filtered DNS (compact layout, LES handles)
+    double* phys = nullptr;        // 3 physical fields on the collocation grid (closure)
+    struct s2d_cnn* cnn = nullptr; // closure network used by s2d_les_integrate_steps
     void* Ibase = nullptr;
     void* I[3] = {nullptr, nullptr, nullptr};
     size_t Ibytes = 0;

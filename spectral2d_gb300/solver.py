@@ -294,3 +294,123 @@ class Ensemble:
         t, c, ms = C.c_int32(), C.c_int32(), C.c_double()
         L.check(self._L.s2d_batch_tune(self._b, C.byref(t), C.byref(c), C.byref(ms)))
         return t.value, c.value, ms.value
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+class ClosureNet:
+    """The subgrid-closure CNN (6 circular 3x3 layers, 32 channels, GELU,
+    BF16 activations/weights with FP32 accumulation, Adam) on the LES
+    collocation grid ``grid`` x ``grid``."""
+
+    def __init__(self, grid: int, max_batch: int = 64, seed: int = 0, device: int = 0):
+        self._L = L.lib()
+        c = C.c_void_p()
+        L.check(self._L.s2d_cnn_create(grid, max_batch, seed, device, C.byref(c)))
+        self._c = c
+        self.grid = grid
+        self.max_batch = max_batch
+
+    def close(self) -> None:
+        if getattr(self, "_c", None):
+            self._L.s2d_cnn_destroy(self._c)
+            self._c = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):  # pragma: no cover
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def num_params(self) -> int:
+        return L.check(self._L.s2d_cnn_num_params(self._c))
+
+    def get_params(self) -> np.ndarray:
+        p = np.zeros(self.num_params, dtype=np.float32)
+        L.check(self._L.s2d_cnn_get_params(self._c, _fptr(p)))
+        return p
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.num_params
+        L.check(self._L.s2d_cnn_set_params(self._c, _fptr(p)))
+
+    def set_scales(self, rms) -> None:
+        a = np.ascontiguousarray(rms, dtype=np.float64)
+        L.check(self._L.s2d_cnn_set_scales(self._c, _dptr(a)))
+
+    def get_scales(self) -> np.ndarray:
+        a = np.zeros(3)
+        L.check(self._L.s2d_cnn_get_scales(self._c, _dptr(a)))
+        return a
+
+    def forward(self, x: np.ndarray) -> np.ndarray:
+        """x: (B, grid, grid, 2) (w, psi) -> (B, grid, grid) Pi."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        y = np.zeros(x.shape[:3], dtype=np.float32)
+        L.check(self._L.s2d_cnn_forward_host(self._c, _fptr(x), x.shape[0], _fptr(y)))
+        return y
+
+    def grad(self, x: np.ndarray, target: np.ndarray):
+        """(loss, gradient) of the normalised MSE for one batch."""
+        x = np.ascontiguousarray(x, dtype=np.float32)
+        t = np.ascontiguousarray(target, dtype=np.float32)
+        g = np.zeros(self.num_params, dtype=np.float32)
+        loss = C.c_double()
+        L.check(self._L.s2d_cnn_grad_host(self._c, _fptr(x), _fptr(t), x.shape[0], _fptr(g), C.byref(loss)))
+        return loss.value, g
+
+    def reserve(self, capacity: int) -> None:
+        L.check(self._L.s2d_cnn_dataset_reserve(self._c, capacity))
+
+    def add_sample(self, les: Spectral2D) -> None:
+        L.check(self._L.s2d_cnn_dataset_add(self._c, les._h))
+
+    @property
+    def dataset_size(self) -> int:
+        return L.check(self._L.s2d_cnn_dataset_size(self._c))
+
+    def dataset_stats(self) -> np.ndarray:
+        a = np.zeros(3)
+        L.check(self._L.s2d_cnn_dataset_stats(self._c, _dptr(a)))
+        return a
+
+    def train_epoch(self, first: int, count: int, batch: int, lr: float, seed: int) -> float:
+        loss = C.c_double()
+        L.check(self._L.s2d_cnn_train_epoch(self._c, first, count, batch, lr, seed, C.byref(loss)))
+        return loss.value
+
+    def eval(self, first: int, count: int) -> float:
+        loss = C.c_double()
+        L.check(self._L.s2d_cnn_eval(self._c, first, count, C.byref(loss)))
+        return loss.value
+
+
+def filter_state(dns: Spectral2D, les: Spectral2D) -> None:
+    """LES state := sharp spectral filter of the DNS state."""
+    L.check(L.lib().s2d_filter_state(dns._h, les._h))
+
+
+def subgrid_flux(dns: Spectral2D, les: Spectral2D, host: bool = False):
+    """Filter the DNS into the LES and form the subgrid flux Pi^ on the LES
+    grid (returned in the reference layout when ``host``)."""
+    out = np.zeros(les.shape, dtype=np.complex128) if host else None
+    L.check(L.lib().s2d_subgrid_flux(dns._h, les._h, _dptr(out.view(np.float64)) if host else None))
+    return out
+
+
+def les_set_closure(les: Spectral2D, net: ClosureNet | None) -> None:
+    L.check(L.lib().s2d_les_set_closure(les._h, net._c if net is not None else None))
+
+
+def les_integrate_steps(les: Spectral2D, n: int, dt: float) -> None:
+    L.check(L.lib().s2d_les_integrate_steps(les._h, n, dt))

@@ -1,0 +1,138 @@
+"""GPU tests of the learned-closure pieces: the CNN's forward pass and
+gradients against the FP64 numpy oracle (oracle/cnn_oracle.py, fed the same
+BF16-rounded weights and inputs; tolerances cover the BF16 rounding of the
+GPU's intermediate activations), the subgrid flux against the spectral
+oracle, training reducing the loss, and the LES step with the closure."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from oracle import cnn_oracle as CO
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def S(built_lib):
+    import spectral2d_gb300 as S
+    return S
+
+
+def _oracle_params(p, bf=True):
+    out, o = [], 0
+    for l in range(6):
+        ci, co = CO.CHANNELS[l], CO.CHANNELS[l + 1]
+        W = p[o:o + co * 9 * ci].reshape(co, 9, ci).astype(np.float64)
+        o += co * 9 * ci
+        b = p[o:o + co].astype(np.float64)
+        o += co
+        out.append((CO.bf16(W) if bf else W, b))
+    return out
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def test_cnn_forward_and_gradients_vs_oracle(S):
+    grid, B = 24, 2
+    rng = np.random.default_rng(0)
+    with S.ClosureNet(grid, max_batch=4, seed=3) as net:
+        net.set_scales([1.0, 1.0, 1.0])
+        p = net.get_params()
+        assert p.size == 608 + 4 * 9248 + 289
+        x = rng.standard_normal((B, grid, grid, 2)).astype(np.float32)
+        t = (0.3 * rng.standard_normal((B, grid, grid))).astype(np.float32)
+        y = net.forward(x)
+        loss, g = net.grad(x, t)
+    params = _oracle_params(p)
+    xb = CO.bf16(x)
+    yo, _ = CO.forward(params, xb)
+    assert _rel(y, yo) < 2e-2
+    lo, go, _ = CO.loss_and_grads(params, xb, t.astype(np.float64))
+    assert abs(loss - lo) < 2e-2 * lo
+    gp = _oracle_params(g, bf=False)
+    for l in range(6):
+        eW, eb = _rel(gp[l][0], go[l][0]), _rel(gp[l][1], go[l][1])
+        print(f"layer {l}: dW rel {eW:.2e}, db rel {eb:.2e}")
+        assert eW < 5e-2 and eb < 5e-2
+
+
+def test_subgrid_flux_vs_oracle(S):
+    nd, nl, nu = 64, 16, 2e-3
+    gd, gl = O.get_grid_size(nd, nd), O.get_grid_size(nl, nl)
+    w = O.random_state(gd, 17, decay=0.05)
+    with S.Spectral2D(nd, nu=nu) as dns, S.Spectral2D(nl, nu=nu) as les:
+        dns.set_state(w)
+        pi = S.subgrid_flux(dns, les, host=True)
+        wl, _ = les.get_state()
+    wo = O.truncate(w, gd)
+    po = O.truncate(O.compute_psi(wo, gd), gd)
+    dW, _ = O.compute_rhs(wo, po, gd, nu, round_trip=False)
+    Nd = -(O.truncate(dW, gd) + nu * (gd.kx ** 2 + gd.ky ** 2) * wo)
+    # sharp filter to the LES modes |k| <= nl/2
+    def to_les(a):
+        out = np.zeros((gl.nyG, gl.cISize), complex)
+        K = nl // 2
+        for ky in range(-K, K + 1):
+            for kx in range(0, K + 1):
+                if kx * kx + ky * ky <= K * K:
+                    out[ky % gl.nyG, kx] = a[ky % gd.nyG, kx]
+        return out
+    wf = to_les(wo)
+    assert O.rel_l2(wl, wf) < 1e-15
+    pf = O.truncate(O.compute_psi(wf, gl), gl)
+    dWl, _ = O.compute_rhs(wf, pf, gl, nu, round_trip=False)
+    Nl = -(O.truncate(dWl, gl) + nu * (gl.kx ** 2 + gl.ky ** 2) * wf)
+    pio = O.truncate(to_les(Nd) - Nl, gl)
+    assert O.rel_l2(pi, pio) < 1e-12
+
+
+def _dataset(S, net, nd=64, nl=16, nsnap=48, every=4):
+    with S.Spectral2D(nd, nu=2e-3) as dns, S.Spectral2D(nl, nu=2e-3) as les:
+        dns.set_turbulent_velocity(seed=5, spectrum="k4gauss", k0=4.0, tke=0.5)
+        dt = dns.compute_time_step(0.5)
+        net.reserve(nsnap)
+        for _ in range(nsnap):
+            dns.integrate_steps(every, dt)
+            S.subgrid_flux(dns, les)
+            net.add_sample(les)
+    return dt
+
+
+def test_training_reduces_loss(S):
+    with S.ClosureNet(24, max_batch=8, seed=1) as net:
+        _dataset(S, net)
+        assert net.dataset_size == 48
+        rms = net.dataset_stats()
+        assert np.all(rms > 0)
+        net.set_scales(rms)
+        l0 = net.eval(0, 48)
+        losses = [net.train_epoch(0, 40, 8, 1e-3, seed=e) for e in range(40)]
+        l1 = net.eval(0, 48)
+        print(f"loss {l0:.3f} -> {l1:.3f}; epoch losses {losses[0]:.3f} ... {losses[-1]:.3f}")
+        assert l1 < 0.7 * l0
+
+
+def test_les_with_closure_runs_and_changes_the_solution(S):
+    with S.ClosureNet(24, max_batch=8, seed=2) as net:
+        dt = _dataset(S, net, nsnap=16)
+        net.set_scales(net.dataset_stats())
+        for e in range(5):
+            net.train_epoch(0, 16, 8, 1e-3, seed=e)
+        with S.Spectral2D(16, nu=2e-3) as a, S.Spectral2D(16, nu=2e-3) as b:
+            w0 = O.random_state(O.get_grid_size(16, 16), 4, decay=0.2)
+            a.set_state(w0)
+            b.set_state(w0)
+            S.les_set_closure(a, net)
+            S.les_integrate_steps(a, 20, dt)
+            S.les_integrate_steps(b, 20, dt)
+            a.check_finite()
+            wa, _ = a.get_state()
+            wb, _ = b.get_state()
+            S.les_set_closure(a, None)
+    assert np.all(np.isfinite(wa))
+    d = O.rel_l2(wa, wb)
+    print(f"closure changes the 20-step LES state by rel-L2 {d:.2e}")
+    assert 1e-8 < d < 0.5
