@@ -144,7 +144,11 @@ int kIntMaxBins(int kxMG, int kyMG) {
 
 namespace {
 
-int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_group, int target_threads,
+// G transforms of threads_per_group threads per CTA: at most target_threads
+// per CTA, at least one warp, and no more transforms per CTA than spread the
+// kernel's `items` transforms over two CTAs per SM (small grids would
+// otherwise leave most SMs idle).
+int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_group, int target_threads, long items,
                 Launch* L, const char* what) {
     const size_t cap_pair = (size_t)h->max_smem / 2;
     if (bytes_per_group > (size_t)h->max_smem)
@@ -152,7 +156,10 @@ int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_gro
                     bytes_per_group, h->max_smem);
     if (threads_per_group > 512)
         return fail(S2D_ERR_UNSUPPORTED, "%s: %d threads per transform exceed 512", what, threads_per_group);
-    int G = std::max(1, target_threads / threads_per_group);
+    const int gmax = std::max(1, target_threads / threads_per_group);
+    const int gmin = std::max(1, (32 + threads_per_group - 1) / threads_per_group);
+    const long gfill = (items + 2L * h->sms - 1) / (2L * h->sms);
+    int G = (int)std::max<long>(gmin, std::min<long>(gmax, gfill));
     while (G > 1 && (G * threads_per_group > 512 || G * bytes_per_group > cap_pair)) --G;
     L->G = G;
     L->threads = G * threads_per_group;
@@ -388,6 +395,7 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     if (cudaGetDeviceProperties(&prop, h->device) != cudaSuccess)
         return bail(fail(S2D_ERR_CUDA, "cudaGetDeviceProperties failed"));
     h->max_smem = (int)prop.sharedMemPerBlockOptin - 1024;
+    h->sms = prop.multiProcessorCount;
     {
         static bool configured[64] = {false};
         if (h->device >= 0 && h->device < 64 && !configured[h->device]) {
@@ -456,19 +464,21 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     const size_t tb = (size_t)d.M * h->vsz;
     const int tgt = 256;
     int rr;
-    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_yinv, "inverse y-pass")) != S2D_OK) return bail(rr);
-    if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, &h->L_xpass, "x-pass")) != S2D_OK) return bail(rr);
+    const int nf = h->ph.form == S2D_NL_BASDEVANT ? 2 : 3;
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, (long)nf * d.KX, &h->L_yinv, "inverse y-pass")) != S2D_OK)
+        return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, d.M / 2, &h->L_xpass, "x-pass")) != S2D_OK) return bail(rr);
     {
         // forward y-pass: G columns x 2 fields, run in rounds of c transforms
         Launch L{};
-        if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, &L, "forward y-pass")) != S2D_OK) return bail(rr);
+        if ((rr = pick_launch(h, d.Tg, 2 * tb, tgt, d.KX, &L, "forward y-pass")) != S2D_OK) return bail(rr);
         int c = std::max(1, std::min(2 * L.G, tgt / d.Tg));
         while ((2 * L.G) % c) --c;
         L.threads = c * d.Tg;
         h->L_yfwd = L;
     }
-    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
-    if ((rr = pick_launch(h, d.Tg, tb, tgt, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, d.M, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, d.KX, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
     *out = h;

@@ -257,20 +257,43 @@ __global__ void k_refresh(const float* __restrict__ Wm, int CO, int CI, __nv_bfl
     }
 }
 
-// Network input (channels 0, 1 = w / s0, psi / s1; 2..15 = 0) and target
-// (Pi / s2) of a batch, from dataset samples idx[b] (FP32 [HW][3]).
-__global__ void k_pack(const float* __restrict__ data, const int* __restrict__ idx, int B, long HW, float r0,
-                       float r1, float r2, __nv_bfloat16* x, float* tgt) {
+// Network input (channels 0, 1 = w / (a s0), psi / (a s1); 2..15 = 0) and
+// target (Pi / (a^2 s2)) of a batch, from dataset samples idx[b] (FP32
+// [HW][3]); a = amp[idx[b]] is the sample's rms vorticity (1 when amp is
+// null).  Dividing by a and a^2 makes the closure equivariant to the
+// amplitude of the flow: Pi is quadratic in w.
+__global__ void k_pack(const float* __restrict__ data, const float* __restrict__ amp,
+                       const int* __restrict__ idx, int B, long HW, float r0, float r1, float r2,
+                       __nv_bfloat16* x, float* tgt) {
     const long P = (long)B * HW;
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < P; p += (long)gridDim.x * blockDim.x) {
         const long b = p / HW, q = p - b * HW;
         const float* s = data + ((long)idx[b] * HW + q) * 3;
+        const float ia = amp ? 1.f / amp[idx[b]] : 1.f;
         uint32_t* xr = reinterpret_cast<uint32_t*>(x + p * 16);
-        xr[0] = pack_bf16(s[0] * r0, s[1] * r1);
+        xr[0] = pack_bf16(s[0] * r0 * ia, s[1] * r1 * ia);
         for (int c = 1; c < 8; ++c) xr[c] = 0u;
-        if (tgt) tgt[p] = s[2] * r2;
+        if (tgt) tgt[p] = s[2] * r2 * ia * ia;
     }
 }
+
+// sum of squares of n doubles, accumulated into *acc (zeroed by the caller)
+__global__ void k_sumsq(const double* __restrict__ v, long n, double* acc) {
+    __shared__ double red[256];
+    double s = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        s += v[i] * v[i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) atomicAdd(acc, red[0]);
+}
+
+// amp[i] = sqrt(*acc / n)
+__global__ void k_store_rms(const double* __restrict__ acc, long n, float* amp) { *amp = (float)sqrt(*acc / (double)n); }
 
 // ---- LES-side kernels ---------------------------------------------------
 
@@ -365,30 +388,38 @@ __global__ void k_to_sample(const double* __restrict__ w, const double* __restri
     }
 }
 
-// Network input of one LES state: channels (w / s0, psi / s1).
+// Network input of one LES state: channels (w / (a s0), psi / (a s1)) with
+// a = sqrt(*sumsq / HW), the state's rms vorticity.
 __global__ void k_pack_les(const double* __restrict__ w, const double* __restrict__ p, long HW, float r0, float r1,
-                           __nv_bfloat16* x) {
+                           const double* __restrict__ sumsq, __nv_bfloat16* x) {
+    const double ia = 1.0 / sqrt(*sumsq / (double)HW);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
         uint32_t* xr = reinterpret_cast<uint32_t*>(x + i * 16);
-        xr[0] = pack_bf16((float)(w[i] * r0), (float)(p[i] * r1));
+        xr[0] = pack_bf16((float)(w[i] * r0 * ia), (float)(p[i] * r1 * ia));
         for (int c = 1; c < 8; ++c) xr[c] = 0u;
     }
 }
 
-// phys = scale * y (network output, FP32) as FP64.
-__global__ void k_scale_out(const float* __restrict__ y, long n, double scale, double* phys) {
+// phys = scale * a^2 * y (network output) as FP64, a^2 = *sumsq / HW.
+__global__ void k_scale_out(const float* __restrict__ y, long n, double scale, const double* __restrict__ sumsq,
+                            double* phys) {
+    const double s = scale * (*sumsq / (double)n);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        phys[i] = scale * (double)y[i];
+        phys[i] = s * (double)y[i];
 }
 
-// Moments of the dataset: per-block sums of squares of the 3 channels.
-__global__ void k_moments(const float* __restrict__ data, long n, double* part) {
+// Moments of the dataset after the per-sample amplitude normalisation:
+// per-block sums of (w/a)^2, (psi/a)^2, (Pi/a^2)^2.
+__global__ void k_moments(const float* __restrict__ data, const float* __restrict__ amp, long HW, long n,
+                          double* part) {
     __shared__ double red[3][256];
     double s0 = 0, s1 = 0, s2 = 0;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-        s0 += (double)data[3 * i] * data[3 * i];
-        s1 += (double)data[3 * i + 1] * data[3 * i + 1];
-        s2 += (double)data[3 * i + 2] * data[3 * i + 2];
+        const double ia = 1.0 / (double)amp[i / HW];
+        const double a = data[3 * i] * ia, b = data[3 * i + 1] * ia, c = data[3 * i + 2] * ia * ia;
+        s0 += a * a;
+        s1 += b * b;
+        s2 += c * c;
     }
     red[0][threadIdx.x] = s0;
     red[1][threadIdx.x] = s1;
@@ -425,6 +456,8 @@ struct s2d_cnn {
     double* lpart = nullptr;
     int* idx = nullptr;
     float* data = nullptr;
+    float* amp = nullptr;       // per-sample rms vorticity
+    double* sumsq = nullptr;    // scratch accumulator (rms of one state)
     int data_cap = 0, data_n = 0;
     double scale[3] = {1.0, 1.0, 1.0};
     long step = 0;
@@ -580,7 +613,7 @@ int upload_host_batch(s2d_cnn* c, const float* x, const float* target, int B) {
     for (int b = 0; b < B; ++b) id[b] = b;
     C_CUDA(cudaMemcpyAsync(tmp, s.data(), s.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     C_CUDA(cudaMemcpyAsync(idx, id.data(), sizeof(int) * B, cudaMemcpyHostToDevice, c->stream));
-    k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(tmp, idx, B, HW, (float)(1.0 / c->scale[0]),
+    k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(tmp, nullptr, idx, B, HW, (float)(1.0 / c->scale[0]),
                                                               (float)(1.0 / c->scale[1]), (float)(1.0 / c->scale[2]),
                                                               c->X0, c->tgt);
     cudaError_t e = cudaGetLastError();
@@ -665,7 +698,8 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
               cudaMalloc(&c->tgt, P * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&c->part, c->part_n * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&c->lpart, 256 * sizeof(double)) == cudaSuccess &&
-              cudaMalloc(&c->idx, max_batch * sizeof(int)) == cudaSuccess;
+              cudaMalloc(&c->idx, max_batch * sizeof(int)) == cudaSuccess &&
+              cudaMalloc(&c->sumsq, 64) == cudaSuccess;
     for (int l = 0; l < kLayers && ok; ++l) {
         const size_t n = (size_t)kCoutP[l] * 9 * kCinP[l] * sizeof(__nv_bfloat16);
         ok = cudaMalloc(&c->Wb[l], n) == cudaSuccess && cudaMalloc(&c->WTb[l], n) == cudaSuccess;
@@ -708,7 +742,7 @@ S2D_API void s2d_cnn_destroy(s2d_cnn* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* ptrs[] = {c->master, c->grad, c->m, c->v, c->X0, c->dZ6, c->dZa, c->dZb, c->Y, c->tgt, c->part,
-                    c->lpart, c->idx, c->data};
+                    c->lpart, c->idx, c->data, c->amp, c->sumsq};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int l = 0; l < kLayers; ++l) {
@@ -800,6 +834,9 @@ S2D_API int s2d_cnn_dataset_reserve(s2d_cnn* c, int32_t capacity) {
     if (c->data) cudaFree(c->data);
     c->data = nullptr;
     C_CUDA(cudaMalloc(&c->data, (size_t)capacity * c->H * c->Wd * 3 * sizeof(float)));
+    if (c->amp) cudaFree(c->amp);
+    c->amp = nullptr;
+    C_CUDA(cudaMalloc(&c->amp, (size_t)capacity * sizeof(float)));
     c->data_cap = capacity;
     c->data_n = 0;
     return S2D_OK;
@@ -816,7 +853,7 @@ S2D_API int s2d_cnn_dataset_stats(s2d_cnn* c, double* rms) {
     const long n = (long)c->data_n * c->H * c->Wd;
     double* part = nullptr;
     C_CUDA(cudaMalloc(&part, 3 * 256 * sizeof(double)));
-    k_moments<<<256, 256, 0, c->stream>>>(c->data, n, part);
+    k_moments<<<256, 256, 0, c->stream>>>(c->data, c->amp, (long)c->H * c->Wd, n, part);
     std::vector<double> h(3 * 256);
     cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     cudaError_t e = cudaStreamSynchronize(c->stream);
@@ -847,7 +884,7 @@ S2D_API int s2d_cnn_train_epoch(s2d_cnn* c, int32_t first, int32_t count, int32_
     for (int s = 0; s + batch <= count; s += batch) {
         C_CUDA(cudaMemcpyAsync(c->idx, order.data() + s, sizeof(int) * batch, cudaMemcpyHostToDevice, c->stream));
         k_pack<<<nblocks((long)batch * HW, 256), 256, 0, c->stream>>>(
-            c->data, c->idx, batch, HW, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]),
+            c->data, c->amp, c->idx, batch, HW, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]),
             (float)(1.0 / c->scale[2]), c->X0, c->tgt);
         C_CUDA(cudaGetLastError());
         int r = forward(c, batch);
@@ -874,7 +911,8 @@ S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_
         std::vector<int> id(B);
         for (int b = 0; b < B; ++b) id[b] = first + s + b;
         C_CUDA(cudaMemcpyAsync(c->idx, id.data(), sizeof(int) * B, cudaMemcpyHostToDevice, c->stream));
-        k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(c->data, c->idx, B, HW, (float)(1.0 / c->scale[0]),
+        k_pack<<<nblocks((long)B * HW, 256), 256, 0, c->stream>>>(c->data, c->amp, c->idx, B, HW,
+                                                                  (float)(1.0 / c->scale[0]),
                                                                   (float)(1.0 / c->scale[1]),
                                                                   (float)(1.0 / c->scale[2]), c->X0, c->tgt);
         int r = forward(c, B);
@@ -978,6 +1016,10 @@ S2D_API int s2d_cnn_dataset_add(s2d_cnn* c, s2d_handle* les) {
     if (r != S2D_OK) return r;
     k_to_sample<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, ppi, HW, c->data + (size_t)c->data_n * HW * 3);
     C_CUDA(cudaGetLastError());
+    C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
+    k_sumsq<<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
+    k_store_rms<<<1, 1, 0, les->stream>>>(c->sumsq, HW, c->amp + c->data_n);
+    C_CUDA(cudaGetLastError());
     C_CUDA(cudaStreamSynchronize(les->stream));
     c->data_n += 1;
     return S2D_OK;
@@ -1010,8 +1052,10 @@ S2D_API int s2d_les_closure_term(s2d_handle* les) {
     double* ppi = les->phys + 2 * HW;
     int r = state_to_phys(les, les->S0, pw, pp, true);
     if (r != S2D_OK) return r;
+    C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
+    k_sumsq<<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
     k_pack_les<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, HW, (float)(1.0 / c->scale[0]),
-                                                          (float)(1.0 / c->scale[1]), c->X0);
+                                                          (float)(1.0 / c->scale[1]), c->sumsq, c->X0);
     C_CUDA(cudaGetLastError());
     // the network runs on the LES stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
@@ -1019,7 +1063,7 @@ S2D_API int s2d_les_closure_term(s2d_handle* les) {
     r = forward(c, 1);
     c->stream = saved;
     if (r != S2D_OK) return r;
-    k_scale_out<<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], ppi);
+    k_scale_out<<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], c->sumsq, ppi);
     C_CUDA(cudaGetLastError());
     C_CUDA(Kern<double>::xfwd_phys(les->d, ppi, les->I[2], les->tw, les->stream, les->L_xrow));
     C_CUDA(Kern<double>::yfwd_store(les->d, les->I[2], les->src, les->tw, les->stream, les->L_ystore));
@@ -1028,14 +1072,28 @@ S2D_API int s2d_les_closure_term(s2d_handle* les) {
 
 S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {
     if (!les || n < 0) return cerr(S2D_ERR_INVALID, "bad argument");
-    for (int i = 0; i < n; ++i) {
-        if (les->cnn) {
-            const int r = s2d_les_closure_term(les);
-            if (r != S2D_OK) return r;
-        }
-        const int r = s2d_integrate_one_step(les, dt);
-        if (r != S2D_OK) return r;
+    if (!les->cnn) return s2d_integrate_steps(les, n, dt);
+    if (n == 0) return S2D_OK;
+    C_CUDA(cudaSetDevice(les->device));
+    // one step (closure term + RK3 step) captured as a CUDA graph, rebuilt
+    // on every call so that it picks up new network scales and dt
+    C_CUDA(cudaStreamBeginCapture(les->stream, cudaStreamCaptureModeThreadLocal));
+    int r = s2d_les_closure_term(les);
+    if (r == S2D_OK) r = s2d_integrate_one_step(les, dt);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(les->stream, &g);
+    if (r != S2D_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return r != S2D_OK ? r : cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
     }
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t e2 = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e2));
+    cudaError_t e3 = cudaSuccess;
+    for (int i = 0; i < n && e3 == cudaSuccess; ++i) e3 = cudaGraphLaunch(x, les->stream);
+    cudaGraphExecDestroy(x);
+    if (e3 != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e3));
     return S2D_OK;
 }
 

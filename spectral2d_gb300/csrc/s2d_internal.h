@@ -159,6 +159,7 @@ struct s2d_handle {
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0.0;
     int max_smem = 0;
+    int sms = 152;
 };
 
 namespace s2d {
