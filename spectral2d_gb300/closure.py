@@ -10,8 +10,9 @@
    collocation grid (192^2) become one training pair.
 2. Training: Adam (lr 1e-3, batch 64) over the pairs of the training seeds,
    the last 10% held out as validation.
-3. Evaluation on held-out seeds: the DNS and two 128^2 LES runs started from
-   the filtered DNS state -- one with the trained closure, one without (the
+3. Evaluation on held-out seeds: the DNS and two 128^2 LES runs (FP32 by
+   default; the DNS that makes the data stays FP64) started from the
+   filtered DNS state -- one with the trained closure, one without (the
    fallback) -- advance with the same dt; the energy spectra E(k) of the LES
    runs are compared with the filtered DNS for k <= 40, together with the
    enstrophy, and the wall-clock per step of each solver is measured.
@@ -76,12 +77,13 @@ def _rel_err(a, b, kmax):
     return np.abs(a[k] - b[k]) / np.abs(b[k])
 
 
-def evaluate(net, seeds, n_dns, n_les, nu, cfl, steps, every, log=print):
+def evaluate(net, seeds, n_dns, n_les, nu, cfl, steps, every, les_precision="fp32", log=print):
     """DNS vs LES with and without the closure on held-out seeds."""
     out = []
     for s in seeds:
         with S.Spectral2D(n_dns, nu=nu) as dns, S.Spectral2D(n_les, nu=nu) as filt, \
-                S.Spectral2D(n_les, nu=nu) as les_c, S.Spectral2D(n_les, nu=nu) as les_0:
+                S.Spectral2D(n_les, nu=nu, precision=les_precision) as les_c, \
+                S.Spectral2D(n_les, nu=nu, precision=les_precision) as les_0:
             dns.set_turbulent_velocity(seed=s, spectrum="k4gauss", k0=10.0, tke=0.5)
             dt = dns.compute_time_step(cfl)
             S.filter_state(dns, les_c)
@@ -163,6 +165,7 @@ def main(argv=None):
     ap.add_argument("--eval-seeds", type=str, default="8,9")
     ap.add_argument("--eval-steps", type=int, default=20000)
     ap.add_argument("--eval-every", type=int, default=1000)
+    ap.add_argument("--les-precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--weights", default=None)
     ap.add_argument("--load", default=None, help="skip data and training; use these weights")
     ap.add_argument("--out", default=None)
@@ -183,7 +186,8 @@ def main(argv=None):
             if a.weights:
                 save_weights(net, a.weights)
         ev = [int(s) for s in a.eval_seeds.split(",") if s]
-        res["eval"] = evaluate(net, ev, a.n_dns, a.n_les, a.nu, a.cfl, a.eval_steps, a.eval_every)
+        res["eval"] = evaluate(net, ev, a.n_dns, a.n_les, a.nu, a.cfl, a.eval_steps, a.eval_every,
+                               a.les_precision)
     if a.out:
         with open(a.out, "w") as f:
             json.dump(res, f)

@@ -278,11 +278,12 @@ __global__ void k_pack(const float* __restrict__ data, const float* __restrict__
 }
 
 // sum of squares of n doubles, accumulated into *acc (zeroed by the caller)
-__global__ void k_sumsq(const double* __restrict__ v, long n, double* acc) {
+template <typename T>
+__global__ void k_sumsq(const T* __restrict__ v, long n, double* acc) {
     __shared__ double red[256];
     double s = 0.0;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        s += v[i] * v[i];
+        s += (double)v[i] * (double)v[i];
     red[threadIdx.x] = s;
     __syncthreads();
     for (int w = blockDim.x / 2; w > 0; w >>= 1) {
@@ -297,9 +298,11 @@ __global__ void k_store_rms(const double* __restrict__ acc, long n, float* amp) 
 
 // ---- LES-side kernels ---------------------------------------------------
 
-// Sharp filter DNS -> LES (|k| <= K_les) of w, and N_dns = -(dW + nu k^2 w).
+// Sharp filter DNS -> LES (|k| <= K_les) of w (LES state in FP64 or FP32),
+// and N_dns = -(dW + nu k^2 w) when dWd is given.
+template <typename VTL>
 __global__ void k_filter_gather(Dims dd, Dims dl, const double2* __restrict__ wd, const double2* __restrict__ dWd,
-                                double nu_d, double2* wl, double2* pil) {
+                                double nu_d, VTL* wl, double2* pil) {
     const int total = dl.KX * dl.KY;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
         const int kx = i / dl.KY, jc = i - kx * dl.KY;
@@ -316,7 +319,8 @@ __global__ void k_filter_gather(Dims dd, Dims dl, const double2* __restrict__ wd
             }
         }
         const size_t ol = (size_t)kx * dl.ldS + jc;
-        wl[ol] = w;
+        wl[ol].x = w.x;
+        wl[ol].y = w.y;
         if (pil) pil[ol] = nl;
     }
 }
@@ -341,30 +345,32 @@ __global__ void k_pi_finish(Dims dl, const double2* __restrict__ w, const double
 
 // Physical rows of two spectral fields X, Y (half-spectral rows, Y may be
 // null): one inverse FFT of X + iY per row, real part -> ox, imaginary -> oy.
-__global__ void __launch_bounds__(512) k_xinv_phys2(Dims d, const double2* __restrict__ X,
-                                                    const double2* __restrict__ Y, const double2* __restrict__ tw,
-                                                    int G, double* ox, double* oy) {
+template <typename T>
+__global__ void __launch_bounds__(512) k_xinv_phys2(Dims d, const typename Vec<T>::t* __restrict__ X,
+                                                    const typename Vec<T>::t* __restrict__ Y,
+                                                    const typename Vec<T>::t* __restrict__ tw, int G, T* ox, T* oy) {
+    using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double2* bufs = reinterpret_cast<double2*>(smem_raw);
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
     const int g = threadIdx.x / d.Tg;
     const int lane = threadIdx.x - g * d.Tg;
     const int y = blockIdx.x * G + g;
     const bool active = y < d.M;
-    double2* Z = bufs + (size_t)g * d.M;
+    VT* Z = bufs + (size_t)g * d.M;
     const int yy = active ? y : 0;
     if (Y) {
         build_pair(Z, X + (size_t)yy * d.ldI, Y + (size_t)yy * d.ldI, d, lane, active);
     } else {
         // X alone: Z = X Hermitian-extended
         for (int n = lane; n < d.M; n += d.Tg) {
-            double2 z = make_double2(0.0, 0.0);
+            VT z = mk<VT>((T)0, (T)0);
             if (active) {
-                const double2* Xr = X + (size_t)yy * d.ldI;
-                if (n == 0) z = make_double2(__ldcg(&Xr[0]).x, 0.0);
+                const VT* Xr = X + (size_t)yy * d.ldI;
+                if (n == 0) z = mk<VT>(__ldcg(&Xr[0]).x, (T)0);
                 else if (n <= d.K) z = __ldcg(&Xr[n]);
                 else if (n >= d.M - d.K) {
-                    const double2 a = __ldcg(&Xr[d.M - n]);
-                    z = make_double2(a.x, -a.y);
+                    const VT a = __ldcg(&Xr[d.M - n]);
+                    z = mk<VT>(a.x, -a.y);
                 }
             }
             Z[n] = z;
@@ -390,22 +396,24 @@ __global__ void k_to_sample(const double* __restrict__ w, const double* __restri
 
 // Network input of one LES state: channels (w / (a s0), psi / (a s1)) with
 // a = sqrt(*sumsq / HW), the state's rms vorticity.
-__global__ void k_pack_les(const double* __restrict__ w, const double* __restrict__ p, long HW, float r0, float r1,
+template <typename T>
+__global__ void k_pack_les(const T* __restrict__ w, const T* __restrict__ p, long HW, float r0, float r1,
                            const double* __restrict__ sumsq, __nv_bfloat16* x) {
     const double ia = 1.0 / sqrt(*sumsq / (double)HW);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
         uint32_t* xr = reinterpret_cast<uint32_t*>(x + i * 16);
-        xr[0] = pack_bf16((float)(w[i] * r0 * ia), (float)(p[i] * r1 * ia));
+        xr[0] = pack_bf16((float)((double)w[i] * r0 * ia), (float)((double)p[i] * r1 * ia));
         for (int c = 1; c < 8; ++c) xr[c] = 0u;
     }
 }
 
 // phys = scale * a^2 * y (network output) as FP64, a^2 = *sumsq / HW.
+template <typename T>
 __global__ void k_scale_out(const float* __restrict__ y, long n, double scale, const double* __restrict__ sumsq,
-                            double* phys) {
+                            T* phys) {
     const double s = scale * (*sumsq / (double)n);
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        phys[i] = s * (double)y[i];
+        phys[i] = (T)(s * (double)y[i]);
 }
 
 // Moments of the dataset after the per-sample amplitude normalisation:
@@ -624,34 +632,65 @@ int upload_host_batch(s2d_cnn* c, const float* x, const float* target, int B) {
     return S2D_OK;
 }
 
-// Physical w and psi of an FP64 handle's state on its collocation grid (into h->phys, h->phys + M*M).
-int state_to_phys(s2d_handle* h, const void* S, double* ow, double* op, bool with_psi) {
+// Physical w (and psi) of a spectral field of the handle on its collocation grid.
+template <typename T>
+int state_to_phys(s2d_handle* h, const void* S, T* ow, T* op, bool with_psi) {
+    using VT = typename Vec<T>::t;
     FieldSet fs{};
     fs.nf = with_psi ? 2 : 1;
     fs.op[0] = OP_W;
     fs.op[1] = OP_PSI;
     fs.out[0] = h->I[0];
     fs.out[1] = h->I[1];
-    C_CUDA(Kern<double>::yinv(h->d, S, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    C_CUDA(Kern<T>::yinv(h->d, S, h->rk2, fs, h->tw, h->stream, h->L_yinv));
     const Launch& L = h->L_xrow;
-    k_xinv_phys2<<<(h->d.M + L.G - 1) / L.G, L.threads, L.smem, h->stream>>>(
-        h->d, (const double2*)h->I[0], with_psi ? (const double2*)h->I[1] : nullptr, (const double2*)h->tw, L.G, ow,
+    k_xinv_phys2<T><<<(h->d.M + L.G - 1) / L.G, L.threads, L.smem, h->stream>>>(
+        h->d, (const VT*)h->I[0], with_psi ? (const VT*)h->I[1] : nullptr, (const VT*)h->tw, L.G, ow,
         with_psi ? op : nullptr);
     C_CUDA(cudaGetLastError());
     return S2D_OK;
 }
 
 int ensure_les_buffers(s2d_handle* h) {
-    if (h->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "closure LES handles must be FP64");
     static bool attr[64] = {false};
     if (h->device >= 0 && h->device < 64 && !attr[h->device]) {
-        C_CUDA(cudaFuncSetAttribute(k_xinv_phys2, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
+        C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
+        C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
         attr[h->device] = true;
     }
     const size_t cs = (size_t)h->d.KX * h->d.ldS * sizeof(double2);
     if (!h->pi) C_CUDA(cudaMalloc(&h->pi, cs));
     if (!h->Sdw) C_CUDA(cudaMalloc(&h->Sdw, cs));
     if (!h->phys) C_CUDA(cudaMalloc(&h->phys, 3 * (size_t)h->d.M * h->d.M * sizeof(double)));
+    return S2D_OK;
+}
+
+// -Pi^ of the LES state into les->src: physical (w, psi), per-state rms,
+// network, rescale, forward transform with truncation.
+template <typename T>
+int closure_term(s2d_handle* les) {
+    s2d_cnn* c = les->cnn;
+    const long HW = (long)les->d.M * les->d.M;
+    T* pw = (T*)les->phys;
+    T* pp = pw + HW;
+    T* ppi = pw + 2 * HW;
+    int r = state_to_phys<T>(les, les->S0, pw, pp, true);
+    if (r != S2D_OK) return r;
+    C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
+    k_sumsq<T><<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
+    k_pack_les<T><<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, HW, (float)(1.0 / c->scale[0]),
+                                                             (float)(1.0 / c->scale[1]), c->sumsq, c->X0);
+    C_CUDA(cudaGetLastError());
+    // the network runs on the LES stream: borrow it for the forward pass
+    cudaStream_t saved = c->stream;
+    c->stream = les->stream;
+    r = forward(c, 1);
+    c->stream = saved;
+    if (r != S2D_OK) return r;
+    k_scale_out<T><<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], c->sumsq, ppi);
+    C_CUDA(cudaGetLastError());
+    C_CUDA(Kern<T>::xfwd_phys(les->d, ppi, les->I[2], les->tw, les->stream, les->L_xrow));
+    C_CUDA(Kern<T>::yfwd_store(les->d, les->I[2], les->src, les->tw, les->stream, les->L_ystore));
     return S2D_OK;
 }
 
@@ -928,13 +967,17 @@ S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_
 
 S2D_API int s2d_filter_state(s2d_handle* dns, s2d_handle* les) {
     if (!dns || !les) return cerr(S2D_ERR_INVALID, "null handle");
-    if (dns->prec != S2D_FP64 || les->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "filtering needs FP64 handles");
+    if (dns->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "filtering needs an FP64 DNS handle");
     if (les->d.K > dns->d.K) return cerr(S2D_ERR_INVALID, "the LES grid must be coarser than the DNS grid");
     C_CUDA(cudaSetDevice(dns->device));
     C_CUDA(cudaStreamSynchronize(les->stream));
     const int total = les->d.KX * les->d.KY;
-    k_filter_gather<<<nblocks(total, 256), 256, 0, dns->stream>>>(dns->d, les->d, (const double2*)dns->S0, nullptr,
-                                                                   0.0, (double2*)les->S0, nullptr);
+    if (les->prec == S2D_FP64)
+        k_filter_gather<double2><<<nblocks(total, 256), 256, 0, dns->stream>>>(
+            dns->d, les->d, (const double2*)dns->S0, nullptr, 0.0, (double2*)les->S0, nullptr);
+    else
+        k_filter_gather<float2><<<nblocks(total, 256), 256, 0, dns->stream>>>(
+            dns->d, les->d, (const double2*)dns->S0, nullptr, 0.0, (float2*)les->S0, nullptr);
     C_CUDA(cudaGetLastError());
     C_CUDA(cudaStreamSynchronize(dns->stream));
     return S2D_OK;
@@ -965,7 +1008,7 @@ S2D_API int s2d_subgrid_flux(s2d_handle* dns, s2d_handle* les, double* pi_host) 
     }
     C_CUDA(cudaStreamSynchronize(les->stream));
     const int total = les->d.KX * les->d.KY;
-    k_filter_gather<<<nblocks(total, 256), 256, 0, dns->stream>>>(dns->d, les->d, (const double2*)dns->S0,
+    k_filter_gather<double2><<<nblocks(total, 256), 256, 0, dns->stream>>>(dns->d, les->d, (const double2*)dns->S0,
                                                                    (const double2*)dns->Sdw, dns->ph.nu,
                                                                    (double2*)les->S0, (double2*)les->pi);
     C_CUDA(cudaGetLastError());
@@ -1008,16 +1051,17 @@ S2D_API int s2d_cnn_dataset_add(s2d_cnn* c, s2d_handle* les) {
     if (c->data_n >= c->data_cap) return cerr(S2D_ERR_INVALID, "dataset full");
     C_CUDA(cudaSetDevice(c->device));
     const long HW = (long)les->d.M * les->d.M;
-    double* pw = les->phys;
-    double* pp = les->phys + HW;
-    double* ppi = les->phys + 2 * HW;
-    int r = state_to_phys(les, les->S0, pw, pp, true);
-    if (r == S2D_OK) r = state_to_phys(les, les->pi, ppi, nullptr, false);
+    if (les->prec != S2D_FP64) return cerr(S2D_ERR_UNSUPPORTED, "training data needs an FP64 LES handle");
+    double* pw = (double*)les->phys;
+    double* pp = pw + HW;
+    double* ppi = pw + 2 * HW;
+    int r = state_to_phys<double>(les, les->S0, pw, pp, true);
+    if (r == S2D_OK) r = state_to_phys<double>(les, les->pi, ppi, (double*)nullptr, false);
     if (r != S2D_OK) return r;
     k_to_sample<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, ppi, HW, c->data + (size_t)c->data_n * HW * 3);
     C_CUDA(cudaGetLastError());
     C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
-    k_sumsq<<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
+    k_sumsq<double><<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
     k_store_rms<<<1, 1, 0, les->stream>>>(c->sumsq, HW, c->amp + c->data_n);
     C_CUDA(cudaGetLastError());
     C_CUDA(cudaStreamSynchronize(les->stream));
@@ -1032,7 +1076,7 @@ S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
     if (c) {
         int r = ensure_les_buffers(les);
         if (r != S2D_OK) return r;
-        if (!les->src) C_CUDA(cudaMalloc(&les->src, (size_t)les->d.KX * les->d.ldS * sizeof(double2)));
+        if (!les->src) C_CUDA(cudaMalloc(&les->src, (size_t)les->d.KX * les->d.ldS * les->vsz));
     } else if (les->src) {
         C_CUDA(cudaStreamSynchronize(les->stream));
         cudaFree(les->src);
@@ -1044,30 +1088,8 @@ S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
 
 S2D_API int s2d_les_closure_term(s2d_handle* les) {
     if (!les || !les->cnn || !les->src) return cerr(S2D_ERR_INVALID, "no closure set");
-    s2d_cnn* c = les->cnn;
     C_CUDA(cudaSetDevice(les->device));
-    const long HW = (long)les->d.M * les->d.M;
-    double* pw = les->phys;
-    double* pp = les->phys + HW;
-    double* ppi = les->phys + 2 * HW;
-    int r = state_to_phys(les, les->S0, pw, pp, true);
-    if (r != S2D_OK) return r;
-    C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
-    k_sumsq<<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
-    k_pack_les<<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, HW, (float)(1.0 / c->scale[0]),
-                                                          (float)(1.0 / c->scale[1]), c->sumsq, c->X0);
-    C_CUDA(cudaGetLastError());
-    // the network runs on the LES stream: borrow it for the forward pass
-    cudaStream_t saved = c->stream;
-    c->stream = les->stream;
-    r = forward(c, 1);
-    c->stream = saved;
-    if (r != S2D_OK) return r;
-    k_scale_out<<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], c->sumsq, ppi);
-    C_CUDA(cudaGetLastError());
-    C_CUDA(Kern<double>::xfwd_phys(les->d, ppi, les->I[2], les->tw, les->stream, les->L_xrow));
-    C_CUDA(Kern<double>::yfwd_store(les->d, les->I[2], les->src, les->tw, les->stream, les->L_ystore));
-    return S2D_OK;
+    return les->prec == S2D_FP64 ? closure_term<double>(les) : closure_term<float>(les);
 }
 
 S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {

@@ -141,7 +141,7 @@ struct s2d_handle {
     void* Sdw = nullptr; // dW for compute_rhs (lazily allocated)
     void* src = nullptr; // optional additive source of dW (compact layout), e.g. a closure term
     void* pi = nullptr;  // subgrid flux of the filtered DNS (compact layout, LES handles)
-    double* phys = nullptr;        // 3 physical fields on the collocation grid (closure)
+    void* phys = nullptr;          // 3 physical fields on the collocation grid (closure), 8 B/element
     struct s2d_cnn* cnn = nullptr; // closure network used by s2d_les_integrate_steps
     void* Ibase = nullptr;
     void* I[3] = {nullptr, nullptr, nullptr};

@@ -115,13 +115,15 @@ def test_training_reduces_loss(S):
         assert l1 < 0.7 * l0
 
 
-def test_les_with_closure_runs_and_changes_the_solution(S):
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_les_with_closure_runs_and_changes_the_solution(S, precision):
     with S.ClosureNet(24, max_batch=8, seed=2) as net:
         dt = _dataset(S, net, nsnap=16)
         net.set_scales(net.dataset_stats())
         for e in range(5):
             net.train_epoch(0, 16, 8, 1e-3, seed=e)
-        with S.Spectral2D(16, nu=2e-3) as a, S.Spectral2D(16, nu=2e-3) as b:
+        with S.Spectral2D(16, nu=2e-3, precision=precision) as a, \
+                S.Spectral2D(16, nu=2e-3, precision=precision) as b:
             w0 = O.random_state(O.get_grid_size(16, 16), 4, decay=0.2)
             a.set_state(w0)
             b.set_state(w0)
@@ -134,5 +136,5 @@ def test_les_with_closure_runs_and_changes_the_solution(S):
             S.les_set_closure(a, None)
     assert np.all(np.isfinite(wa))
     d = O.rel_l2(wa, wb)
-    print(f"closure changes the 20-step LES state by rel-L2 {d:.2e}")
+    print(f"{precision}: closure changes the 20-step LES state by rel-L2 {d:.2e}")
     assert 1e-8 < d < 0.5
