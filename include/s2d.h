@@ -181,6 +181,11 @@ S2D_API int s2d_turbulent_ic_host(int32_t nx, uint64_t seed, int32_t spectrum,
  * (src/TimeIntegration.F90:213-215).  Synchronises. */
 S2D_API int s2d_cfl_dt(s2d_handle* h, double cfl, double* dt);
 
+/* x and y vorticity-gradient skewness of Analysis (src/Analysis.F90:135-225):
+ * -2 <a b^2> / (sqrt(<a^2>) <b^2>) with (a, b) = (du/dx, dw/dx) and
+ * (dv/dy, dw/dy) on the collocation grid.  Either output may be NULL. */
+S2D_API int s2d_skewness(s2d_handle* h, double* xskew, double* yskew);
+
 /* S2D_ERR_NONFINITE if a NaN/Inf was written to the state since the last
  * call (flag raised on the device by the stage update); clears the flag. */
 S2D_API int s2d_check_finite(s2d_handle* h);
@@ -206,6 +211,20 @@ S2D_API int s2d_host_free(void* ptr);
 /* Measured FP64 throughput of this GPU (a register-resident FMA loop),
  * in TFLOP/s (2 flops per FMA). */
 S2D_API int s2d_probe_fp64_peak(int32_t device, double* tflops);
+
+/* ---- checkpoints and restart files -------------------------------------- *
+ * Checkpoint: the spectral state and run parameters; reading it back resumes
+ * the run bit for bit (the reference writes restarts but cannot read them,
+ * src/IO.F90:98-143).
+ * Restart: the physical fields Omega, Psi, u, v on the collocation grid with
+ * nx, ny, nadv, time, nu (the content of src/IO.F90:306-424) as
+ * <root>_<num:08d>.bin (64-byte header, four little-endian float64 arrays,
+ * x fastest) plus an XDMF sidecar <root>_<num:08d>.xmf.  s2d_read_restart
+ * reloads Omega through the forward transform. */
+S2D_API int s2d_checkpoint_write(s2d_handle* h, const char* path, int64_t nadv, double time);
+S2D_API int s2d_checkpoint_read(s2d_handle* h, const char* path, int64_t* nadv, double* time);
+S2D_API int s2d_write_restart(s2d_handle* h, const char* root, int32_t num, int64_t nadv, double time);
+S2D_API int s2d_read_restart(s2d_handle* h, const char* path, int64_t* nadv, double* time);
 
 /* ---- ensembles of independent runs (no reference counterpart) ----------- *
  * A batch advances nruns independent simulations of uneven sizes (nx a power

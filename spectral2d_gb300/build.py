@@ -20,9 +20,10 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libspectral2d_gb300.so")
+DRIVER = os.path.join(PKG, "spectral2d_run")
 
 SOURCES = ["s2d_kernels.cu", "s2d_capi.cu", "s2d_ic.cpp", "s2d_noalloc.cu", "s2d_batch.cu",
-           "s2d_closure.cu"]
+           "s2d_closure.cu", "s2d_io.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"),
@@ -68,6 +69,12 @@ def build(verbose: bool = False, ptxas_info: bool = False) -> str:
     tmp = LIB + ".tmp"
     _run([nvcc, *ARCH, "-shared", "-o", tmp, *[o for _, o in jobs]], verbose)
     os.replace(tmp, LIB)
+    # the main program (src/Spectral2D.F90) linked against the library
+    tmp = DRIVER + ".tmp"
+    _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+          os.path.join(CSRC, "s2d_driver.cpp"), "-o", tmp, "-L", PKG, "-lspectral2d_gb300",
+          "-Wl,-rpath,$ORIGIN"], verbose)
+    os.replace(tmp, DRIVER)
     return LIB
 
 

@@ -675,6 +675,59 @@ S2D_API int s2d_cfl_dt(s2d_handle* h, double cfl, double* dt) {
     return S2D_OK;
 }
 
+S2D_API int s2d_skewness(s2d_handle* h, double* xskew, double* yskew) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    S2D_CUDA(cudaSetDevice(h->device));
+    const Dims& d = h->d;
+    std::vector<double> rows(3 * (size_t)d.M);
+    double sk[2];
+    double* dev = nullptr;
+    S2D_CUDA(cudaMalloc(&dev, rows.size() * sizeof(double)));
+    // x: a = du/dx = i kx u, b = dw/dx (src/Analysis.F90:142-179);
+    // y: a = dv/dy = i ky v, b = dw/dy (src/Analysis.F90:188-225)
+    const int ops[2][2] = {{OP_UX, OP_WX}, {OP_VY, OP_WY}};
+    int r = S2D_OK;
+    for (int pass = 0; pass < 2 && r == S2D_OK; ++pass) {
+        FieldSet fs{};
+        fs.nf = 2;
+        fs.op[0] = ops[pass][0];
+        fs.op[1] = ops[pass][1];
+        fs.out[0] = h->I[0];
+        fs.out[1] = h->I[1];
+        cudaError_t e;
+        if (h->prec == S2D_FP64) {
+            e = Kern<double>::yinv(d, h->S0, h->rk2, fs, h->tw, h->stream, h->L_yinv);
+            if (e == cudaSuccess) e = Kern<double>::xinv_moments(d, h->I[0], h->I[1], h->tw, dev, h->stream, h->L_xrow);
+        } else {
+            e = Kern<float>::yinv(d, h->S0, h->rk2, fs, h->tw, h->stream, h->L_yinv);
+            if (e == cudaSuccess) e = Kern<float>::xinv_moments(d, h->I[0], h->I[1], h->tw, dev, h->stream, h->L_xrow);
+        }
+        if (e == cudaSuccess) e = cudaMemcpyAsync(rows.data(), dev, rows.size() * sizeof(double),
+                                                  cudaMemcpyDeviceToHost, h->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) {
+            r = fail(S2D_ERR_CUDA, "skewness: %s", cudaGetErrorString(e));
+            break;
+        }
+        double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        for (int y = 0; y < d.M; ++y) {
+            s1 += rows[3 * y];
+            s2 += rows[3 * y + 1];
+            s3 += rows[3 * y + 2];
+        }
+        const double fact = (double)d.M * (double)d.M;
+        s1 /= fact;
+        s2 /= fact;
+        s3 /= fact;
+        sk[pass] = -2.0 * s1 / (std::sqrt(s2) * s3);
+    }
+    cudaFree(dev);
+    if (r != S2D_OK) return r;
+    if (xskew) *xskew = sk[0];
+    if (yskew) *yskew = sk[1];
+    return S2D_OK;
+}
+
 S2D_API int s2d_check_finite(s2d_handle* h) {
     if (!h) return fail(S2D_ERR_INVALID, "null handle");
     S2D_CUDA(cudaSetDevice(h->device));

@@ -694,7 +694,31 @@ int closure_term(s2d_handle* les) {
     return S2D_OK;
 }
 
+template <typename T>
+int physical_pair_t(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB) {
+    using VT = typename Vec<T>::t;
+    int r = ensure_les_buffers(h);
+    if (r != S2D_OK) return r;
+    FieldSet fs{};
+    fs.nf = outB ? 2 : 1;
+    fs.op[0] = opA;
+    fs.op[1] = opB;
+    fs.out[0] = h->I[0];
+    fs.out[1] = h->I[1];
+    C_CUDA(Kern<T>::yinv(h->d, S, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    const Launch& L = h->L_xrow;
+    k_xinv_phys2<T><<<(h->d.M + L.G - 1) / L.G, L.threads, L.smem, h->stream>>>(
+        h->d, (const VT*)h->I[0], outB ? (const VT*)h->I[1] : nullptr, (const VT*)h->tw, L.G, (T*)outA, (T*)outB);
+    C_CUDA(cudaGetLastError());
+    return S2D_OK;
+}
+
 }  // namespace
+
+int s2d::physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB) {
+    return h->prec == S2D_FP64 ? physical_pair_t<double>(h, S, opA, opB, outA, outB)
+                               : physical_pair_t<float>(h, S, opA, opB, outA, outB);
+}
 
 extern "C" {
 

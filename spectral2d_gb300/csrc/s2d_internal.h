@@ -111,6 +111,8 @@ struct Kern {
                               cudaStream_t st);
     static cudaError_t xinv_cfl(const Dims& d, const void* Iu, const void* Iv, const void* tw,
                                 unsigned long long* maxbits, cudaStream_t st, const Launch& L);
+    static cudaError_t xinv_moments(const Dims& d, const void* Ia, const void* Ib, const void* tw,
+                                    double* out, cudaStream_t st, const Launch& L);
     static cudaError_t fill_tg(const Dims& d, const double* sx, const double* sy, void* phys,
                                cudaStream_t st);
     static cudaError_t xfwd_phys(const Dims& d, const void* phys, void* Iout, const void* tw,
@@ -169,6 +171,11 @@ int create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handle** o
 
 // Shared-memory attribute setup (called once per process and device).
 cudaError_t configure_kernels(int max_smem_optin);
+
+// Physical fields (operators opA, opB of the spectral field S, see FieldOp)
+// on the M x M collocation grid, row-major, in the handle's precision; outB
+// may be null.  Asynchronous on the handle's stream.
+int physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB);
 
 // Record msg as this thread's last error (s2d_last_error) and return code.
 int set_error(int code, const char* msg);

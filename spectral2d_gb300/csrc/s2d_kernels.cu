@@ -298,6 +298,53 @@ __global__ void __launch_bounds__(512) k_xinv_cfl(Dims d, const typename Vec<T>:
     }
 }
 
+// Skewness moments of two physical fields a (real part) and b (imaginary
+// part) of one inverse FFT per row: out[row] = (sum a b^2, sum a^2, sum b^2)
+// (src/Analysis.F90:157-163, :203-209), summed over rows later in order.
+template <typename T>
+__global__ void __launch_bounds__(512) k_xinv_moments(Dims d, const typename Vec<T>::t* __restrict__ Ia,
+                                                      const typename Vec<T>::t* __restrict__ Ib,
+                                                      const typename Vec<T>::t* __restrict__ tw, int G,
+                                                      double* out) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    VT* Z = bufs + (size_t)g * d.M;
+    const int yy = active ? y : 0;
+    build_pair(Z, Ia + (size_t)yy * d.ldI, Ib + (size_t)yy * d.ldI, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);
+    // one row per group; the group's threads reduce in a fixed order
+    double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (int n = lane; n < d.M; n += d.Tg) {
+        const double a = (double)Z[n].x, b = (double)Z[n].y;
+        s1 += a * b * b;
+        s2 += a * a;
+        s3 += b * b;
+    }
+    __syncthreads();
+    double* scratch = reinterpret_cast<double*>(bufs);   // reuse: 3 x blockDim doubles
+    scratch[3 * threadIdx.x] = s1;
+    scratch[3 * threadIdx.x + 1] = s2;
+    scratch[3 * threadIdx.x + 2] = s3;
+    __syncthreads();
+    if (lane == 0 && active) {
+        double t1 = 0.0, t2 = 0.0, t3 = 0.0;
+        for (int i = 0; i < d.Tg; ++i) {
+            const int k = g * d.Tg + i;
+            t1 += scratch[3 * k];
+            t2 += scratch[3 * k + 1];
+            t3 += scratch[3 * k + 2];
+        }
+        out[3 * y] = t1;
+        out[3 * y + 1] = t2;
+        out[3 * y + 2] = t3;
+    }
+}
+
 // Taylor-Green vorticity on the physical grid, 2 sin(x_i) sin(y_j) with the
 // 1-based coordinates of src/SetIC.F90:88-96 (sx, sy precomputed on the host
 // with the same FP64 sin as the reference).
@@ -492,6 +539,15 @@ cudaError_t Kern<T>::xinv_cfl(const Dims& d, const void* Iu, const void* Iv, con
 }
 
 template <typename T>
+cudaError_t Kern<T>::xinv_moments(const Dims& d, const void* Ia, const void* Ib, const void* tw, double* out,
+                                  cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    k_xinv_moments<T><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (const VT*)Ia, (const VT*)Ib,
+                                                                         (const VT*)tw, L.G, out);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t Kern<T>::fill_tg(const Dims& d, const double* sx, const double* sy, void* phys, cudaStream_t st) {
     k_fill_tg<T><<<grid_for((long)d.M * d.M, 256), 256, 0, st>>>(d, sx, sy, (T*)phys);
     return cudaGetLastError();
@@ -551,6 +607,8 @@ cudaError_t configure_kernels(int max_smem_optin) {
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
     S2D_SET(k_xinv_cfl<double>);
+    S2D_SET(k_xinv_moments<double>);
+    S2D_SET(k_xinv_moments<float>);
     S2D_SET(k_xinv_cfl<float>);
     S2D_SET(k_xfwd_phys<double>);
     S2D_SET(k_xfwd_phys<float>);

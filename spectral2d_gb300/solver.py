@@ -197,6 +197,31 @@ class Spectral2D:
         L.check(self._L.s2d_spectrum(self._h, _dptr(Ek), nb, C.byref(t), C.byref(e), C.byref(z)))
         return np.arange(nb, dtype=np.float64), Ek, t.value, e.value, z.value
 
+    def skewness(self):
+        """(xSkew, ySkew) of ``Analysis`` (src/Analysis.F90:135-225)."""
+        x, y = C.c_double(), C.c_double()
+        L.check(self._L.s2d_skewness(self._h, C.byref(x), C.byref(y)))
+        return x.value, y.value
+
+    # -- checkpoints and restart files ---------------------------------------
+    def checkpoint_write(self, path: str, nadv: int = 0, time: float = 0.0) -> None:
+        L.check(self._L.s2d_checkpoint_write(self._h, path.encode(), nadv, time))
+
+    def checkpoint_read(self, path: str):
+        n, t = C.c_int64(), C.c_double()
+        L.check(self._L.s2d_checkpoint_read(self._h, path.encode(), C.byref(n), C.byref(t)))
+        return n.value, t.value
+
+    def write_restart(self, root: str, num: int, nadv: int, time: float) -> str:
+        """Physical Omega, Psi, u, v; returns the path of the binary file."""
+        L.check(self._L.s2d_write_restart(self._h, root.encode(), num, nadv, time))
+        return f"{root}_{num:08d}.bin"
+
+    def read_restart(self, path: str):
+        n, t = C.c_int64(), C.c_double()
+        L.check(self._L.s2d_read_restart(self._h, path.encode(), C.byref(n), C.byref(t)))
+        return n.value, t.value
+
     def enstrophy(self) -> float:
         v = C.c_double()
         L.check(self._L.s2d_enstrophy(self._h, C.byref(v)))
