@@ -135,7 +135,7 @@ class Clocks:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -175,36 +175,6 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
-
-
-class Dist:
-    """Barrier and max/sum over ranks (torch.distributed, only when N > 1)."""
-
-    def __init__(self, world, local):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch
-            import torch.distributed as dist
-            torch.cuda.set_device(local)
-            dist.init_process_group("nccl")
-            self.torch, self.dist = torch, dist
-            self.dev = torch.device("cuda", local)
-
-    def barrier(self):
-        if self.world > 1:
-            self.dist.barrier()
-
-    def reduce(self, x: float, op: str) -> float:
-        if self.world == 1:
-            return x
-        t = self.torch.tensor([x], dtype=self.torch.float64, device=self.dev)
-        self.dist.all_reduce(t, op=getattr(self.dist.ReduceOp, op))
-        return float(t.item())
-
-    def close(self):
-        if self.world > 1:
-            self.dist.destroy_process_group()
 
 
 # ---------------------------------------------------------------------------
@@ -272,6 +242,29 @@ def run_ensemble(args, rank, world):
     ms = ens.time_steps(args.steps)
     ens.status()
     pts = sum(n * n for n in nxs)
+    check = None
+    if args.ens_check_steps > 0:
+        # every run advanced in both precisions from the same state; the FP64
+        # batch equals single-run FP64 bit for bit (tests/test_gpu_ensemble.py)
+        other = "fp64" if args.precision == "fp32" else "fp32"
+        ens2 = Ensemble(nxs, nus, precision=other)
+        for i, r in enumerate(ens.runs):
+            ens2.runs[i].set_state(r.get_state()[0])
+        ens2.set_dt(dts)
+        ens.integrate_steps(args.ens_check_steps)
+        ens2.integrate_steps(args.ens_check_steps)
+        ens.status()
+        ens2.status()
+        e32 = ens if args.precision == "fp32" else ens2
+        e64 = ens2 if args.precision == "fp32" else ens
+        errs = {}
+        for i, n in enumerate(nxs):
+            a, b = e32.runs[i].get_state()[0], e64.runs[i].get_state()[0]
+            errs.setdefault(n, []).append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+        check = {"steps": args.ens_check_steps,
+                 "fp32_vs_fp64_w_rel_l2": {str(n): {"max": max(v), "median": float(np.median(v))}
+                                           for n, v in errs.items()}}
+        ens2.close()
     if rank == 0:
         print(json.dumps({
             "metric": "ensemble Mpt*steps/s (96 runs: 32x128^2, 32x256^2, 32x512^2)",
@@ -282,30 +275,104 @@ def run_ensemble(args, rank, world):
             "data": "synthetic (seeded random-phase ICs)",
             "config": {"workload": "batched ensemble, one persistent launch per RK3 stage",
                        "tile_threads": threads, "ctas_per_sm": cps},
-            "gpu_launches": 3 * args.steps}), flush=True)
+            "gpu_launches": 3 * args.steps, "precision_check": check}), flush=True)
     ens.close()
     return 0
 
 
-def workload_config(n):
+def run_les_batch(args, rank, world):
+    """Concurrent closure LES (not the headline line): args.les_runs runs of
+    256^2 (384^2 collocation grid), decaying turbulence with per-run seeds,
+    nu = 1e-4, CFL-0.5 dt; every step is one network forward over all runs
+    (the trained 128^2 closure's weights when packaged, else a seeded random
+    network) plus the batched transforms and three persistent stage launches,
+    replayed from one CUDA graph.  Both precisions are timed; the FP32 runs'
+    energy spectra are compared with the FP64 runs' after the same steps."""
+    import os
+    import numpy as np
+    from spectral2d_gb300 import ClosureNet, Ensemble, closure
+    nr, n, nu = args.les_runs, 256, 1e-4
+    grid = 3 * n // 2
+    net = ClosureNet(grid, max_batch=nr, seed=0)
+    wpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "spectral2d_gb300", "data",
+                         "closure_les128.npz")
+    if os.path.exists(wpath):
+        closure.load_weights(net, wpath)
+        weights = "trained 128^2 closure (spectral2d_gb300/data/closure_les128.npz)"
+    else:
+        net.set_scales([1.0, 1.0, 1.0])
+        weights = "seeded random network"
+    ens = {p: Ensemble([n] * nr, [nu] * nr, precision=p) for p in ("fp64", "fp32")}
+    dts = []
+    for i in range(nr):
+        r64 = ens["fp64"].runs[i]
+        r64.set_turbulent_velocity(seed=1000 * rank + i, spectrum="k4gauss", k0=10.0, tke=0.5)
+        dts.append(r64.compute_time_step(CFL))
+        ens["fp32"].runs[i].set_state(r64.get_state()[0])
+    res = {}
+    for p, e in ens.items():
+        e.set_dt(dts)
+        e.set_closure(net)
+        e.integrate_steps(args.warmup)
+        e.synchronize()
+        ms = e.time_steps(args.steps)
+        e.status()
+        res[p] = ms / args.steps
+    # the network's buffers are shared: the two batches ran one after the other
+    errs = []
+    for i in range(nr):
+        _, e64, _, _, _ = ens["fp64"].runs[i].compute_spectrum()
+        _, e32, _, _, _ = ens["fp32"].runs[i].compute_spectrum()
+        kk = slice(1, 41)
+        errs.append(float(np.max(np.abs(e32[kk] - e64[kk]) / e64[kk])))
+    p = args.precision
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"closure-LES run-steps/s ({nr} concurrent 256^2 runs)",
+            "value": nr / (res[p] * 1e-3), "unit": "run-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[p],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if p == "fp64" else "f32",
+            "data": "synthetic (seeded random-phase ICs)",
+            "config": {"workload": "batched closure LES, one network forward + three persistent stage "
+                                   "launches per step in one CUDA graph",
+                       "runs": nr, "n": n, "nu": nu, "cfl": CFL, "network": weights},
+            "ms_per_step_fp64": res["fp64"], "ms_per_step_fp32": res["fp32"],
+            "mpt_steps_per_s": nr * n * n / (res[p] * 1e-3) / 1e6,
+            "fp32_vs_fp64_Ek_max_rel_err_k_le_40": {"max_over_runs": max(errs),
+                                                    "mean_over_runs": float(np.mean(errs)),
+                                                    "after_steps": args.warmup + args.steps}}),
+              flush=True)
+    for e in ens.values():
+        e.set_closure(None)
+        e.close()
+    net.close()
+    return 0
+
+
+def workload_config(n, precision="fp64"):
+    w = 16 if precision == "fp64" else 8
+    ws = 2 * (n // 2 + 1) * (3 * n // 2) * w / 1e9   # the two half-spectral intermediates
     return {"workload": f"decaying 2-D turbulence DNS, N={n} (padded {3 * n // 2}^2, 3/2 rule), "
-                        f"FP64, nu={NU}, dt=CFL {CFL}, TVD-RK3",
+                        f"{precision.upper()}, nu={NU}, dt=CFL {CFL}, TVD-RK3",
             "n": n, "padded": 3 * n // 2, "nu": NU, "cfl": CFL, "seed": SEED,
             "ic": "E(k)~k^4 exp(-2(k/10)^2), TKE 0.5",
-            "l2": "no flush: per-step working set ~0.3 GB > 126 MB L2",
+            "l2": f"no flush: each stage streams {ws:.2f} GB of intermediates (> 126 MB L2)",
             "parallelism": "replicas (one independent run per GPU)"}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=150)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--form", default="basdevant", choices=["basdevant", "conservative"])
-    ap.add_argument("--workload", default="dns", choices=["dns", "ensemble"])
+    ap.add_argument("--workload", default="dns", choices=["dns", "ensemble", "les-batch"])
+    ap.add_argument("--les-runs", type=int, default=256)
+    ap.add_argument("--ens-check-steps", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
@@ -317,6 +384,8 @@ def main():
         return run_reference(args, rank, world)
     if args.workload == "ensemble":
         return run_ensemble(args, rank, world)
+    if args.workload == "les-batch":
+        return run_les_batch(args, rank, world)
 
     # CPU baseline first (no GPU context yet in this process)
     cpu = None
@@ -329,7 +398,8 @@ def main():
     import numpy as np
     from spectral2d_gb300 import Spectral2D, probe_fp64_peak
 
-    D = Dist(world, local)
+    from spectral2d_gb300.replicas import ReplicaGroup
+    D = ReplicaGroup()
     n = args.n
     s = Spectral2D(n, nu=NU, precision=args.precision, device=local, nonlinear_form=args.form)
     s.set_turbulent_velocity(seed=SEED + rank, spectrum="k4gauss", k0=10.0, tke=0.5)
@@ -399,17 +469,18 @@ def main():
             "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if args.precision == "fp64" else "f32",
             "data": "synthetic (seeded random-phase IC)",
-            "config": workload_config(n),
+            "config": workload_config(n, args.precision),
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
                          "unit": "GB/s", "frac": achieved / hbm,
                          "peak_source": f"{hbm_src} HBM copy bandwidth",
                          "traffic": traffic,
                          "algorithmic_bytes_per_launch": bm["per_kernel"][dom],
                          "launch_ms": avg[dom],
-                         "fp64_alu": {"achieved_tflops": alu, "peak_tflops": fp64,
-                                      "frac": (alu / fp64) if fp64 else None,
-                                      "peak_source": "measured FP64 FMA loop on this GPU",
-                                      "flops_per_launch": fm[dom]},
+                         "fp64_alu": ({"achieved_tflops": alu, "peak_tflops": fp64,
+                                       "frac": (alu / fp64) if fp64 else None,
+                                       "peak_source": "measured FP64 FMA loop on this GPU",
+                                       "flops_per_launch": fm[dom]}
+                                      if args.precision == "fp64" else None),
                          "step_hbm_frac": bm["step"] / (ms_per_step * 1e-3) / 1e9 / hbm,
                          "step_hbm_frac_reference_form_bytes": bm["step_reference_form"] / (ms_per_step * 1e-3) / 1e9 / hbm,
                          "nonlinear_form": args.form,

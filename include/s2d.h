@@ -260,7 +260,8 @@ S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm,
  * Pi^ = T[N_dns(w)] - N_les(T w) (N = F[u . grad w]), and a 6-layer circular
  * 3x3 CNN (2 -> 32 x 5 -> 1 channels, GELU, BF16 activations and weights,
  * FP32 accumulation, Adam) that predicts Pi from the filtered (w, psi) on the
- * LES collocation grid.  Closure handles must be FP64. */
+ * LES collocation grid.  Handles that make training data (DNS and LES) must
+ * be FP64; an LES advanced with a closure may be FP64 or FP32. */
 typedef struct s2d_cnn s2d_cnn;
 /* grid = LES collocation grid (3*nx_les/2); max_batch = largest batch */
 S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32_t device, s2d_cnn** out);
@@ -300,6 +301,12 @@ S2D_API int s2d_les_closure_term(s2d_handle* les);
 /* n steps; with a closure attached, -Pi^ of the state at the start of each
  * step is added to dW in its three RK3 stages */
 S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt);
+/* attach (c != NULL) or detach one closure network for every run of a batch:
+ * all runs on the network's grid, at most its max_batch runs.  Each batch
+ * step then starts with the closure terms of all runs -- one network forward
+ * over the whole batch, the transforms batched over runs -- before the three
+ * persistent stage launches, all in the step's CUDA graph. */
+S2D_API int s2d_batch_set_closure(s2d_batch* b, s2d_cnn* c);
 
 /* ---- allocation-free right-hand side ----------------------------------- *
  * No counterpart in the reference.  For callers that must not allocate

@@ -44,6 +44,7 @@ struct RunDev {
     typename Vec<T>::t* S1;
     typename Vec<T>::t* I0;
     typename Vec<T>::t* I1;
+    const typename Vec<T>::t* src;   // closure term added to dW, or null
     const double* rk2;
     const typename Vec<T>::t* tw;
     double dt;
@@ -113,7 +114,7 @@ __global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict
                 const T scale = (T)(0.5 / ((double)R.d.M * (double)R.d.M));
                 xpass_bas_body<T>(R.d, R.I0, R.I1, R.tw, R.G12, scale, blk, bufs);
             } else {
-                bad |= yfwd_body<T>(R.d, R.I0, R.I1, R.S0, R.S1, nullptr, nullptr, stage, R.dt, R.ph, R.tw, R.G3,
+                bad |= yfwd_body<T>(R.d, R.I0, R.I1, R.S0, R.S1, nullptr, R.src, stage, R.dt, R.ph, R.tw, R.G3,
                                     blk, bufs);
             }
         }
@@ -165,6 +166,8 @@ struct s2d_batch {
     int max_smem = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
+    s2d_cnn* cnn = nullptr;   // closure network of every run (LES batches)
+    void* cl_tab = nullptr;   // its device table (closure_table)
 };
 
 namespace {
@@ -185,6 +188,8 @@ cudaError_t launch_stage(s2d_batch* b, int stage) {
 }
 
 cudaError_t launch_step(s2d_batch* b) {
+    if (b->cnn && closure_terms(b->cnn, b->runs.data(), b->n, b->cl_tab, b->stream) != S2D_OK)
+        return cudaErrorUnknown;
     for (int s = 1; s <= 3; ++s) {
         cudaError_t e = b->prec == S2D_FP64 ? launch_stage<double>(b, s) : launch_stage<float>(b, s);
         if (e != cudaSuccess) return e;
@@ -216,6 +221,7 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
         R.S1 = (VT*)h->S1;
         R.I0 = (VT*)h->I[0];
         R.I1 = (VT*)h->I[1];
+        R.src = b->cnn ? (const VT*)h->src : nullptr;
         R.rk2 = h->rk2;
         R.tw = (const VT*)h->tw;
         R.dt = b->dt[i];
@@ -355,7 +361,7 @@ S2D_API void s2d_batch_destroy(s2d_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graph(b);
     for (auto* h : b->runs) s2d_destroy(h);
-    void* ptrs[] = {b->d_runs, b->d_tasks, b->d_ctrl, b->d_done, b->d_flags};
+    void* ptrs[] = {b->d_runs, b->d_tasks, b->d_ctrl, b->d_done, b->d_flags, b->cl_tab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -381,6 +387,31 @@ S2D_API int s2d_batch_set_dt(s2d_batch* b, const double* dt) {
     }
     B_CUDA(cudaSetDevice(b->device));
     return upload_dt(b);
+}
+
+S2D_API int s2d_batch_set_closure(s2d_batch* b, s2d_cnn* c) {
+    if (!b) return berr(S2D_ERR_INVALID, "null batch");
+    B_CUDA(cudaSetDevice(b->device));
+    B_CUDA(cudaStreamSynchronize(b->stream));
+    if (c) {
+        if (b->n > cnn_max_batch(c)) return berr(S2D_ERR_INVALID, "more runs than the network's batch capacity");
+        for (auto* h : b->runs)
+            if (h->d.K != b->runs[0]->d.K || h->d.M != cnn_grid(c))
+                return berr(S2D_ERR_INVALID, "closure batches need every run on the network's grid");
+        for (auto* h : b->runs) {
+            const int r = ensure_closure_buffers(h);
+            if (r != S2D_OK) return r;
+        }
+        if (!b->cl_tab) {
+            const int r = closure_table(b->runs.data(), b->n, &b->cl_tab);
+            if (r != S2D_OK) return r;
+        }
+    } else if (b->cl_tab) {
+        cudaFree(b->cl_tab);
+        b->cl_tab = nullptr;
+    }
+    b->cnn = c;
+    return configure_any(b, b->threads, b->ctas_per_sm);
 }
 
 S2D_API int s2d_batch_integrate_steps(s2d_batch* b, int32_t n) {

@@ -493,7 +493,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
     void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->tw,  h->ref_stage,
-                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys};
+                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);

@@ -394,26 +394,158 @@ __global__ void k_to_sample(const double* __restrict__ w, const double* __restri
     }
 }
 
-// Network input of one LES state: channels (w / (a s0), psi / (a s1)) with
-// a = sqrt(*sumsq / HW), the state's rms vorticity.
+// ---- closure terms of n LES runs of one grid (blockIdx.y = run) ----------
+// Per-run pointers; the same layout for both precisions.
 template <typename T>
-__global__ void k_pack_les(const T* __restrict__ w, const T* __restrict__ p, long HW, float r0, float r1,
-                           const double* __restrict__ sumsq, __nv_bfloat16* x) {
-    const double ia = 1.0 / sqrt(*sumsq / (double)HW);
+struct LesRun {
+    const typename Vec<T>::t* S0;
+    typename Vec<T>::t* I0;
+    typename Vec<T>::t* I1;
+    typename Vec<T>::t* I2;
+    T* pw;          // physical w on the M x M collocation grid
+    T* pp;          // physical psi
+    typename Vec<T>::t* src;   // -Pi^ (compact layout)
+    double* part;   // sums of w^2 per row tile of k_cl_xinv
+};
+
+// sum of the nparts partial sums, in order (one thread): w^2 summed over the grid
+__device__ __forceinline__ double ordered_sum(const double* __restrict__ part, int nparts) {
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += __ldcg(&part[i]);
+    return s;
+}
+
+// K1 of (w, psi): inverse y-pass of every run's state.
+template <typename T>
+__global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __restrict__ runs,
+                                                  const double* __restrict__ rk2,
+                                                  const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const LesRun<T>& R = runs[blockIdx.y];
+    FieldSet fs{};
+    fs.nf = 2;
+    fs.op[0] = OP_W;
+    fs.op[1] = OP_PSI;
+    fs.out[0] = R.I0;
+    fs.out[1] = R.I1;
+    yinv_body<T>(d, R.S0, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
+}
+
+// Physical rows of w and psi (one inverse FFT of W + i PSI per row) and the
+// tile's sum of w^2 (fixed order: per thread, then warps in order).
+template <typename T>
+__global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
+                                                  const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const LesRun<T>& R = runs[blockIdx.y];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    const int yy = active ? y : 0;
+    VT* Z = bufs + (size_t)g * d.M;
+    build_pair(Z, R.I0 + (size_t)yy * d.ldI, R.I1 + (size_t)yy * d.ldI, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);
+    double s = 0.0;
+    if (active)
+        for (int n = lane; n < d.M; n += d.Tg) {
+            const VT z = Z[n];
+            R.pw[(size_t)y * d.M + n] = z.x;
+            R.pp[(size_t)y * d.M + n] = z.y;
+            s += (double)z.x * (double)z.x;
+        }
+    // tree over the CTA in the (now free) FFT buffers: G*M*16 B >= 8 B per thread
+    double* red = reinterpret_cast<double*>(smem_raw);
+    __syncthreads();
+    red[threadIdx.x] = s;
+    __syncthreads();
+    int w = 1;
+    while (w < (int)blockDim.x) w <<= 1;
+    for (w >>= 1; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w && threadIdx.x + w < blockDim.x) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) R.part[blockIdx.x] = red[0];
+}
+
+// Network input of every run: (w / (a s0), psi / (a s1)), a = rms w of the run.
+template <typename T>
+__global__ void k_cl_pack(const LesRun<T>* __restrict__ runs, int nparts, long HW, float r0, float r1,
+                          __nv_bfloat16* x) {
+    __shared__ double s_ia;
+    const LesRun<T>& R = runs[blockIdx.y];
+    if (threadIdx.x == 0) s_ia = 1.0 / sqrt(ordered_sum(R.part, nparts) / (double)HW);
+    __syncthreads();
+    const double ia = s_ia;
+    __nv_bfloat16* xb = x + (size_t)blockIdx.y * HW * 16;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
-        uint32_t* xr = reinterpret_cast<uint32_t*>(x + i * 16);
-        xr[0] = pack_bf16((float)((double)w[i] * r0 * ia), (float)((double)p[i] * r1 * ia));
+        uint32_t* xr = reinterpret_cast<uint32_t*>(xb + i * 16);
+        xr[0] = pack_bf16((float)((double)R.pw[i] * r0 * ia), (float)((double)R.pp[i] * r1 * ia));
         for (int c = 1; c < 8; ++c) xr[c] = 0u;
     }
 }
 
-// phys = scale * a^2 * y (network output) as FP64, a^2 = *sumsq / HW.
+// Network output -> -Pi on the grid (scale a^2 y, scale = -s2), forward x-FFT
+// of row pairs into the half-spectral rows I2.
 template <typename T>
-__global__ void k_scale_out(const float* __restrict__ y, long n, double scale, const double* __restrict__ sumsq,
-                            T* phys) {
-    const double s = scale * (*sumsq / (double)n);
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-        phys[i] = (T)(s * (double)y[i]);
+__global__ void __launch_bounds__(512) k_cl_xfwd(Dims d, const LesRun<T>* __restrict__ runs, int nparts,
+                                                  const float* __restrict__ Y, double scale,
+                                                  const typename Vec<T>::t* __restrict__ tw, int G, T xscale) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double s_s;
+    const LesRun<T>& R = runs[blockIdx.y];
+    const long HW = (long)d.M * d.M;
+    if (threadIdx.x == 0) s_s = scale * (ordered_sum(R.part, nparts) / (double)HW);
+    __syncthreads();
+    const double s = s_s;
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int p = blockIdx.x * G + g;
+    const bool active = p < d.M / 2;
+    const int y1 = active ? 2 * p : 0;
+    VT* Z = bufs + (size_t)g * d.M;
+    const float* r1 = Y + (size_t)blockIdx.y * HW + (size_t)y1 * d.M;
+    const float* r2 = r1 + d.M;
+    for (int n = lane; n < d.M; n += d.Tg)
+        Z[n] = active ? mk<VT>((T)(s * (double)r1[n]), (T)(s * (double)r2[n])) : mk<VT>((T)0, (T)0);
+    fft_run<false>(Z, d, lane, tw);
+    extract_pair(Z, R.I2 + (size_t)y1 * d.ldI, R.I2 + (size_t)(y1 + 1) * d.ldI, d, lane, active, xscale);
+}
+
+// Forward y-FFT of the columns of I2 with Truncate into src.
+template <typename T>
+__global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __restrict__ runs,
+                                                    const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const LesRun<T>& R = runs[blockIdx.y];
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int kx0 = blockIdx.x * G;
+    const int gtot = min(G, d.KX - kx0);
+    for (int idx = threadIdx.x; idx < G * d.M; idx += blockDim.x) {
+        const int gg = idx % G;
+        const int y = idx / G;
+        bufs[(size_t)gg * d.M + y] = gg < gtot ? __ldcg(&R.I2[(size_t)y * d.ldI + kx0 + gg]) : mk<VT>((T)0, (T)0);
+    }
+    fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = idx / d.KY;
+        const int jc = idx - gg * d.KY;
+        const int kx = kx0 + gg;
+        const int ky = ky_of_jc(d, jc);
+        const int n = jc <= d.K ? jc : ky + d.M;
+        VT v = bufs[(size_t)gg * d.M + n];
+        if (kx * kx + ky * ky > d.K * d.K) v = mk<VT>((T)0, (T)0);
+        R.src[(size_t)kx * d.ldS + jc] = v;
+    }
 }
 
 // Moments of the dataset after the per-sample amplitude normalisation:
@@ -656,6 +788,12 @@ int ensure_les_buffers(s2d_handle* h) {
     if (h->device >= 0 && h->device < 64 && !attr[h->device]) {
         C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
         C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
+        const void* fns[] = {(const void*)k_cl_yinv<double>, (const void*)k_cl_yinv<float>,
+                             (const void*)k_cl_xinv<double>, (const void*)k_cl_xinv<float>,
+                             (const void*)k_cl_xfwd<double>, (const void*)k_cl_xfwd<float>,
+                             (const void*)k_cl_ystore<double>, (const void*)k_cl_ystore<float>};
+        for (const void* f : fns)
+            C_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
         attr[h->device] = true;
     }
     const size_t cs = (size_t)h->d.KX * h->d.ldS * sizeof(double2);
@@ -665,32 +803,65 @@ int ensure_les_buffers(s2d_handle* h) {
     return S2D_OK;
 }
 
-// -Pi^ of the LES state into les->src: physical (w, psi), per-state rms,
-// network, rescale, forward transform with truncation.
+// LesRun table of n runs followed by n * nparts partial sums.
+int closure_table_impl(s2d_handle* const* runs, int n, void** tab) {
+    const s2d_handle* h0 = runs[0];
+    const int nparts = (h0->d.M + h0->L_xrow.G - 1) / h0->L_xrow.G;
+    const size_t head = (size_t)n * sizeof(LesRun<double>);
+    void* t = nullptr;
+    C_CUDA(cudaMalloc(&t, head + (size_t)n * nparts * sizeof(double)));
+    std::vector<LesRun<double>> rows(n);
+    const long HW = (long)h0->d.M * h0->d.M;
+    for (int i = 0; i < n; ++i) {
+        s2d_handle* h = runs[i];
+        LesRun<double>& R = rows[i];
+        R.S0 = (const double2*)h->S0;
+        R.I0 = (double2*)h->I[0];
+        R.I1 = (double2*)h->I[1];
+        R.I2 = (double2*)h->I[2];
+        // phys holds M*M 8-byte elements per field; FP32 runs use the front half
+        R.pw = (double*)h->phys;
+        R.pp = h->prec == S2D_FP64 ? R.pw + HW : (double*)((float*)h->phys + HW);
+        R.src = (double2*)h->src;
+        R.part = (double*)((char*)t + head) + (size_t)i * nparts;
+    }
+    const cudaError_t e = cudaMemcpy(t, rows.data(), head, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(t);
+        return cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    }
+    *tab = t;
+    return S2D_OK;
+}
+
 template <typename T>
-int closure_term(s2d_handle* les) {
-    s2d_cnn* c = les->cnn;
-    const long HW = (long)les->d.M * les->d.M;
-    T* pw = (T*)les->phys;
-    T* pp = pw + HW;
-    T* ppi = pw + 2 * HW;
-    int r = state_to_phys<T>(les, les->S0, pw, pp, true);
-    if (r != S2D_OK) return r;
-    C_CUDA(cudaMemsetAsync(c->sumsq, 0, sizeof(double), les->stream));
-    k_sumsq<T><<<1, 256, 0, les->stream>>>(pw, HW, c->sumsq);   // one block: deterministic
-    k_pack_les<T><<<nblocks(HW, 256), 256, 0, les->stream>>>(pw, pp, HW, (float)(1.0 / c->scale[0]),
-                                                             (float)(1.0 / c->scale[1]), c->sumsq, c->X0);
+int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab, cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    const s2d_handle* h0 = runs[0];
+    const Dims& d = h0->d;
+    const LesRun<T>* R = (const LesRun<T>*)tab;
+    const long HW = (long)d.M * d.M;
+    const Launch& Ly = h0->L_yinv;
+    const Launch& Lx = h0->L_xrow;
+    const Launch& Ls = h0->L_ystore;
+    const int nparts = (d.M + Lx.G - 1) / Lx.G;
+    const VT* tw = (const VT*)h0->tw;
+    k_cl_yinv<T><<<dim3(2 * ((d.KX + Ly.G - 1) / Ly.G), n), Ly.threads, Ly.smem, st>>>(d, R, h0->rk2, tw, Ly.G);
+    k_cl_xinv<T><<<dim3(nparts, n), Lx.threads, Lx.smem, st>>>(d, R, tw, Lx.G);
+    const int chunks = (int)std::min<long>((HW + 255) / 256, 64);
+    k_cl_pack<T><<<dim3(chunks, n), 256, 0, st>>>(R, nparts, HW, (float)(1.0 / c->scale[0]),
+                                                  (float)(1.0 / c->scale[1]), c->X0);
     C_CUDA(cudaGetLastError());
-    // the network runs on the LES stream: borrow it for the forward pass
+    // the network runs on the caller's stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
-    c->stream = les->stream;
-    r = forward(c, 1);
+    c->stream = st;
+    const int r = forward(c, n);
     c->stream = saved;
     if (r != S2D_OK) return r;
-    k_scale_out<T><<<nblocks(HW, 256), 256, 0, les->stream>>>(c->Y, HW, -c->scale[2], c->sumsq, ppi);
+    k_cl_xfwd<T><<<dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st>>>(
+        d, R, nparts, c->Y, -c->scale[2], tw, Lx.G, (T)(0.5 / ((double)d.M * (double)d.M)));
+    k_cl_ystore<T><<<dim3((d.KX + Ls.G - 1) / Ls.G, n), Ls.threads, Ls.smem, st>>>(d, R, tw, Ls.G);
     C_CUDA(cudaGetLastError());
-    C_CUDA(Kern<T>::xfwd_phys(les->d, ppi, les->I[2], les->tw, les->stream, les->L_xrow));
-    C_CUDA(Kern<T>::yfwd_store(les->d, les->I[2], les->src, les->tw, les->stream, les->L_ystore));
     return S2D_OK;
 }
 
@@ -714,6 +885,25 @@ int physical_pair_t(s2d_handle* h, const void* S, int opA, int opB, void* outA, 
 }
 
 }  // namespace
+
+int s2d::ensure_closure_buffers(s2d_handle* h) {
+    int r = ensure_les_buffers(h);
+    if (r != S2D_OK) return r;
+    if (!h->src) C_CUDA(cudaMalloc(&h->src, (size_t)h->d.KX * h->d.ldS * h->vsz));
+    return S2D_OK;
+}
+
+int s2d::closure_table(s2d_handle* const* runs, int n, void** tab) { return closure_table_impl(runs, n, tab); }
+
+int s2d::closure_terms(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab, cudaStream_t st) {
+    if (!c || !runs || n <= 0 || !tab) return cerr(S2D_ERR_INVALID, "bad closure arguments");
+    if (n > c->maxB) return cerr(S2D_ERR_INVALID, "more runs than the network's batch capacity");
+    return runs[0]->prec == S2D_FP64 ? closure_terms_t<double>(c, runs, n, tab, st)
+                                     : closure_terms_t<float>(c, runs, n, tab, st);
+}
+
+int s2d::cnn_grid(const s2d_cnn* c) { return c->H; }
+int s2d::cnn_max_batch(const s2d_cnn* c) { return c->maxB; }
 
 int s2d::physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB) {
     return h->prec == S2D_FP64 ? physical_pair_t<double>(h, S, opA, opB, outA, outB)
@@ -1098,22 +1288,27 @@ S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
     if (c && les->d.M != c->H) return cerr(S2D_ERR_INVALID, "network grid differs from the LES collocation grid");
     C_CUDA(cudaSetDevice(les->device));
     if (c) {
-        int r = ensure_les_buffers(les);
+        int r = s2d::ensure_closure_buffers(les);
         if (r != S2D_OK) return r;
-        if (!les->src) C_CUDA(cudaMalloc(&les->src, (size_t)les->d.KX * les->d.ldS * les->vsz));
+        if (!les->les_tab) {
+            r = closure_table_impl(&les, 1, &les->les_tab);
+            if (r != S2D_OK) return r;
+        }
     } else if (les->src) {
         C_CUDA(cudaStreamSynchronize(les->stream));
         cudaFree(les->src);
         les->src = nullptr;
+        cudaFree(les->les_tab);
+        les->les_tab = nullptr;
     }
     les->cnn = c;
     return S2D_OK;
 }
 
 S2D_API int s2d_les_closure_term(s2d_handle* les) {
-    if (!les || !les->cnn || !les->src) return cerr(S2D_ERR_INVALID, "no closure set");
+    if (!les || !les->cnn || !les->src || !les->les_tab) return cerr(S2D_ERR_INVALID, "no closure set");
     C_CUDA(cudaSetDevice(les->device));
-    return les->prec == S2D_FP64 ? closure_term<double>(les) : closure_term<float>(les);
+    return s2d::closure_terms(les->cnn, &les, 1, les->les_tab, les->stream);
 }
 
 S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {

@@ -145,6 +145,7 @@ struct s2d_handle {
     void* pi = nullptr;  // subgrid flux of the filtered DNS (compact layout, LES handles)
     void* phys = nullptr;          // 3 physical fields on the collocation grid (closure), 8 B/element
     struct s2d_cnn* cnn = nullptr; // closure network used by s2d_les_integrate_steps
+    void* les_tab = nullptr;       // device table of closure_terms for this handle alone
     void* Ibase = nullptr;
     void* I[3] = {nullptr, nullptr, nullptr};
     size_t Ibytes = 0;
@@ -176,6 +177,19 @@ cudaError_t configure_kernels(int max_smem_optin);
 // on the M x M collocation grid, row-major, in the handle's precision; outB
 // may be null.  Asynchronous on the handle's stream.
 int physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB);
+
+// Closure terms of n LES runs of one grid and precision (the network's grid):
+// physical (w, psi) of every run, its rms vorticity, one network forward over
+// all n runs, rescale, forward transform with truncation into each run's src.
+// closure_table allocates the device table the kernels read (per-run
+// pointers and partial sums; free with cudaFree); closure_terms enqueues the
+// work on st.  Every run needs src and phys buffers (ensure_closure_buffers).
+int ensure_closure_buffers(s2d_handle* h);
+int closure_table(s2d_handle* const* runs, int n, void** tab);
+int closure_terms(struct s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab, cudaStream_t st);
+// the network's grid and batch capacity
+int cnn_grid(const struct s2d_cnn* c);
+int cnn_max_batch(const struct s2d_cnn* c);
 
 // Record msg as this thread's last error (s2d_last_error) and return code.
 int set_error(int code, const char* msg);

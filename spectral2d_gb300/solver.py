@@ -314,6 +314,12 @@ class Ensemble:
     def synchronize(self) -> None:
         L.check(self._L.s2d_batch_synchronize(self._b))
 
+    def set_closure(self, net: "ClosureNet | None") -> None:
+        """One closure network for every run (all on its grid): each step
+        starts with one network forward over the whole batch."""
+        L.check(self._L.s2d_batch_set_closure(self._b, net._c if net is not None else None))
+        self._net = net   # keep the network alive while attached
+
     def tune(self):
         """Autotune the tile schedule; returns (threads, ctas_per_sm, ms_per_step)."""
         t, c, ms = C.c_int32(), C.c_int32(), C.c_double()

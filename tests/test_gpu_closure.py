@@ -138,3 +138,32 @@ def test_les_with_closure_runs_and_changes_the_solution(S, precision):
     d = O.rel_l2(wa, wb)
     print(f"{precision}: closure changes the 20-step LES state by rel-L2 {d:.2e}")
     assert 1e-8 < d < 0.5
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_batched_closure_les_matches_single_runs(S, precision):
+    """A batch of LES runs with one closure network (one forward over all
+    runs per step) against each run advanced alone with the same network."""
+    n, nu, steps = 16, 2e-3, 12
+    with S.ClosureNet(24, max_batch=8, seed=5) as net:
+        dt = _dataset(S, net, nsnap=8)
+        net.set_scales(net.dataset_stats())
+        net.train_epoch(0, 8, 8, 1e-3, seed=0)
+        w0 = [O.random_state(O.get_grid_size(n, n), 30 + i, decay=0.2) for i in range(3)]
+        with S.Ensemble([n] * 3, [nu] * 3, precision=precision) as ens:
+            for i in range(3):
+                ens.runs[i].set_state(w0[i])
+            ens.set_dt([dt] * 3)
+            ens.set_closure(net)
+            ens.integrate_steps(steps)
+            ens.status()
+            wb = [r.get_state()[0] for r in ens.runs]
+            ens.set_closure(None)
+        for i in range(3):
+            with S.Spectral2D(n, nu=nu, precision=precision) as a:
+                a.set_state(w0[i])
+                S.les_set_closure(a, net)
+                S.les_integrate_steps(a, steps, dt)
+                wa, _ = a.get_state()
+                S.les_set_closure(a, None)
+            assert np.array_equal(wa, wb[i]), O.rel_l2(wb[i], wa)

@@ -282,3 +282,29 @@ def test_full_size_one_step_vs_oracle(S2D):
     err = O.rel_l2(w1, wr)
     print(f"2048^2 one step: rel-L2 {err:.3e}")
     assert err < 1e-12
+
+
+def test_kolmogorov_4096_one_step_vs_oracle(S2D):
+    """The 4096^2 (6144^2 padded) Kolmogorov-flow workload, F = 4 cos(4y),
+    drag 0.1, nu = 1e-5: one FP64 RK3 step from a seeded state against the
+    oracle, and the FP32 form against the same oracle step."""
+    n, nu, alpha, amp, kf = 4096, 1e-5, 0.1, 4.0, 4
+    g = O.get_grid_size(n, n)
+    O.set_workers(O.cpu_count())
+    with S2D(n, nu=nu, alpha=alpha, forcing_amp=amp, forcing_k=kf) as s:
+        s.set_turbulent_velocity(seed=1, spectrum="k4gauss", k0=10.0, tke=0.5)
+        w0, _ = s.get_state()
+        dt = s.compute_time_step(0.5)
+        s.integrate_one_step(dt)
+        s.check_finite()
+        w1, _ = s.get_state()
+    with S2D(n, nu=nu, alpha=alpha, forcing_amp=amp, forcing_k=kf, precision="fp32") as s:
+        s.set_state(w0)
+        s.integrate_one_step(dt)
+        w32, _ = s.get_state()
+    wo, po = _oracle_state(w0, g)
+    F = O.kolmogorov_forcing(g, amp, kf)
+    wr, _ = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False, forcing=F, alpha=alpha)
+    err, err32 = O.rel_l2(w1, wr), O.rel_l2(w32, wr)
+    print(f"4096^2 Kolmogorov one step: FP64 rel-L2 {err:.3e}, FP32 rel-L2 {err32:.3e}")
+    assert err < 1e-12 and err32 < 1e-5
