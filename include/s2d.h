@@ -273,6 +273,10 @@ S2D_API int s2d_cnn_set_params(s2d_cnn* c, const float* params);
 /* normalisation: rms of w, psi and Pi (inputs divided, output multiplied) */
 S2D_API int s2d_cnn_set_scales(s2d_cnn* c, const double* rms3);
 S2D_API int s2d_cnn_get_scales(const s2d_cnn* c, double* rms3);
+/* band of the closure term in the LES: modes with |k| < k_min get none
+ * (default 0: every retained mode) */
+S2D_API int s2d_cnn_set_band(s2d_cnn* c, double k_min);
+S2D_API int s2d_cnn_get_band(const s2d_cnn* c, double* k_min);
 /* x: batch x grid x grid x 2 (w, psi); y: batch x grid x grid (Pi) */
 S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t batch, float* y);
 /* MSE loss of the normalised output against target/rms_Pi and its gradient

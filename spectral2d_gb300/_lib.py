@@ -105,6 +105,8 @@ SIGNATURES = {
     "s2d_cnn_set_params": (C.c_int, [C.c_void_p, _fp]),
     "s2d_cnn_set_scales": (C.c_int, [C.c_void_p, _dp]),
     "s2d_cnn_get_scales": (C.c_int, [C.c_void_p, _dp]),
+    "s2d_cnn_set_band": (C.c_int, [C.c_void_p, C.c_double]),
+    "s2d_cnn_get_band": (C.c_int, [C.c_void_p, _dp]),
     "s2d_cnn_forward_host": (C.c_int, [C.c_void_p, _fp, C.c_int32, _fp]),
     "s2d_cnn_grad_host": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int32, _fp, _dp]),
     "s2d_cnn_dataset_reserve": (C.c_int, [C.c_void_p, C.c_int32]),

@@ -24,6 +24,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import time
 
 import numpy as np
@@ -58,95 +59,118 @@ def generate(net, seeds, n_dns, n_les, nu, cfl, spinup, nsnap, every, log=print)
     return dts, time.time() - t0
 
 
-def train(net, n, epochs, batch, lr, log=print):
+def train(net, n, epochs, batch, lr, lr_min_frac=0.05, log=print):
+    """Adam over the first 90% of the pairs (the rest validates), the
+    learning rate following a cosine from lr down to lr * lr_min_frac."""
     nval = max(batch, n // 10)
     ntr = n - nval
     hist = []
     t0 = time.time()
     for e in range(epochs):
-        tr = net.train_epoch(0, ntr, batch, lr, seed=1000 + e)
+        f = lr_min_frac + (1.0 - lr_min_frac) * 0.5 * (1.0 + math.cos(math.pi * e / max(1, epochs - 1)))
+        tr = net.train_epoch(0, ntr, batch, lr * f, seed=1000 + e)
         va = net.eval(ntr, nval)
         hist.append((tr, va))
         if e % 10 == 0 or e == epochs - 1:
-            log(f"epoch {e}: train {tr:.4f} val {va:.4f} ({time.time() - t0:.1f} s)")
+            log(f"epoch {e}: train {tr:.4f} val {va:.4f} lr {lr * f:.2e} ({time.time() - t0:.1f} s)")
     return hist, time.time() - t0
 
 
-def _rel_err(a, b, kmax):
-    k = np.arange(1, kmax + 1)
-    return np.abs(a[k] - b[k]) / np.abs(b[k])
+KMAX = 40   # spectra are compared for 1 <= k <= KMAX
 
 
-def evaluate(net, seeds, n_dns, n_les, nu, cfl, steps, every, les_precision="fp32", log=print):
-    """DNS vs LES with and without the closure on held-out seeds."""
+def _rel_err(a, b):
+    return np.abs(a - b) / np.abs(b)
+
+
+def evaluate(net, seeds, n_dns, n_les, nu, cfl, steps, every, bands=(0.0,), les_precision="fp32",
+             log=print):
+    """The FP64 DNS against 128^2 LES runs started from its filtered state:
+    one without closure (the fallback) and one with the closure per band
+    k_min.  Per report: the LES and filtered-DNS spectra for k <= KMAX, TKE,
+    enstrophy, and the wall-clock per step of every solver."""
     out = []
+    names = ["none"] + [f"closure_k{b:g}" for b in bands]
     for s in seeds:
-        with S.Spectral2D(n_dns, nu=nu) as dns, S.Spectral2D(n_les, nu=nu) as filt, \
-                S.Spectral2D(n_les, nu=nu, precision=les_precision) as les_c, \
-                S.Spectral2D(n_les, nu=nu, precision=les_precision) as les_0:
+        with S.Spectral2D(n_dns, nu=nu) as dns, S.Spectral2D(n_les, nu=nu) as filt:
+            les = {nm: S.Spectral2D(n_les, nu=nu, precision=les_precision) for nm in names}
             dns.set_turbulent_velocity(seed=s, spectrum="k4gauss", k0=10.0, tke=0.5)
             dt = dns.compute_time_step(cfl)
-            S.filter_state(dns, les_c)
-            S.filter_state(dns, les_0)
-            S.les_set_closure(les_c, net)
-            rec = {"seed": s, "dt": dt, "t": [], "err_closure": [], "err_none": [],
-                   "enst_dns": [], "enst_closure": [], "enst_none": [], "tke_dns": [],
-                   "tke_closure": [], "tke_none": []}
-            t_dns = t_c = t_0 = 0.0
+            for nm, h in les.items():
+                S.filter_state(dns, h)
+                if nm != "none":
+                    S.les_set_closure(h, net)
+            rec = {"seed": s, "dt": dt, "t": [], "E": {nm: [] for nm in ["dns"] + names},
+                   "tke": {nm: [] for nm in ["dns"] + names}, "enst": {nm: [] for nm in ["dns"] + names}}
+            wall = {nm: 0.0 for nm in ["dns"] + names}
             for done in range(0, steps, every):
                 n = min(every, steps - done)
                 dns.synchronize()
                 a = time.perf_counter()
                 dns.integrate_steps(n, dt)
                 dns.synchronize()
-                b = time.perf_counter()
-                S.les_integrate_steps(les_c, n, dt)
-                les_c.synchronize()
-                c = time.perf_counter()
-                les_0.integrate_steps(n, dt)
-                les_0.synchronize()
-                d = time.perf_counter()
-                t_dns += b - a
-                t_c += c - b
-                t_0 += d - c
+                wall["dns"] += time.perf_counter() - a
+                for nm, h in les.items():
+                    if nm != "none":   # the band is read when the step's graph is built
+                        net.band = bands[names.index(nm) - 1]
+                    h.synchronize()
+                    a = time.perf_counter()
+                    S.les_integrate_steps(h, n, dt)
+                    h.synchronize()
+                    wall[nm] += time.perf_counter() - a
                 S.filter_state(dns, filt)
-                Ef, tf, zf = _spectrum(filt)
-                Ec, tc, zc = _spectrum(les_c)
-                E0, t0_, z0 = _spectrum(les_0)
                 rec["t"].append((done + n) * dt)
-                rec["err_closure"].append(_rel_err(Ec, Ef, 40).tolist())
-                rec["err_none"].append(_rel_err(E0, Ef, 40).tolist())
-                for key, v in (("enst_dns", zf), ("enst_closure", zc), ("enst_none", z0),
-                               ("tke_dns", tf), ("tke_closure", tc), ("tke_none", t0_)):
-                    rec[key].append(v)
-            les_c.check_finite()
-            S.les_set_closure(les_c, None)
-            rec["ms_per_step"] = {"dns": 1e3 * t_dns / steps, "les_closure": 1e3 * t_c / steps,
-                                  "les_none": 1e3 * t_0 / steps}
-            ec = np.array(rec["err_closure"])
-            e0 = np.array(rec["err_none"])
-            rec["summary"] = {
-                "mean_rel_err_k_le_40_closure_final": float(ec[-1].mean()),
-                "mean_rel_err_k_le_40_none_final": float(e0[-1].mean()),
-                "mean_rel_err_k_le_40_closure_time_avg": float(ec.mean()),
-                "mean_rel_err_k_le_40_none_time_avg": float(e0.mean()),
-                "max_rel_err_k_le_40_closure_final": float(ec[-1].max()),
-                "max_rel_err_k_le_40_none_final": float(e0[-1].max()),
-                "speedup_vs_dns": t_dns / t_c,
-            }
-            log(f"seed {s}: {json.dumps(rec['summary'])}")
+                for nm, h in [("dns", filt)] + list(les.items()):
+                    E, tke, z = _spectrum(h)
+                    rec["E"][nm].append(E[:KMAX + 1].tolist())
+                    rec["tke"][nm].append(tke)
+                    rec["enst"][nm].append(z)
+            for nm, h in les.items():
+                h.check_finite()
+                if nm != "none":
+                    S.les_set_closure(h, None)
+                h.close()
+            rec["ms_per_step"] = {nm: 1e3 * v / steps for nm, v in wall.items()}
+            rec["summary"] = {nm: _summary([rec], nm) for nm in names}
+            for nm in names[1:]:
+                rec["summary"][nm]["speedup_vs_dns"] = wall["dns"] / wall[nm]
+            log(f"seed {s}: " + ", ".join(f"{nm} {rec['summary'][nm]['mean_rel_err_time_avg']:.3f}"
+                                          for nm in names))
             out.append(rec)
     return out
 
 
+def _summary(recs, nm):
+    """Spectrum errors of variant nm against the filtered DNS for 1 <= k <= KMAX:
+    per seed (mean over k, then over report times, and at the final time) and
+    of the seed-averaged spectra (the ensemble statistics of the held-out
+    seeds), plus the final enstrophy error."""
+    k = slice(1, KMAX + 1)
+    per = np.array([[_rel_err(np.array(e)[k], np.array(f)[k]) for e, f in zip(r["E"][nm], r["E"]["dns"])]
+                    for r in recs])                        # seeds x times x k
+    Em = np.mean([np.array(r["E"][nm]) for r in recs], axis=0)[:, k]
+    Ed = np.mean([np.array(r["E"]["dns"]) for r in recs], axis=0)[:, k]
+    ens = _rel_err(Em, Ed)                                 # times x k
+    zf = np.array([r["enst"][nm][-1] / r["enst"]["dns"][-1] - 1.0 for r in recs])
+    return {"mean_rel_err_time_avg": float(per.mean()),
+            "mean_rel_err_final": float(per[:, -1].mean()),
+            "max_rel_err_final": float(per[:, -1].max()),
+            "seed_avg_mean_rel_err_time_avg": float(ens.mean()),
+            "seed_avg_mean_rel_err_final": float(ens[-1].mean()),
+            "seed_avg_max_rel_err_time_avg": float(ens.mean(axis=0).max()),
+            "enstrophy_rel_err_final": float(np.abs(zf).mean())}
+
+
 def save_weights(net, path):
-    np.savez_compressed(path, params=net.get_params(), scales=net.get_scales(), grid=net.grid)
+    np.savez_compressed(path, params=net.get_params(), scales=net.get_scales(), grid=net.grid,
+                        band=net.band)
 
 
 def load_weights(net, path):
     d = np.load(path)
     net.set_params(d["params"])
     net.set_scales(d["scales"])
+    net.band = float(d["band"]) if "band" in d else 0.0
 
 
 def main(argv=None):
@@ -157,11 +181,15 @@ def main(argv=None):
     ap.add_argument("--cfl", type=float, default=0.5)
     ap.add_argument("--train-seeds", type=int, default=8)
     ap.add_argument("--snaps", type=int, default=500)
-    ap.add_argument("--every", type=int, default=10)
-    ap.add_argument("--spinup", type=int, default=1000)
-    ap.add_argument("--epochs", type=int, default=60)
+    ap.add_argument("--every", type=int, default=40)
+    ap.add_argument("--spinup", type=int, default=0)
+    ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--batch", type=int, default=64)
     ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr-min-frac", type=float, default=0.05)
+    ap.add_argument("--bands", type=str, default="0,4,8,16",
+                    help="candidate k_min of the closure term, chosen on --val-seed")
+    ap.add_argument("--val-seed", type=int, default=10)
     ap.add_argument("--eval-seeds", type=str, default="8,9")
     ap.add_argument("--eval-steps", type=int, default=20000)
     ap.add_argument("--eval-every", type=int, default=1000)
@@ -172,22 +200,45 @@ def main(argv=None):
     a = ap.parse_args(argv)
     grid = 3 * a.n_les // 2
     res = {"config": vars(a)}
+    bands = [float(b) for b in a.bands.split(",") if b]
     with S.ClosureNet(grid, max_batch=a.batch, seed=0) as net:
         if a.load:
             load_weights(net, a.load)
+            bands = [net.band]
         else:
             seeds = list(range(a.train_seeds))
             dts, tg = generate(net, seeds, a.n_dns, a.n_les, a.nu, a.cfl, a.spinup, a.snaps, a.every)
             rms = net.dataset_stats()
             net.set_scales(rms)
-            hist, tt = train(net, net.dataset_size, a.epochs, a.batch, a.lr)
+            hist, tt = train(net, net.dataset_size, a.epochs, a.batch, a.lr, a.lr_min_frac)
             res.update({"pairs": net.dataset_size, "data_seconds": tg, "train_seconds": tt,
                         "rms": rms.tolist(), "loss_history": hist})
+            # the band is chosen on a validation seed that is neither trained on nor evaluated
+            if len(bands) > 1:
+                val = evaluate(net, [a.val_seed], a.n_dns, a.n_les, a.nu, a.cfl, a.eval_steps,
+                               a.eval_every, bands, a.les_precision)
+                score = {b: val[0]["summary"][f"closure_k{b:g}"]["mean_rel_err_time_avg"] for b in bands}
+                best = min(bands, key=lambda b: score[b])
+                res["band_selection"] = {"val_seed": a.val_seed, "score": {f"{b:g}": v for b, v in score.items()},
+                                         "k_min": best}
+                print(f"band chosen on seed {a.val_seed}: k_min = {best:g} ({score})")
+                bands = sorted({0.0, best})
+                net.band = best
+            else:
+                net.band = bands[0]
             if a.weights:
                 save_weights(net, a.weights)
         ev = [int(s) for s in a.eval_seeds.split(",") if s]
-        res["eval"] = evaluate(net, ev, a.n_dns, a.n_les, a.nu, a.cfl, a.eval_steps, a.eval_every,
-                               a.les_precision)
+        recs = evaluate(net, ev, a.n_dns, a.n_les, a.nu, a.cfl, a.eval_steps, a.eval_every, bands,
+                        a.les_precision)
+        res["eval"] = recs
+        res["eval_summary"] = {nm: _summary(recs, nm) for nm in recs[0]["summary"]}
+        for nm in recs[0]["summary"]:
+            if nm != "none":
+                res["eval_summary"][nm]["speedup_vs_dns"] = float(np.mean(
+                    [r["summary"][nm]["speedup_vs_dns"] for r in recs]))
+        res["k_min"] = net.band
+        print("eval summary:", json.dumps(res["eval_summary"]))
     if a.out:
         with open(a.out, "w") as f:
             json.dump(res, f)

@@ -517,10 +517,12 @@ __global__ void __launch_bounds__(512) k_cl_xfwd(Dims d, const LesRun<T>* __rest
     extract_pair(Z, R.I2 + (size_t)y1 * d.ldI, R.I2 + (size_t)(y1 + 1) * d.ldI, d, lane, active, xscale);
 }
 
-// Forward y-FFT of the columns of I2 with Truncate into src.
+// Forward y-FFT of the columns of I2 with Truncate into src; modes with
+// |k|^2 < kmin2 (the closure's band) are zero.
 template <typename T>
 __global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __restrict__ runs,
-                                                    const typename Vec<T>::t* __restrict__ tw, int G) {
+                                                    const typename Vec<T>::t* __restrict__ tw, int G,
+                                                    double kmin2) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const LesRun<T>& R = runs[blockIdx.y];
@@ -543,7 +545,8 @@ __global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __re
         const int ky = ky_of_jc(d, jc);
         const int n = jc <= d.K ? jc : ky + d.M;
         VT v = bufs[(size_t)gg * d.M + n];
-        if (kx * kx + ky * ky > d.K * d.K) v = mk<VT>((T)0, (T)0);
+        const int k2 = kx * kx + ky * ky;
+        if (k2 > d.K * d.K || (double)k2 < kmin2) v = mk<VT>((T)0, (T)0);
         R.src[(size_t)kx * d.ldS + jc] = v;
     }
 }
@@ -600,6 +603,7 @@ struct s2d_cnn {
     double* sumsq = nullptr;    // scratch accumulator (rms of one state)
     int data_cap = 0, data_n = 0;
     double scale[3] = {1.0, 1.0, 1.0};
+    double k_min = 0.0;         // the closure term is applied only where |k| >= k_min
     long step = 0;
 };
 
@@ -860,7 +864,8 @@ int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab,
     if (r != S2D_OK) return r;
     k_cl_xfwd<T><<<dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st>>>(
         d, R, nparts, c->Y, -c->scale[2], tw, Lx.G, (T)(0.5 / ((double)d.M * (double)d.M)));
-    k_cl_ystore<T><<<dim3((d.KX + Ls.G - 1) / Ls.G, n), Ls.threads, Ls.smem, st>>>(d, R, tw, Ls.G);
+    k_cl_ystore<T><<<dim3((d.KX + Ls.G - 1) / Ls.G, n), Ls.threads, Ls.smem, st>>>(d, R, tw, Ls.G,
+                                                                                 c->k_min * c->k_min);
     C_CUDA(cudaGetLastError());
     return S2D_OK;
 }
@@ -1047,6 +1052,18 @@ S2D_API int s2d_cnn_set_scales(s2d_cnn* c, const double* s) {
 S2D_API int s2d_cnn_get_scales(const s2d_cnn* c, double* s) {
     if (!c || !s) return cerr(S2D_ERR_INVALID, "null argument");
     for (int i = 0; i < 3; ++i) s[i] = c->scale[i];
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_set_band(s2d_cnn* c, double k_min) {
+    if (!c || !(k_min >= 0.0) || !std::isfinite(k_min)) return cerr(S2D_ERR_INVALID, "k_min must be >= 0");
+    c->k_min = k_min;
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_get_band(const s2d_cnn* c, double* k_min) {
+    if (!c || !k_min) return cerr(S2D_ERR_INVALID, "null argument");
+    *k_min = c->k_min;
     return S2D_OK;
 }
 

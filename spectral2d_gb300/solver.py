@@ -384,6 +384,17 @@ class ClosureNet:
         L.check(self._L.s2d_cnn_get_scales(self._c, _dptr(a)))
         return a
 
+    @property
+    def band(self) -> float:
+        """k_min: the closure term is applied to modes with |k| >= k_min."""
+        v = C.c_double()
+        L.check(self._L.s2d_cnn_get_band(self._c, C.byref(v)))
+        return v.value
+
+    @band.setter
+    def band(self, k_min: float) -> None:
+        L.check(self._L.s2d_cnn_set_band(self._c, float(k_min)))
+
     def forward(self, x: np.ndarray) -> np.ndarray:
         """x: (B, grid, grid, 2) (w, psi) -> (B, grid, grid) Pi."""
         x = np.ascontiguousarray(x, dtype=np.float32)
