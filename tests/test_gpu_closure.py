@@ -167,3 +167,47 @@ def test_batched_closure_les_matches_single_runs(S, precision):
                 wa, _ = a.get_state()
                 S.les_set_closure(a, None)
             assert np.array_equal(wa, wb[i]), O.rel_l2(wb[i], wa)
+
+
+def test_trained_closure_beats_the_closure_free_les(S):
+    """The packaged closure (trained on the FP64 2048^2 DNS of seeds 0-7)
+    against the closure-free 128^2 LES on held-out seed 9: both start from
+    the filtered DNS state and advance 5000 steps with the DNS's dt; the
+    closure's energy-spectrum error (1 <= k <= 40) is well below the
+    fallback's, and the LES with closure is >= 20x cheaper than the DNS."""
+    import os
+    import time
+    from spectral2d_gb300 import closure
+    path = os.path.join(os.path.dirname(S.__file__), "data", "closure_les128.npz")
+    assert os.path.exists(path), "trained closure weights are missing"
+    steps, k = 5000, slice(1, 41)
+    with S.ClosureNet(192, max_batch=1) as net:
+        closure.load_weights(net, path)
+        with S.Spectral2D(2048, nu=1e-4) as dns, S.Spectral2D(128, nu=1e-4) as filt, \
+                S.Spectral2D(128, nu=1e-4, precision="fp32") as les_c, \
+                S.Spectral2D(128, nu=1e-4, precision="fp32") as les_0:
+            dns.set_turbulent_velocity(seed=9, spectrum="k4gauss", k0=10.0, tke=0.5)
+            dt = dns.compute_time_step(0.5)
+            S.filter_state(dns, les_c)
+            S.filter_state(dns, les_0)
+            S.les_set_closure(les_c, net)
+            dns.synchronize()
+            t0 = time.perf_counter()
+            dns.integrate_steps(steps, dt)
+            dns.synchronize()
+            t1 = time.perf_counter()
+            S.les_integrate_steps(les_c, steps, dt)
+            les_c.synchronize()
+            t2 = time.perf_counter()
+            les_0.integrate_steps(steps, dt)
+            S.filter_state(dns, filt)
+            Ef = filt.compute_spectrum()[1][k]
+            Ec = les_c.compute_spectrum()[1][k]
+            E0 = les_0.compute_spectrum()[1][k]
+            S.les_set_closure(les_c, None)
+    ec = float(np.mean(np.abs(Ec - Ef) / Ef))
+    e0 = float(np.mean(np.abs(E0 - Ef) / Ef))
+    speedup = (t1 - t0) / (t2 - t1)
+    print(f"seed 9, {steps} steps: E(k) mean rel err closure {ec:.3f}, none {e0:.3f}; speedup {speedup:.1f}x")
+    assert ec < 0.6 * e0
+    assert speedup >= 20.0

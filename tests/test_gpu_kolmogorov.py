@@ -14,4 +14,4 @@ def test_fp32_tracks_fp64(built_lib):
     last = res["reports"][-1]
     assert last["step"] == 400
     assert last["w_rel_l2"] < 1e-4 and last["Ek_max_rel_err"] < 1e-3
-    assert last["enstrophy_rel_err"] < 1e-5
+    assert last["enstrophy_rel_err"] < 1e-4
