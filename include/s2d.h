@@ -263,7 +263,8 @@ S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm,
  * LES collocation grid.  Handles that make training data (DNS and LES) must
  * be FP64; an LES advanced with a closure may be FP64 or FP32. */
 typedef struct s2d_cnn s2d_cnn;
-/* grid = LES collocation grid (3*nx_les/2); max_batch = largest batch */
+/* grid = LES collocation grid (3*nx_les/2); max_batch = largest batch
+ * (max_batch * grid^2 * 32 < 2^31) */
 S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32_t device, s2d_cnn** out);
 S2D_API void s2d_cnn_destroy(s2d_cnn* c);
 S2D_API int s2d_cnn_num_params(const s2d_cnn* c);

@@ -77,68 +77,113 @@ __device__ __forceinline__ long nbr(long p, int dy, int dx, int H, int Wd) {
     return b * HW + (long)y * Wd + x;
 }
 
-// Implicit-GEMM convolution on the tensor cores.  A warp owns 16 pixels x
-// NC channels; the K loop runs over 9 taps x KC/16 chunks of 16 channels.
+// Implicit-GEMM convolution on the tensor cores.  A warp owns kConvGroups
+// groups of 16 consecutive pixels x NC channels; the K loop runs over 9 taps x
+// KC/16 chunks of 16 channels, and each chunk's weight fragments are loaded
+// once and used for all of the warp's pixel groups.
 //   FWD (SIGN = +1): out[p, n] = sum_{t,k} in[p + off_t, k] W[n, t, k]
 //   data gradient (SIGN = -1): out[q, n] = sum_{t,k} in[q - off_t, k] W^T[n, t, k]
 // Epilogue EPI: 0 = + bias, store z and gelu(z) (BF16); 1 = + bias, store
 // channel 0 as FP32; 2 = multiply by gelu'(zprev), store BF16.
+constexpr int kConvGroups = 4;
+constexpr int kConvPixelsPerCta = 8 * 16 * kConvGroups;   // 8 warps
+
 template <int KC, int NC, int SIGN, int EPI>
-__global__ void __launch_bounds__(256) k_conv_mma(const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(256, 2) k_conv_mma(const __nv_bfloat16* __restrict__ in,
                                                   const __nv_bfloat16* __restrict__ W,
                                                   const float* __restrict__ bias,
                                                   const __nv_bfloat16* __restrict__ zprev, __nv_bfloat16* z,
                                                   __nv_bfloat16* a, float* yout, long P, int H, int Wd) {
+    constexpr int PG = kConvGroups;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, tg = lane & 3;
-    const long p0 = ((long)blockIdx.x * 8 + warp) * 16;
-    if (p0 >= P) return;
-    const long pA = p0 + g, pB = pA + 8;
-    const bool vA = pA < P, vB = pB < P;
-    constexpr int NT = NC / 8;
-    float acc[NT][4];
+    const long pw = ((long)blockIdx.x * 8 + warp) * (16 * PG);
+    if (pw >= P) return;
+    const int HW = H * Wd;   // P * 32 < 2^31 (checked at s2d_cnn_create)
+    // rows g and g+8 of each group: image base, y, x (y < 0: past the end)
+    int base[PG][2], py[PG][2], px[PG][2];
 #pragma unroll
-    for (int i = 0; i < NT; ++i) acc[i][0] = acc[i][1] = acc[i][2] = acc[i][3] = 0.f;
+    for (int q = 0; q < PG; ++q)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const long p = pw + q * 16 + g + 8 * h;
+            if (p < P) {
+                const int pi = (int)p;
+                const int b = pi / HW;
+                const int rem = pi - b * HW;
+                base[q][h] = b * HW;
+                py[q][h] = rem / Wd;
+                px[q][h] = rem - py[q][h] * Wd;
+            } else {
+                base[q][h] = 0;
+                py[q][h] = -1;
+                px[q][h] = 0;
+            }
+        }
+    constexpr int NT = NC / 8;
+    float acc[PG][NT][4];
+#pragma unroll
+    for (int q = 0; q < PG; ++q)
+#pragma unroll
+        for (int i = 0; i < NT; ++i) acc[q][i][0] = acc[q][i][1] = acc[q][i][2] = acc[q][i][3] = 0.f;
 #pragma unroll 1
     for (int t = 0; t < 9; ++t) {
         const int dy = SIGN * (t / 3 - 1), dx = SIGN * (t % 3 - 1);
-        const __nv_bfloat16* rA = in + nbr(vA ? pA : 0, dy, dx, H, Wd) * KC;
-        const __nv_bfloat16* rB = in + nbr(vB ? pB : 0, dy, dx, H, Wd) * KC;
+        int off[PG][2];   // element offset of the neighbour pixel's channels, -1 past the end
+#pragma unroll
+        for (int q = 0; q < PG; ++q)
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                int yy = py[q][h] + dy, xx = px[q][h] + dx;
+                yy += (yy < 0) ? H : ((yy >= H) ? -H : 0);
+                xx += (xx < 0) ? Wd : ((xx >= Wd) ? -Wd : 0);
+                off[q][h] = py[q][h] < 0 ? -1 : (base[q][h] + yy * Wd + xx) * KC;
+            }
 #pragma unroll
         for (int c = 0; c < KC; c += 16) {
-            const uint32_t a0 = vA ? ld32(rA + c + tg * 2) : 0u;
-            const uint32_t a1 = vB ? ld32(rB + c + tg * 2) : 0u;
-            const uint32_t a2 = vA ? ld32(rA + c + tg * 2 + 8) : 0u;
-            const uint32_t a3 = vB ? ld32(rB + c + tg * 2 + 8) : 0u;
+            uint32_t bw[NT][2];
 #pragma unroll
             for (int nt = 0; nt < NT; ++nt) {
                 const __nv_bfloat16* wr = W + ((long)(nt * 8 + g) * 9 + t) * KC + c;
-                mma_bf16(acc[nt], a0, a1, a2, a3, ld32(wr + tg * 2), ld32(wr + tg * 2 + 8));
+                bw[nt][0] = ld32(wr + tg * 2);
+                bw[nt][1] = ld32(wr + tg * 2 + 8);
+            }
+#pragma unroll
+            for (int q = 0; q < PG; ++q) {
+                const int oA = off[q][0], oB = off[q][1];
+                const uint32_t a0 = oA >= 0 ? ld32(in + oA + c + tg * 2) : 0u;
+                const uint32_t a1 = oB >= 0 ? ld32(in + oB + c + tg * 2) : 0u;
+                const uint32_t a2 = oA >= 0 ? ld32(in + oA + c + tg * 2 + 8) : 0u;
+                const uint32_t a3 = oB >= 0 ? ld32(in + oB + c + tg * 2 + 8) : 0u;
+#pragma unroll
+                for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[q][nt], a0, a1, a2, a3, bw[nt][0], bw[nt][1]);
             }
         }
     }
 #pragma unroll
-    for (int nt = 0; nt < NT; ++nt) {
-        const int n0 = nt * 8 + tg * 2;
+    for (int q = 0; q < PG; ++q)
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const long p = h ? pB : pA;
-            if (!(h ? vB : vA)) continue;
-            float v0 = acc[nt][2 * h], v1 = acc[nt][2 * h + 1];
-            if (EPI == 0) {
-                v0 += bias[n0];
-                v1 += bias[n0 + 1];
-                *reinterpret_cast<uint32_t*>(z + p * NC + n0) = pack_bf16(v0, v1);
-                *reinterpret_cast<uint32_t*>(a + p * NC + n0) = pack_bf16(gelu_f(v0), gelu_f(v1));
-            } else if (EPI == 1) {
-                if (n0 == 0) yout[p] = v0 + bias[0];
-            } else {
-                const float2 zz = unpack_bf16(ld32(zprev + p * NC + n0));
-                *reinterpret_cast<uint32_t*>(z + p * NC + n0) =
-                    pack_bf16(v0 * gelu_grad_f(zz.x), v1 * gelu_grad_f(zz.y));
+        for (int nt = 0; nt < NT; ++nt) {
+            const int n0 = nt * 8 + tg * 2;
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                if (py[q][h] < 0) continue;
+                const long p = pw + q * 16 + g + 8 * h;
+                float v0 = acc[q][nt][2 * h], v1 = acc[q][nt][2 * h + 1];
+                if (EPI == 0) {
+                    v0 += bias[n0];
+                    v1 += bias[n0 + 1];
+                    *reinterpret_cast<uint32_t*>(z + p * NC + n0) = pack_bf16(v0, v1);
+                    *reinterpret_cast<uint32_t*>(a + p * NC + n0) = pack_bf16(gelu_f(v0), gelu_f(v1));
+                } else if (EPI == 1) {
+                    if (n0 == 0) yout[p] = v0 + bias[0];
+                } else {
+                    const float2 zz = unpack_bf16(ld32(zprev + p * NC + n0));
+                    *reinterpret_cast<uint32_t*>(z + p * NC + n0) =
+                        pack_bf16(v0 * gelu_grad_f(zz.x), v1 * gelu_grad_f(zz.y));
+                }
             }
         }
-    }
 }
 
 // Weight and bias gradient of one layer on the FP32 pipes:
@@ -632,7 +677,7 @@ int refresh_all(s2d_cnn* c) {
 // forward of the batch in X0 (B images)
 int forward(s2d_cnn* c, int B) {
     const long P = (long)B * c->H * c->Wd;
-    const int grid = (int)((P + 127) / 128);
+    const int grid = (int)((P + kConvPixelsPerCta - 1) / kConvPixelsPerCta);
     const float* bias[kLayers];
     for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
     k_conv_mma<16, 32, 1, 0><<<grid, 256, 0, c->stream>>>(c->X0, c->Wb[0], bias[0], nullptr, c->Z[0], c->A[0],
@@ -649,7 +694,7 @@ int forward(s2d_cnn* c, int B) {
 // loss of the batch (targets in tgt) and, with grads, the full backward pass
 int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
     const long P = (long)B * c->H * c->Wd;
-    const int grid = (int)((P + 127) / 128);
+    const int grid = (int)((P + kConvPixelsPerCta - 1) / kConvPixelsPerCta);
     const int lb = 256;
     k_mse<<<lb, 256, 0, c->stream>>>(c->Y, c->tgt, P, 1.0f / (float)P, c->dZ6, 16, c->lpart);
     C_CUDA(cudaGetLastError());
@@ -919,6 +964,9 @@ extern "C" {
 
 S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32_t device, s2d_cnn** out) {
     if (!out || grid < 8 || max_batch < 1) return cerr(S2D_ERR_INVALID, "bad network arguments");
+    // activations are indexed with 32-bit offsets (32 channels per pixel)
+    if ((long long)max_batch * grid * grid * 32 >= (1LL << 31))
+        return cerr(S2D_ERR_INVALID, "max_batch * grid^2 * 32 must stay below 2^31");
     *out = nullptr;
     s2d_cnn* c = new (std::nothrow) s2d_cnn();
     if (!c) return cerr(S2D_ERR_NOMEM, "host allocation failed");

@@ -1,4 +1,4 @@
-// s2d_fft.cuh -- block-level mixed-radix (2, 3, 4) Stockham FFT in shared memory.
+// s2d_fft.cuh -- block-level mixed-radix Stockham FFT in shared memory.
 //
 // One transform of length M is owned by Tg = M/12 consecutive threads; a CTA
 // runs several transforms of the same length side by side.  Each pass with
@@ -12,8 +12,14 @@
 //
 // FP64 on GB300 has a small fraction of the FP32 issue rate, so the code is
 // written to minimise FP64 instructions: twiddles come from a table (a load,
-// not a sincos), complex twiddle products are 2 MUL + 2 FMA, and the radix-3
-// and radix-4 butterflies use only additions and FMAs.
+// not a sincos), twiddled radix-4/2 passes use the FMA form (TwEnt), and the
+// radix-3 and radix-4 butterflies use only additions and FMAs.
+//
+// FP32 has 64x the FP64 rate; there the in-place passes through shared
+// memory and their barriers are the cost.  When 48 | M, an FP32 transform
+// uses Tg = M/48 threads of 48 elements each and radices up to 48, built as
+// Cooley-Tukey DFTs in registers (dft_ct) with compile-time twiddles: a
+// 3072-point transform takes 3 passes instead of 6.
 #pragma once
 
 #include "s2d_internal.h"
