@@ -6,15 +6,20 @@
 //                (ComputePsi :508-560, ComputeVelocity :576-610) -> inverse
 //                y-FFT of each kx column (the y half of TransformC2R :772-781,
 //                pruned to the N/2+1 non-zero columns) -> half-spectral rows.
-//   K2 xpass     per pair of physical rows: inverse x-FFTs of (u,v) and of
-//                omega (two real rows packed in one complex FFT), the
-//                products u*w and v*w (:442-447), forward x-FFTs and the
-//                real/imaginary split (the x half of TransformR2C :749-763,
-//                normalisation folded in).  Physical fields never touch HBM.
+//   K2 xpass     per physical row (Basdevant form, the default): one inverse
+//                x-FFT of u + i v, the products u v and v^2 - u^2, one
+//                forward x-FFT and the real/imaginary split (the x halves of
+//                TransformC2R / TransformR2C :749-781, normalisation folded
+//                in).  The reference's conservative form (k_xpass_rhs) works
+//                on row pairs: inverse FFTs of (u, v) and omega, the products
+//                u w and v w (:442-447), forward FFTs.  Physical fields never
+//                touch HBM.
 //   K3 yfwd_rk3  forward y-FFT of each kx column of the two products, then
-//                Truncate (:457-458), i kx / i ky (:464-465), the viscous term
-//                (:479) and the TVD-RK3 stage combination with ComputePsi and
-//                Truncate (src/TimeIntegration.F90:156-209) in one epilogue.
+//                Truncate (:457-458), the derivatives -- (kx^2 - ky^2) and
+//                kx ky (Basdevant) or i kx / i ky (:464-465) -- the viscous
+//                term (:479), drag, forcing and an optional source, and the
+//                TVD-RK3 stage combination with ComputePsi and Truncate
+//                (src/TimeIntegration.F90:156-209) in one epilogue.
 //
 // omega is not round-tripped through physical space (the reference does at
 // :435/:453); that changes omega by round-off only.
