@@ -63,7 +63,7 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_batch_stage(const RunDev<T>* __restrict__ runs, int nruns,
+__global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict__ runs, int nruns,
                                                      const int4* __restrict__ tasks, int ntasks, int stage,
                                                      int* ctrl, int* done, unsigned int* flags) {
     using VT = typename Vec<T>::t;
@@ -226,8 +226,7 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
         R.tw = (const VT*)h->tw;
         R.dt = b->dt[i];
         const int Tg = h->d.Tg;
-        if (Tg > threads || threads % Tg || threads > FftCta<T>::max_threads)
-            return berr(S2D_ERR_UNSUPPORTED, "tile shape does not fit a run");
+        if (Tg > threads || threads % Tg) return berr(S2D_ERR_UNSUPPORTED, "tile shape does not fit a run");
         R.G12 = threads / Tg;
         R.G3 = std::max(1, threads / (2 * Tg));
         R.ntask[0] = 2 * ((h->d.KX + R.G12 - 1) / R.G12);
@@ -484,9 +483,8 @@ S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads_out, int32_t* ctas_per
     for (auto* h : b->runs) maxTg = std::max(maxTg, h->d.Tg);
     double best = 1e300;
     int bt = 0, bc = 0;
-    const int tmax = b->prec == S2D_FP64 ? FftCta<double>::max_threads : FftCta<float>::max_threads;
     for (int threads : {128, 256, 512}) {
-        if (threads < maxTg || threads > tmax) continue;
+        if (threads < maxTg) continue;
         for (int cps = 1; cps <= 4; ++cps) {
             if (configure_any(b, threads, cps) != S2D_OK) continue;
             if (b->ctas_per_sm != cps) continue;   // occupancy cap reached

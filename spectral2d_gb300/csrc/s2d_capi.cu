@@ -96,7 +96,7 @@ std::vector<TwEnt<T>> fma_tables(Dims* d) {
     for (int p = 0; p < d->npass; ++p) {
         const int R = d->radix[p];
         d->twoff[p] = -1;
-        if (p > 0 && (R == 4 || R == 2) && d->E == kElemsPerThread) {
+        if (p > 0 && (R == 4 || R == 2)) {
             d->twoff[p] = (int)tab.size();
             const long long step = d->M / (Ns * R);
             for (int k = 0; k < Ns; ++k) {
@@ -119,37 +119,17 @@ std::vector<TwEnt<T>> fma_tables(Dims* d) {
     return tab;
 }
 
-// Radix plan of an M = 2^a 3^b transform.  12 elements per thread (FP64, and
-// FP32 when 48 does not divide M): passes 3..3, (2), 4..4.  48 elements per
-// thread (FP32, 48 | M): the fewest passes whose radices divide 48 -- each
-// pass takes at most four factors 2 and one factor 3, so
-// p = max(ceil(a/4), b) passes; the twos are spread evenly, the threes go
-// to the first passes together with the smallest shares of twos (the first
-// pass has no twiddles).
-bool factor_plan(int M, bool wide, Dims* d) {
+bool factor_plan(int M, Dims* d) {
     int m = M, a = 0, b = 0;
     while (m % 2 == 0) { m /= 2; ++a; }
     while (m % 3 == 0) { m /= 3; ++b; }
     if (m != 1 || M % kElemsPerThread != 0) return false;
     int np = 0;
-    if (wide && M % kElemsWide == 0) {
-        const int p = std::max((a + 3) / 4, b);
-        if (p > kMaxPasses) return false;
-        for (int i = 0; i < p; ++i) {
-            const int twos = a / p + (i >= p - a % p ? 1 : 0);   // ascending shares
-            const int three = i < b ? 3 : 1;
-            d->radix[np++] = three << twos;
-        }
-        d->E = kElemsWide;
-    } else {
-        for (int i = 0; i < b; ++i) d->radix[np++] = 3;
-        if (a % 2) d->radix[np++] = 2;
-        for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
-        if (np > kMaxPasses) return false;
-        d->E = kElemsPerThread;
-    }
+    for (int i = 0; i < b; ++i) d->radix[np++] = 3;
+    if (a % 2) d->radix[np++] = 2;
+    for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
+    if (np > kMaxPasses) return false;
     d->npass = np;
-    d->Tg = M / d->E;
     return true;
 }
 
@@ -174,14 +154,13 @@ int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_gro
     if (bytes_per_group > (size_t)h->max_smem)
         return fail(S2D_ERR_UNSUPPORTED, "%s: %zu bytes of shared memory per transform exceed %d", what,
                     bytes_per_group, h->max_smem);
-    const int tmax = h->prec == S2D_FP64 ? FftCta<double>::max_threads : FftCta<float>::max_threads;
-    if (threads_per_group > tmax)
-        return fail(S2D_ERR_UNSUPPORTED, "%s: %d threads per transform exceed %d", what, threads_per_group, tmax);
+    if (threads_per_group > 512)
+        return fail(S2D_ERR_UNSUPPORTED, "%s: %d threads per transform exceed 512", what, threads_per_group);
     const int gmax = std::max(1, target_threads / threads_per_group);
     const int gmin = std::max(1, (32 + threads_per_group - 1) / threads_per_group);
     const long gfill = (items + 2L * h->sms - 1) / (2L * h->sms);
     int G = (int)std::max<long>(gmin, std::min<long>(gmax, gfill));
-    while (G > 1 && (G * threads_per_group > tmax || G * bytes_per_group > cap_pair)) --G;
+    while (G > 1 && (G * threads_per_group > 512 || G * bytes_per_group > cap_pair)) --G;
     L->G = G;
     L->threads = G * threads_per_group;
     L->smem = G * bytes_per_group;
@@ -382,10 +361,11 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     d.M = h->grid.nxG;
     d.ldS = d.KY + 1;                  // even pitch: 16-byte aligned FP32 columns
     d.ldI = (d.KX + 3) / 4 * 4;
-    if (!factor_plan(d.M, h->prec == S2D_FP32, &d)) {
+    if (!factor_plan(d.M, &d)) {
         delete h;
         return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", d.M);
     }
+    d.Tg = d.M / kElemsPerThread;
     h->ph.nu = cfg->nu;
     h->ph.alpha = cfg->alpha;
     h->ph.form = cfg->nonlinear_form;
@@ -479,11 +459,10 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess)
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
-    // launch shapes: about 256 threads per CTA (128 for the FP32 48-element
-    // threads, ~170 registers each) so that at least two CTAs share an SM and
-    // one CTA's barrier phases overlap the other's arithmetic
+    // launch shapes: about 256 threads per CTA so that at least two CTAs
+    // share an SM and one CTA's barrier phases overlap the other's FP64 work
     const size_t tb = (size_t)d.M * h->vsz;
-    const int tgt = d.E == kElemsWide ? 128 : 256;
+    const int tgt = 256;
     int rr;
     const int nf = h->ph.form == S2D_NL_BASDEVANT ? 2 : 3;
     if ((rr = pick_launch(h, d.Tg, tb, tgt, (long)nf * d.KX, &h->L_yinv, "inverse y-pass")) != S2D_OK)

@@ -391,7 +391,7 @@ __global__ void k_pi_finish(Dims dl, const double2* __restrict__ w, const double
 // Physical rows of two spectral fields X, Y (half-spectral rows, Y may be
 // null): one inverse FFT of X + iY per row, real part -> ox, imaginary -> oy.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xinv_phys2(Dims d, const typename Vec<T>::t* __restrict__ X,
+__global__ void __launch_bounds__(512) k_xinv_phys2(Dims d, const typename Vec<T>::t* __restrict__ X,
                                                     const typename Vec<T>::t* __restrict__ Y,
                                                     const typename Vec<T>::t* __restrict__ tw, int G, T* ox, T* oy) {
     using VT = typename Vec<T>::t;
@@ -462,7 +462,7 @@ __device__ __forceinline__ double ordered_sum(const double* __restrict__ part, i
 
 // K1 of (w, psi): inverse y-pass of every run's state.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_yinv(Dims d, const LesRun<T>* __restrict__ runs,
+__global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __restrict__ runs,
                                                   const double* __restrict__ rk2,
                                                   const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_yinv(Dims d, const
 // Physical rows of w and psi (one inverse FFT of W + i PSI per row) and the
 // tile's sum of w^2 (fixed order: per thread, then warps in order).
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
+__global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
                                                   const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -536,7 +536,7 @@ __global__ void k_cl_pack(const LesRun<T>* __restrict__ runs, int nparts, long H
 // Network output -> -Pi on the grid (scale a^2 y, scale = -s2), forward x-FFT
 // of row pairs into the half-spectral rows I2.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_xfwd(Dims d, const LesRun<T>* __restrict__ runs, int nparts,
+__global__ void __launch_bounds__(512) k_cl_xfwd(Dims d, const LesRun<T>* __restrict__ runs, int nparts,
                                                   const float* __restrict__ Y, double scale,
                                                   const typename Vec<T>::t* __restrict__ tw, int G, T xscale) {
     using VT = typename Vec<T>::t;
@@ -565,7 +565,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_xfwd(Dims d, const
 // Forward y-FFT of the columns of I2 with Truncate into src; modes with
 // |k|^2 < kmin2 (the closure's band) are zero.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_cl_ystore(Dims d, const LesRun<T>* __restrict__ runs,
+__global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __restrict__ runs,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     double kmin2) {
     using VT = typename Vec<T>::t;

@@ -21,19 +21,7 @@
 namespace s2d {
 
 constexpr int kMaxPasses = 16;
-constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass (FP64)
-constexpr int kElemsWide = 48;        // FP32 when 48 | M: radices up to 48 in registers
-
-// Largest CTA of the FFT kernels: FP32 threads hold 48 complex elements and
-// need the registers of a 256-thread CTA.
-template <typename T>
-struct FftCta {
-    static constexpr int max_threads = 512;
-};
-template <>
-struct FftCta<float> {
-    static constexpr int max_threads = 256;
-};
+constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
 
 // Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
 // w_r = i^q_r * c_r * (1 + i t_r) with |t_r| <= 1, so that x*w_r costs two
@@ -56,8 +44,7 @@ struct Dims {
     int M;      // padded grid points per direction (3/2 rule)
     int ldS;    // compact column pitch (elements)
     int ldI;    // half-spectral row pitch (elements)
-    int Tg;     // threads per transform = M / E
-    int E;      // elements per thread: kElemsPerThread, or kElemsWide (FP32)
+    int Tg;     // threads per transform = M / kElemsPerThread
     int npass;  // FFT passes
     int radix[kMaxPasses];
     // per pass: offset (entries) of its TwEnt block, -1 if the pass uses the

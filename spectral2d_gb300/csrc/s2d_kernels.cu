@@ -33,7 +33,7 @@ namespace s2d {
 // K1, K2, K3 of one simulation: one tile per CTA (bodies in s2d_step.cuh).
 // ------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
+__global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
                                                const double* __restrict__ rk2, FieldSet fs,
                                                const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -42,7 +42,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_yinv(Dims d, const ty
 }
 
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+__global__ void __launch_bounds__(512) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
     using VT = typename Vec<T>::t;
@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_xpass_bas(Dims d, typ
 }
 
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_yfwd_rk3(Dims d, const typename Vec<T>::t* __restrict__ Iu,
+__global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>::t* __restrict__ Iu,
                                                    const typename Vec<T>::t* __restrict__ Iv,
                                                    typename Vec<T>::t* S0, typename Vec<T>::t* S1,
                                                    typename Vec<T>::t* Sdw,
@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_yfwd_rk3(Dims d, cons
 // normalised half spectra of u*w / v*w.
 // ------------------------------------------------------------------------
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xpass_rhs(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+__global__ void __launch_bounds__(512) k_xpass_rhs(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
                                                     const typename Vec<T>::t* __restrict__ Iw,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
@@ -270,7 +270,7 @@ __global__ void k_minmax(Dims d, const typename Vec<T>::t* __restrict__ S, unsig
 // Physical u, v of each row (one complex inverse FFT of u + i v), then
 // max(|u|/dx + |v|/dy) with dx = dy = 2 pi / M.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xinv_cfl(Dims d, const typename Vec<T>::t* __restrict__ Iu,
+__global__ void __launch_bounds__(512) k_xinv_cfl(Dims d, const typename Vec<T>::t* __restrict__ Iu,
                                                    const typename Vec<T>::t* __restrict__ Iv,
                                                    const typename Vec<T>::t* __restrict__ tw, int G,
                                                    unsigned long long* maxbits) {
@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_xinv_cfl(Dims d, cons
 // part) of one inverse FFT per row: out[row] = (sum a b^2, sum a^2, sum b^2)
 // (src/Analysis.F90:157-163, :203-209), summed over rows later in order.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xinv_moments(Dims d, const typename Vec<T>::t* __restrict__ Ia,
+__global__ void __launch_bounds__(512) k_xinv_moments(Dims d, const typename Vec<T>::t* __restrict__ Ia,
                                                       const typename Vec<T>::t* __restrict__ Ib,
                                                       const typename Vec<T>::t* __restrict__ tw, int G,
                                                       double* out) {
@@ -366,7 +366,7 @@ __global__ void k_fill_tg(Dims d, const double* __restrict__ sx, const double* _
 // Forward x-transform of physical rows (pitch M) in pairs: one complex FFT
 // of r1 + i r2, split into two normalised half spectra (kx in [0,K]).
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_xfwd_phys(Dims d, const T* __restrict__ phys,
+__global__ void __launch_bounds__(512) k_xfwd_phys(Dims d, const T* __restrict__ phys,
                                                     typename Vec<T>::t* Iout,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(FftCta<T>::max_threads)k_xfwd_phys(Dims d, con
 // Forward y-transform of half-spectral columns into the compact state, with
 // Truncate.
 template <typename T>
-__global__ void __launch_bounds__(FftCta<T>::max_threads)k_yfwd_store(Dims d, const typename Vec<T>::t* __restrict__ I,
+__global__ void __launch_bounds__(512) k_yfwd_store(Dims d, const typename Vec<T>::t* __restrict__ I,
                                                      typename Vec<T>::t* S,
                                                      const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
