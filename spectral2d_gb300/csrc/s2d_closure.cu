@@ -77,98 +77,110 @@ __device__ __forceinline__ long nbr(long p, int dy, int dx, int H, int Wd) {
     return b * HW + (long)y * Wd + x;
 }
 
-// Implicit-GEMM convolution on the tensor cores.  A warp owns kConvGroups
-// groups of 16 consecutive pixels x NC channels; the K loop runs over 9 taps x
-// KC/16 chunks of 16 channels, and each chunk's weight fragments are loaded
-// once and used for all of the warp's pixel groups.
+// Implicit-GEMM convolution on the tensor cores, tiled in shared memory.
+// A CTA (8 warps) owns a tile of kTileY x kTileX pixels of one image; it
+// stages the tile with its one-pixel circular halo and the layer's weights in
+// shared memory once, and each warp computes two tile rows (four groups of 16
+// pixels) x NC channels with mma.sync m16n8k16 (BF16 in, FP32 accumulate):
+// the K loop runs over 9 taps x KC/16 chunks of 16 channels, and each chunk's
+// weight fragments serve all four pixel groups.  Per-pixel channel rows are
+// padded to KC+8 elements so that the fragment loads hit 32 distinct banks.
 //   FWD (SIGN = +1): out[p, n] = sum_{t,k} in[p + off_t, k] W[n, t, k]
 //   data gradient (SIGN = -1): out[q, n] = sum_{t,k} in[q - off_t, k] W^T[n, t, k]
 // Epilogue EPI: 0 = + bias, store z and gelu(z) (BF16); 1 = + bias, store
 // channel 0 as FP32; 2 = multiply by gelu'(zprev), store BF16.
-constexpr int kConvGroups = 4;
-constexpr int kConvPixelsPerCta = 8 * 16 * kConvGroups;   // 8 warps
+constexpr int kTileX = 32;
+constexpr int kTileY = 16;
+
+template <int KC, int NC>
+constexpr size_t conv_smem_bytes() {
+    return ((size_t)(kTileY + 2) * (kTileX + 2) * (KC + 8) + (size_t)NC * 9 * (KC + 8)) * 2;
+}
 
 template <int KC, int NC, int SIGN, int EPI>
-__global__ void __launch_bounds__(256, 2) k_conv_mma(const __nv_bfloat16* __restrict__ in,
+__global__ void __launch_bounds__(256) k_conv_mma(const __nv_bfloat16* __restrict__ in,
                                                   const __nv_bfloat16* __restrict__ W,
                                                   const float* __restrict__ bias,
                                                   const __nv_bfloat16* __restrict__ zprev, __nv_bfloat16* z,
-                                                  __nv_bfloat16* a, float* yout, long P, int H, int Wd) {
-    constexpr int PG = kConvGroups;
+                                                  __nv_bfloat16* a, float* yout, int H, int Wd) {
+    constexpr int KP = KC + 8;                 // padded channel stride (elements)
+    constexpr int HX = kTileX + 2, HY = kTileY + 2;
+    constexpr int NT = NC / 8;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __nv_bfloat16* halo = reinterpret_cast<__nv_bfloat16*>(smem_raw);   // [HY][HX][KP]
+    __nv_bfloat16* ws = halo + HY * HX * KP;                              // [NC][9][KP]
+    const int tiles_x = (Wd + kTileX - 1) / kTileX;
+    const int tx0 = (blockIdx.x % tiles_x) * kTileX;
+    const int ty0 = (blockIdx.x / tiles_x) * kTileY;
+    const long img = (long)blockIdx.y * H * Wd;
+
+    // stage the halo tile (16-byte pieces of 8 channels) and the weights
+    constexpr int PCS = KC / 8;
+    for (int i = threadIdx.x; i < HY * HX * PCS; i += blockDim.x) {
+        const int pc = i % PCS;
+        const int pix = i / PCS;
+        const int hy = pix / HX, hx = pix - (pix / HX) * HX;
+        int yy = ty0 + hy - 1, xx = tx0 + hx - 1;
+        yy = ((yy % H) + H) % H;
+        xx = ((xx % Wd) + Wd) % Wd;
+        const uint4 v = *reinterpret_cast<const uint4*>(in + (img + (long)yy * Wd + xx) * KC + pc * 8);
+        *reinterpret_cast<uint4*>(halo + (hy * HX + hx) * KP + pc * 8) = v;
+    }
+    for (int i = threadIdx.x; i < NC * 9 * PCS; i += blockDim.x) {
+        const int pc = i % PCS;
+        const int row = i / PCS;   // n * 9 + t
+        *reinterpret_cast<uint4*>(ws + row * KP + pc * 8) =
+            *reinterpret_cast<const uint4*>(W + (long)row * KC + pc * 8);
+    }
+    __syncthreads();
+
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int g = lane >> 2, tg = lane & 3;
-    const long pw = ((long)blockIdx.x * 8 + warp) * (16 * PG);
-    if (pw >= P) return;
-    const int HW = H * Wd;   // P * 32 < 2^31 (checked at s2d_cnn_create)
-    // rows g and g+8 of each group: image base, y, x (y < 0: past the end)
-    int base[PG][2], py[PG][2], px[PG][2];
+    // warp rows: tile rows 2 warp, 2 warp + 1; groups q = (row, x half)
+    float acc[4][NT][4];
 #pragma unroll
-    for (int q = 0; q < PG; ++q)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const long p = pw + q * 16 + g + 8 * h;
-            if (p < P) {
-                const int pi = (int)p;
-                const int b = pi / HW;
-                const int rem = pi - b * HW;
-                base[q][h] = b * HW;
-                py[q][h] = rem / Wd;
-                px[q][h] = rem - py[q][h] * Wd;
-            } else {
-                base[q][h] = 0;
-                py[q][h] = -1;
-                px[q][h] = 0;
-            }
-        }
-    constexpr int NT = NC / 8;
-    float acc[PG][NT][4];
-#pragma unroll
-    for (int q = 0; q < PG; ++q)
+    for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int i = 0; i < NT; ++i) acc[q][i][0] = acc[q][i][1] = acc[q][i][2] = acc[q][i][3] = 0.f;
 #pragma unroll 1
     for (int t = 0; t < 9; ++t) {
         const int dy = SIGN * (t / 3 - 1), dx = SIGN * (t % 3 - 1);
-        int off[PG][2];   // element offset of the neighbour pixel's channels, -1 past the end
-#pragma unroll
-        for (int q = 0; q < PG; ++q)
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                int yy = py[q][h] + dy, xx = px[q][h] + dx;
-                yy += (yy < 0) ? H : ((yy >= H) ? -H : 0);
-                xx += (xx < 0) ? Wd : ((xx >= Wd) ? -Wd : 0);
-                off[q][h] = py[q][h] < 0 ? -1 : (base[q][h] + yy * Wd + xx) * KC;
-            }
 #pragma unroll
         for (int c = 0; c < KC; c += 16) {
             uint32_t bw[NT][2];
 #pragma unroll
             for (int nt = 0; nt < NT; ++nt) {
-                const __nv_bfloat16* wr = W + ((long)(nt * 8 + g) * 9 + t) * KC + c;
-                bw[nt][0] = ld32(wr + tg * 2);
-                bw[nt][1] = ld32(wr + tg * 2 + 8);
+                const __nv_bfloat16* wr = ws + ((nt * 8 + g) * 9 + t) * KP + c + tg * 2;
+                bw[nt][0] = *reinterpret_cast<const uint32_t*>(wr);
+                bw[nt][1] = *reinterpret_cast<const uint32_t*>(wr + 8);
             }
 #pragma unroll
-            for (int q = 0; q < PG; ++q) {
-                const int oA = off[q][0], oB = off[q][1];
-                const uint32_t a0 = oA >= 0 ? ld32(in + oA + c + tg * 2) : 0u;
-                const uint32_t a1 = oB >= 0 ? ld32(in + oB + c + tg * 2) : 0u;
-                const uint32_t a2 = oA >= 0 ? ld32(in + oA + c + tg * 2 + 8) : 0u;
-                const uint32_t a3 = oB >= 0 ? ld32(in + oB + c + tg * 2 + 8) : 0u;
+            for (int q = 0; q < 4; ++q) {
+                const int hy = 2 * warp + (q >> 1) + 1 + dy;
+                const int hx = (q & 1) * 16 + g + 1 + dx;
+                const __nv_bfloat16* rA = halo + (hy * HX + hx) * KP + c + tg * 2;
+                const __nv_bfloat16* rB = rA + 8 * KP;
+                const uint32_t a0 = *reinterpret_cast<const uint32_t*>(rA);
+                const uint32_t a1 = *reinterpret_cast<const uint32_t*>(rB);
+                const uint32_t a2 = *reinterpret_cast<const uint32_t*>(rA + 8);
+                const uint32_t a3 = *reinterpret_cast<const uint32_t*>(rB + 8);
 #pragma unroll
                 for (int nt = 0; nt < NT; ++nt) mma_bf16(acc[q][nt], a0, a1, a2, a3, bw[nt][0], bw[nt][1]);
             }
         }
     }
 #pragma unroll
-    for (int q = 0; q < PG; ++q)
+    for (int q = 0; q < 4; ++q) {
+        const int y = ty0 + 2 * warp + (q >> 1);
+        if (y >= H) continue;
 #pragma unroll
         for (int nt = 0; nt < NT; ++nt) {
             const int n0 = nt * 8 + tg * 2;
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
-                if (py[q][h] < 0) continue;
-                const long p = pw + q * 16 + g + 8 * h;
+                const int x = tx0 + (q & 1) * 16 + g + 8 * h;
+                if (x >= Wd) continue;
+                const long p = img + (long)y * Wd + x;
                 float v0 = acc[q][nt][2 * h], v1 = acc[q][nt][2 * h + 1];
                 if (EPI == 0) {
                     v0 += bias[n0];
@@ -184,6 +196,18 @@ __global__ void __launch_bounds__(256, 2) k_conv_mma(const __nv_bfloat16* __rest
                 }
             }
         }
+    }
+}
+
+// Launch k_conv_mma over B images of H x Wd.
+template <int KC, int NC, int SIGN, int EPI>
+cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
+                        const __nv_bfloat16* zprev, __nv_bfloat16* z, __nv_bfloat16* a, float* yout, int B, int H,
+                        int Wd, cudaStream_t st) {
+    const dim3 grid(((Wd + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY), B);
+    k_conv_mma<KC, NC, SIGN, EPI><<<grid, 256, conv_smem_bytes<KC, NC>(), st>>>(in, W, bias, zprev, z, a, yout, H,
+                                                                               Wd);
+    return cudaGetLastError();
 }
 
 // Weight and bias gradient of one layer on the FP32 pipes:
@@ -676,25 +700,21 @@ int refresh_all(s2d_cnn* c) {
 
 // forward of the batch in X0 (B images)
 int forward(s2d_cnn* c, int B) {
-    const long P = (long)B * c->H * c->Wd;
-    const int grid = (int)((P + kConvPixelsPerCta - 1) / kConvPixelsPerCta);
     const float* bias[kLayers];
     for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
-    k_conv_mma<16, 32, 1, 0><<<grid, 256, 0, c->stream>>>(c->X0, c->Wb[0], bias[0], nullptr, c->Z[0], c->A[0],
-                                                           nullptr, P, c->H, c->Wd);
+    C_CUDA((launch_conv<16, 32, 1, 0>(c->X0, c->Wb[0], bias[0], nullptr, c->Z[0], c->A[0], nullptr, B, c->H,
+                                      c->Wd, c->stream)));
     for (int l = 1; l < kLayers - 1; ++l)
-        k_conv_mma<32, 32, 1, 0><<<grid, 256, 0, c->stream>>>(c->A[l - 1], c->Wb[l], bias[l], nullptr, c->Z[l],
-                                                               c->A[l], nullptr, P, c->H, c->Wd);
-    k_conv_mma<32, 16, 1, 1><<<grid, 256, 0, c->stream>>>(c->A[kLayers - 2], c->Wb[kLayers - 1], bias[kLayers - 1],
-                                                           nullptr, nullptr, nullptr, c->Y, P, c->H, c->Wd);
-    C_CUDA(cudaGetLastError());
+        C_CUDA((launch_conv<32, 32, 1, 0>(c->A[l - 1], c->Wb[l], bias[l], nullptr, c->Z[l], c->A[l], nullptr, B,
+                                          c->H, c->Wd, c->stream)));
+    C_CUDA((launch_conv<32, 16, 1, 1>(c->A[kLayers - 2], c->Wb[kLayers - 1], bias[kLayers - 1], nullptr, nullptr,
+                                      nullptr, c->Y, B, c->H, c->Wd, c->stream)));
     return S2D_OK;
 }
 
 // loss of the batch (targets in tgt) and, with grads, the full backward pass
 int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
     const long P = (long)B * c->H * c->Wd;
-    const int grid = (int)((P + kConvPixelsPerCta - 1) / kConvPixelsPerCta);
     const int lb = 256;
     k_mse<<<lb, 256, 0, c->stream>>>(c->Y, c->tgt, P, 1.0f / (float)P, c->dZ6, 16, c->lpart);
     C_CUDA(cudaGetLastError());
@@ -720,12 +740,11 @@ int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
             if (l > 0) {
                 __nv_bfloat16* out = bufs[l & 1];
                 if (CO == 16)
-                    k_conv_mma<16, 32, -1, 2><<<grid, 256, 0, c->stream>>>(dz, c->WTb[l], nullptr, c->Z[l - 1], out,
-                                                                            nullptr, nullptr, P, c->H, c->Wd);
+                    C_CUDA((launch_conv<16, 32, -1, 2>(dz, c->WTb[l], nullptr, c->Z[l - 1], out, nullptr, nullptr,
+                                                       B, c->H, c->Wd, c->stream)));
                 else
-                    k_conv_mma<32, 32, -1, 2><<<grid, 256, 0, c->stream>>>(dz, c->WTb[l], nullptr, c->Z[l - 1], out,
-                                                                            nullptr, nullptr, P, c->H, c->Wd);
-                C_CUDA(cudaGetLastError());
+                    C_CUDA((launch_conv<32, 32, -1, 2>(dz, c->WTb[l], nullptr, c->Z[l - 1], out, nullptr, nullptr,
+                                                       B, c->H, c->Wd, c->stream)));
                 dz = out;
             }
         }
@@ -980,6 +999,20 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
     if (cudaSetDevice(device) != cudaSuccess) return bail(cerr(S2D_ERR_CUDA, "cudaSetDevice failed"));
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(cerr(S2D_ERR_CUDA, "stream creation failed"));
+    {
+        static bool attr[64] = {false};
+        if (device >= 0 && device < 64 && !attr[device]) {
+            const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
+            const bool set =
+                cudaFuncSetAttribute(k_conv_mma<16, 32, 1, 0>, A, (int)conv_smem_bytes<16, 32>()) == cudaSuccess &&
+                cudaFuncSetAttribute(k_conv_mma<32, 32, 1, 0>, A, (int)conv_smem_bytes<32, 32>()) == cudaSuccess &&
+                cudaFuncSetAttribute(k_conv_mma<32, 16, 1, 1>, A, (int)conv_smem_bytes<32, 16>()) == cudaSuccess &&
+                cudaFuncSetAttribute(k_conv_mma<16, 32, -1, 2>, A, (int)conv_smem_bytes<16, 32>()) == cudaSuccess &&
+                cudaFuncSetAttribute(k_conv_mma<32, 32, -1, 2>, A, (int)conv_smem_bytes<32, 32>()) == cudaSuccess;
+            if (!set) return bail(cerr(S2D_ERR_CUDA, "cudaFuncSetAttribute failed"));
+            attr[device] = true;
+        }
+    }
     long off = 0;
     for (int l = 0; l < kLayers; ++l) {
         c->poff[l] = off;
