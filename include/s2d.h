@@ -253,6 +253,12 @@ S2D_API int s2d_batch_synchronize(s2d_batch* b);
  * i.e. transforms per tile, and 1-4 CTAs per SM) on this ensemble, keeps the
  * fastest and restores every run's state.  Any output may be NULL. */
 S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm, double* ms_per_step);
+/* Fault injection for tests, made on the host: the x-pass tiles of run
+ * `run` wait for an inverse y-pass tile that does not exist, so every step
+ * takes about one bounded wait (~1 s) per stage and s2d_batch_status then
+ * reports S2D_ERR_TIMEOUT; that run's state is not advanced correctly, the
+ * others are.  run = -1 removes the stall. */
+S2D_API int s2d_batch_inject_stall(s2d_batch* b, int32_t run);
 
 /* ---- learned subgrid closure for coarse LES (no reference counterpart) -- *
  * Sharp spectral filter of a DNS state to an LES grid (a Truncate-style mask

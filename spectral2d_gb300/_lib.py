@@ -98,6 +98,7 @@ SIGNATURES = {
     "s2d_batch_status": (C.c_int, [C.c_void_p]),
     "s2d_batch_synchronize": (C.c_int, [C.c_void_p]),
     "s2d_batch_tune": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32), _dp]),
+    "s2d_batch_inject_stall": (C.c_int, [C.c_void_p, C.c_int32]),
     "s2d_cnn_create": (C.c_int, [C.c_int32, C.c_int32, C.c_uint64, C.c_int32, C.POINTER(C.c_void_p)]),
     "s2d_cnn_destroy": (None, [C.c_void_p]),
     "s2d_cnn_num_params": (C.c_int, [C.c_void_p]),

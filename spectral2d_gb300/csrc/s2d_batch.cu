@@ -168,6 +168,7 @@ struct s2d_batch {
     cudaGraphExec_t gexec = nullptr;
     s2d_cnn* cnn = nullptr;   // closure network of every run (LES batches)
     void* cl_tab = nullptr;   // its device table (closure_table)
+    int stall_run = -1;       // s2d_batch_inject_stall
 };
 
 namespace {
@@ -236,6 +237,10 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
         smem = std::max(smem, (size_t)2 * R.G3 * h->d.M * sizeof(VT));
         for (int p = 0; p < 3; ++p)
             for (int k = 0; k < R.ntask[p]; ++k) tasks[p].push_back(make_int4(i, p, k, 0));
+        // injected stall: the x-pass tiles of this run wait for one more
+        // inverse y-pass tile than the table holds, so their bounded waits
+        // run out (S2D_ERR_TIMEOUT) -- a host-made fault for tests
+        if (i == b->stall_run) R.ntask[0] += 1;
     }
     if (smem > (size_t)b->max_smem) return berr(S2D_ERR_UNSUPPORTED, "tile needs too much shared memory");
     std::vector<int4> all;
@@ -387,6 +392,14 @@ S2D_API int s2d_batch_set_dt(s2d_batch* b, const double* dt) {
     }
     B_CUDA(cudaSetDevice(b->device));
     return upload_dt(b);
+}
+
+S2D_API int s2d_batch_inject_stall(s2d_batch* b, int32_t run) {
+    if (!b || run < -1 || run >= b->n) return berr(S2D_ERR_INVALID, "bad run index");
+    B_CUDA(cudaSetDevice(b->device));
+    B_CUDA(cudaStreamSynchronize(b->stream));
+    b->stall_run = run;
+    return configure_any(b, b->threads, b->ctas_per_sm);
 }
 
 S2D_API int s2d_batch_set_closure(s2d_batch* b, s2d_cnn* c) {

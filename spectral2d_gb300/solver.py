@@ -314,6 +314,11 @@ class Ensemble:
     def synchronize(self) -> None:
         L.check(self._L.s2d_batch_synchronize(self._b))
 
+    def inject_stall(self, run: int) -> None:
+        """Host-made fault for tests: run's x-pass tiles wait for a tile that
+        does not exist until their bounded waits run out (run = -1 clears)."""
+        L.check(self._L.s2d_batch_inject_stall(self._b, run))
+
     def set_closure(self, net: "ClosureNet | None") -> None:
         """One closure network for every run (all on its grid): each step
         starts with one network forward over the whole batch."""

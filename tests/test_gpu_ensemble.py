@@ -109,3 +109,37 @@ def test_uneven_ensemble_of_the_ensemble_workload_shape(mods):
             s.set_state(w0[i])
             s.integrate_steps(4, dts[i])
             assert O.rel_l2(wb[i], s.get_state()[0]) <= 1e-15
+
+
+def test_bounded_wait_times_out_and_the_context_stays_usable(mods):
+    """Failure detection without a GPU fault: run 1's x-pass tiles are made
+    to wait for a tile that never comes (injected on the host); each wait
+    gives up after its iteration limit, the step ends, the status is
+    S2D_ERR_TIMEOUT, and once the stall is removed the batch steps normally
+    and the untouched run is exactly the single-run result."""
+    import time
+    from spectral2d_gb300 import S2DError
+    Ensemble, Spectral2D = mods
+    nxs, nus, seeds = [32, 16], [2e-3, 2e-3], [21, 22]
+    with Ensemble(nxs, nus) as ens:
+        dts = _setup(ens, nxs, seeds)
+        w0 = ens.runs[0].get_state()[0]
+        ens.inject_stall(1)
+        t0 = time.perf_counter()
+        ens.integrate_steps(1)
+        with pytest.raises(S2DError) as ei:
+            ens.status()
+        waited = time.perf_counter() - t0
+        assert ei.value.code == -4   # S2D_ERR_TIMEOUT
+        assert 0.2 < waited < 60.0
+        w1 = ens.runs[0].get_state()[0]
+        ens.inject_stall(-1)
+        ens.integrate_steps(2)
+        ens.status()
+        w3 = ens.runs[0].get_state()[0]
+    with Spectral2D(32, nu=2e-3) as s:
+        s.set_state(w0)
+        s.integrate_steps(1, dts[0])
+        assert np.array_equal(s.get_state()[0], w1)
+        s.integrate_steps(2, dts[0])
+        assert np.array_equal(s.get_state()[0], w3)
