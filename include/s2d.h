@@ -299,6 +299,10 @@ S2D_API int s2d_cnn_dataset_stats(s2d_cnn* c, double* rms3);
 S2D_API int s2d_cnn_train_epoch(s2d_cnn* c, int32_t first, int32_t count, int32_t batch, double lr,
                                 uint64_t seed, double* mean_loss);
 S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_loss);
+/* S2D_ERR_TIMEOUT if a tensor-core completion wait of the network's kernels
+ * gave up since the last call (the forward/gradient/train/eval calls check
+ * this themselves; LES runs call it after their steps); clears the flag. */
+S2D_API int s2d_cnn_status(s2d_cnn* c);
 /* les state := sharp-filtered dns state */
 S2D_API int s2d_filter_state(s2d_handle* dns, s2d_handle* les);
 /* les state := filtered dns state, and the subgrid flux of the DNS state on

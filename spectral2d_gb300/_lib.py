@@ -117,6 +117,7 @@ SIGNATURES = {
     "s2d_cnn_train_epoch": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64,
                                       _dp]),
     "s2d_cnn_eval": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, _dp]),
+    "s2d_cnn_status": (C.c_int, [C.c_void_p]),
     "s2d_filter_state": (C.c_int, [C.c_void_p, C.c_void_p]),
     "s2d_subgrid_flux": (C.c_int, [C.c_void_p, C.c_void_p, _dp]),
     "s2d_les_set_closure": (C.c_int, [C.c_void_p, C.c_void_p]),
