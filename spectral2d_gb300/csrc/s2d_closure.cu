@@ -217,10 +217,14 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
             int yy = ty0 + hr - 1, xx = tx0 + c + d - 1;
             yy = ((yy % H) + H) % H;
             xx = ((xx % Wd) + Wd) % Wd;
-            const uint4 v = *reinterpret_cast<const uint4*>(in + (img + (long)yy * Wd + xx) * KC + kg * 8);
             const int off = d * TL::COPY + ((hr * 2 + c / 8) * KG + kg) * TL::CORE + (c % 8) * 16;
-            *reinterpret_cast<uint4*>(acp + off) = v;
+            // 16-byte asynchronous copy: all of a thread's copies are in flight at once
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(acp + off)),
+                         "l"(in + (img + (long)yy * Wd + xx) * KC + kg * 8)
+                         : "memory");
         }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
         // make the staged operands visible to the tensor core (async proxy)
         asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
