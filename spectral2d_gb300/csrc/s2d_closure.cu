@@ -214,9 +214,14 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
             r /= 2;
             const int hr = r % TL::HR;
             const int d = r / TL::HR;
+            // yy in [-1, H + 8], xx in [-1, Wd + 16): at most two wraps (grid >= 8)
             int yy = ty0 + hr - 1, xx = tx0 + c + d - 1;
-            yy = ((yy % H) + H) % H;
-            xx = ((xx % Wd) + Wd) % Wd;
+            yy += yy < 0 ? H : 0;
+            yy -= yy >= H ? H : 0;
+            yy -= yy >= H ? H : 0;
+            xx += xx < 0 ? Wd : 0;
+            xx -= xx >= Wd ? Wd : 0;
+            xx -= xx >= Wd ? Wd : 0;
             const int off = d * TL::COPY + ((hr * 2 + c / 8) * KG + kg) * TL::CORE + (c % 8) * 16;
             // 16-byte asynchronous copy: all of a thread's copies are in flight at once
             asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(acp + off)),
