@@ -259,10 +259,13 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
             asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
                          : "memory");
         }
-        // every thread waits for this tile's MMAs (bounded)
-        bool done = false;
-        for (int it = 0; it < kMbarSpinLimit && !done; ++it) done = mbar_try_wait(bar, phase);
-        if (!done) s_ok = 0;
+        // one thread polls for this tile's MMAs (bounded); the others wait at
+        // the barrier without taking issue slots from the SM's other CTAs
+        if (tid == 0) {
+            bool done = false;
+            for (int it = 0; it < kMbarSpinLimit && !done; ++it) done = mbar_try_wait(bar, phase);
+            if (!done) s_ok = 0;
+        }
         __syncthreads();
         if (!s_ok) break;
         phase ^= 1u;
