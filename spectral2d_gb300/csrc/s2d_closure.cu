@@ -13,9 +13,9 @@
 // channels, GELU (erf) after the first five; activations and working weights
 // in BF16, accumulation FP32, FP32 master weights, Adam.  Convolutions are
 // implicit GEMMs (pixels x out-channels x 9*in-channels): the forward pass and
-// the data gradient on the tensor cores with mma.sync m16n8k16 BF16->FP32,
-// the weight gradient on the FP32 pipes with a deterministic two-stage
-// reduction over pixels.  Channel counts are padded to multiples of 16
+// the data gradient on the tcgen05 tensor cores (BF16 operands from shared
+// memory, FP32 accumulator in tensor memory), the weight gradient on the FP32
+// pipes with a deterministic two-stage reduction over pixels.  Channel counts are padded to multiples of 16
 // (input 2 -> 16, output 1 -> 16) with zero weights.
 //
 // LES with closure: each step the network maps (w, psi) of the LES state to
@@ -53,28 +53,6 @@ __device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
 __device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
 __device__ __forceinline__ float gelu_grad_f(float x) {
     return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
-}
-
-__device__ __forceinline__ void mma_bf16(float* c, uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
-                                         uint32_t b1) {
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// Periodic neighbour of pixel p shifted by (dy, dx).
-__device__ __forceinline__ long nbr(long p, int dy, int dx, int H, int Wd) {
-    const long HW = (long)H * Wd;
-    const long b = p / HW;
-    const int rem = (int)(p - b * HW);
-    int y = rem / Wd, x = rem - (rem / Wd) * Wd;
-    y += dy;
-    x += dx;
-    y += (y < 0) ? H : ((y >= H) ? -H : 0);
-    x += (x < 0) ? Wd : ((x >= Wd) ? -Wd : 0);
-    return b * HW + (long)y * Wd + x;
 }
 
 // ---- tcgen05 (5th-generation tensor core) helpers -----------------------
@@ -123,7 +101,8 @@ constexpr int kMbarSpinLimit = 1 << 22;
 // One thread issues the 9 * KC/16 MMAs (M=128, N=NC, K=16) and commits them
 // to an mbarrier; after a bounded wait each warp reads its 32 lanes of the
 // accumulator (tcgen05.ld) for the epilogue:
-//   EPI 0: + bias, store z and gelu(z) (BF16); 1: + bias, channel 0 as FP32;
+//   EPI 0: + bias, store z (unless z is null: no backward follows) and
+//   gelu(z) (BF16); 1: + bias, channel 0 as FP32;
 //   2: multiply by gelu'(zprev), store BF16.
 //   FWD (SIGN = +1): out[p, n] = sum_{t,k} in[p + off_t, k] W[n, t, k]
 //   data gradient (SIGN = -1): out[q, n] = sum_{t,k} in[q - off_t, k] W^T[n, t, k]
@@ -326,7 +305,8 @@ __global__ void __launch_bounds__(128) k_conv_tc(const __nv_bfloat16* __restrict
                             zz[e] = pack_bf16(v0 * gelu_grad_f(g.x), v1 * gelu_grad_f(g.y));
                         }
                     }
-                    *reinterpret_cast<uint4*>(z + p * NC + q * 8) = make_uint4(zz[0], zz[1], zz[2], zz[3]);
+                    if (EPI != 0 || z)
+                        *reinterpret_cast<uint4*>(z + p * NC + q * 8) = make_uint4(zz[0], zz[1], zz[2], zz[3]);
                     if (EPI == 0)
                         *reinterpret_cast<uint4*>(a + p * NC + q * 8) = make_uint4(aa[0], aa[1], aa[2], aa[3]);
                 }
@@ -849,15 +829,16 @@ int refresh_all(s2d_cnn* c) {
     return S2D_OK;
 }
 
-// forward of the batch in X0 (B images)
-int forward(s2d_cnn* c, int B) {
+// forward of the batch in X0 (B images); the pre-activations z are kept only
+// when a backward pass follows
+int forward(s2d_cnn* c, int B, bool keep_z) {
     const float* bias[kLayers];
     for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
-    C_CUDA((launch_conv<16, 32, 1, 0>(c->X0, c->Wb[0], bias[0], nullptr, c->Z[0], c->A[0], nullptr, B, c->H,
-                                      c->Wd, c->cflags, c->sms, c->stream)));
+    C_CUDA((launch_conv<16, 32, 1, 0>(c->X0, c->Wb[0], bias[0], nullptr, keep_z ? c->Z[0] : nullptr, c->A[0],
+                                      nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
     for (int l = 1; l < kLayers - 1; ++l)
-        C_CUDA((launch_conv<32, 32, 1, 0>(c->A[l - 1], c->Wb[l], bias[l], nullptr, c->Z[l], c->A[l], nullptr, B,
-                                          c->H, c->Wd, c->cflags, c->sms, c->stream)));
+        C_CUDA((launch_conv<32, 32, 1, 0>(c->A[l - 1], c->Wb[l], bias[l], nullptr, keep_z ? c->Z[l] : nullptr,
+                                          c->A[l], nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
     C_CUDA((launch_conv<32, 16, 1, 1>(c->A[kLayers - 2], c->Wb[kLayers - 1], bias[kLayers - 1], nullptr, nullptr,
                                       nullptr, c->Y, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
     return S2D_OK;
@@ -1074,7 +1055,7 @@ int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab,
     // the network runs on the caller's stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
     c->stream = st;
-    const int r = forward(c, n);
+    const int r = forward(c, n, false);
     c->stream = saved;
     if (r != S2D_OK) return r;
     k_cl_xfwd<T><<<dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st>>>(
@@ -1306,7 +1287,7 @@ S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t B, float* y
     C_CUDA(cudaSetDevice(c->device));
     int r = upload_host_batch(c, x, nullptr, B);
     if (r != S2D_OK) return r;
-    r = forward(c, B);
+    r = forward(c, B, false);
     if (r != S2D_OK) return r;
     const long P = (long)B * c->H * c->Wd;
     std::vector<float> out(P);
@@ -1322,7 +1303,7 @@ S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, i
     C_CUDA(cudaSetDevice(c->device));
     int r = upload_host_batch(c, x, target, B);
     if (r != S2D_OK) return r;
-    if ((r = forward(c, B)) != S2D_OK) return r;
+    if ((r = forward(c, B, true)) != S2D_OK) return r;
     if ((r = loss_backward(c, B, true, loss)) != S2D_OK) return r;
     if (grads) {
         std::vector<float> pad(c->nparam_pad);
@@ -1391,7 +1372,7 @@ S2D_API int s2d_cnn_train_epoch(s2d_cnn* c, int32_t first, int32_t count, int32_
             c->data, c->amp, c->idx, batch, HW, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]),
             (float)(1.0 / c->scale[2]), c->X0, c->tgt);
         C_CUDA(cudaGetLastError());
-        int r = forward(c, batch);
+        int r = forward(c, batch, true);
         double l = 0.0;
         if (r == S2D_OK) r = loss_backward(c, batch, true, &l);
         if (r == S2D_OK) r = adam_step(c, lr);
@@ -1419,7 +1400,7 @@ S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_
                                                                   (float)(1.0 / c->scale[0]),
                                                                   (float)(1.0 / c->scale[1]),
                                                                   (float)(1.0 / c->scale[2]), c->X0, c->tgt);
-        int r = forward(c, B);
+        int r = forward(c, B, false);
         double l = 0.0;
         if (r == S2D_OK) r = loss_backward(c, B, false, &l);
         if (r != S2D_OK) return r;
