@@ -142,5 +142,52 @@ MODULE s2d_m
          IMPORT :: C_INT, C_PTR
          TYPE(C_PTR), VALUE :: h
       END FUNCTION s2d_synchronize
+
+      ! Analysis (src/Analysis.F90:135-225): x and y vorticity-gradient skewness
+      INTEGER(C_INT) FUNCTION s2d_skewness(h, xSkew, ySkew) BIND(C, NAME='s2d_skewness')
+         IMPORT :: C_INT, C_PTR, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         REAL(C_DOUBLE), INTENT(OUT) :: xSkew, ySkew
+      END FUNCTION s2d_skewness
+
+      INTEGER(C_INT) FUNCTION s2d_enstrophy(h, enst) BIND(C, NAME='s2d_enstrophy')
+         IMPORT :: C_INT, C_PTR, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         REAL(C_DOUBLE), INTENT(OUT) :: enst
+      END FUNCTION s2d_enstrophy
+
+      ! WriteRestart (src/IO.F90:98-143): root_<num>.bin + root_<num>.xmf
+      INTEGER(C_INT) FUNCTION s2d_write_restart(h, root, num, nadv, time) BIND(C, NAME='s2d_write_restart')
+         IMPORT :: C_INT, C_PTR, C_CHAR, C_INT32_T, C_INT64_T, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         CHARACTER(KIND=C_CHAR), DIMENSION(*), INTENT(IN) :: root   ! NUL-terminated
+         INTEGER(C_INT32_T), VALUE :: num
+         INTEGER(C_INT64_T), VALUE :: nadv
+         REAL(C_DOUBLE), VALUE :: time
+      END FUNCTION s2d_write_restart
+
+      INTEGER(C_INT) FUNCTION s2d_read_restart(h, path, nadv, time) BIND(C, NAME='s2d_read_restart')
+         IMPORT :: C_INT, C_PTR, C_CHAR, C_INT64_T, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         CHARACTER(KIND=C_CHAR), DIMENSION(*), INTENT(IN) :: path
+         INTEGER(C_INT64_T), INTENT(OUT) :: nadv
+         REAL(C_DOUBLE), INTENT(OUT) :: time
+      END FUNCTION s2d_read_restart
+
+      INTEGER(C_INT) FUNCTION s2d_checkpoint_write(h, path, nadv, time) BIND(C, NAME='s2d_checkpoint_write')
+         IMPORT :: C_INT, C_PTR, C_CHAR, C_INT64_T, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         CHARACTER(KIND=C_CHAR), DIMENSION(*), INTENT(IN) :: path
+         INTEGER(C_INT64_T), VALUE :: nadv
+         REAL(C_DOUBLE), VALUE :: time
+      END FUNCTION s2d_checkpoint_write
+
+      INTEGER(C_INT) FUNCTION s2d_checkpoint_read(h, path, nadv, time) BIND(C, NAME='s2d_checkpoint_read')
+         IMPORT :: C_INT, C_PTR, C_CHAR, C_INT64_T, C_DOUBLE
+         TYPE(C_PTR), VALUE :: h
+         CHARACTER(KIND=C_CHAR), DIMENSION(*), INTENT(IN) :: path
+         INTEGER(C_INT64_T), INTENT(OUT) :: nadv
+         REAL(C_DOUBLE), INTENT(OUT) :: time
+      END FUNCTION s2d_checkpoint_read
    END INTERFACE
 END MODULE s2d_m

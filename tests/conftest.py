@@ -14,10 +14,10 @@ def pytest_configure(config):
 
 @pytest.fixture(scope="session")
 def built_lib():
-    """Path of the shared library, building it in-tree if it is absent."""
-    from spectral2d_gb300 import _lib
-    if not os.path.exists(_lib.LIB_PATH):
-        from spectral2d_gb300 import build
+    """Path of the shared library, building it (and the spectral2d_run main
+    program) in-tree if either is absent."""
+    from spectral2d_gb300 import _lib, build
+    if not os.path.exists(_lib.LIB_PATH) or not os.path.exists(build.DRIVER):
         build.build()
     return _lib.LIB_PATH
 

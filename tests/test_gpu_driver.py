@@ -96,12 +96,3 @@ def test_desired_end_time_lands_on_t_end(driver, tmp_path):
         wb, _ = r.get_state()
     assert nadv == 4 and t == pytest.approx(t_end, abs=1e-15)
     assert np.array_equal(wa, wb)
-
-
-def test_bad_arguments_exit_nonzero(driver, tmp_path):
-    p = subprocess.run([driver, "--nx", "60", "--out", str(tmp_path)], stdout=subprocess.PIPE,
-                       stderr=subprocess.STDOUT, text=True, timeout=60)
-    assert p.returncode == 1 and "s2d_create" in p.stdout
-    p = subprocess.run([driver, "--bogus"], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
-                       text=True, timeout=60)
-    assert p.returncode == 2
