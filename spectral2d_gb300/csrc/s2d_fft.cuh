@@ -153,6 +153,59 @@ __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int T
     __syncthreads();
 }
 
+// Radix-3 DFT of (a, 0, c): 8 instead of 12 floating-point instructions.
+template <bool INV, typename VT>
+__device__ __forceinline__ void bf3_bzero(VT* v) {
+    using T = decltype(v[0].x);
+    const T s = (T)0.86602540378443864676;
+    const T h = (T)0.5;
+    const VT a = v[0], c = v[2];
+    const T mx = a.x - h * c.x, my = a.y - h * c.y;
+    v[0].x = a.x + c.x;
+    v[0].y = a.y + c.y;
+    if (!INV) {  // y1 = m + i s c, y2 = m - i s c
+        v[1].x = mx - s * c.y;
+        v[1].y = my + s * c.x;
+        v[2].x = mx + s * c.y;
+        v[2].y = my - s * c.x;
+    } else {
+        v[1].x = mx + s * c.y;
+        v[1].y = my - s * c.x;
+        v[2].x = mx - s * c.y;
+        v[2].y = my + s * c.x;
+    }
+}
+
+// First pass of an inverse transform whose input is zero in the middle third
+// except at index M/3 -- every inverse transform here: the spectra are
+// truncated to |k| <= K = M/3, so index n is non-zero only for n <= K or
+// n >= M - K.  Butterfly j reads (x[j], x[j + M/3], x[j + 2M/3]); its middle
+// input is zero for j > 0.
+template <bool INV, typename VT>
+__device__ __forceinline__ void fft_pass3_midzero(VT* buf, int M, int lane, int Tg) {
+    constexpr int NB = kElemsPerThread / 3;
+    VT v[NB][3];
+    const int stride = M / 3;
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = lane + b * Tg;
+        v[b][0] = buf[j];
+        v[b][1] = buf[j + stride];
+        v[b][2] = buf[j + 2 * stride];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+        const int j = lane + b * Tg;
+        if (j == 0) bf3<INV>(v[b]);
+        else bf3_bzero<INV>(v[b]);
+        buf[j * 3] = v[b][0];
+        buf[j * 3 + 1] = v[b][1];
+        buf[j * 3 + 2] = v[b][2];
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ double ffma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float ffma(float a, float b, float c) { return fmaf(a, b, c); }
 
@@ -276,7 +329,9 @@ __device__ __forceinline__ void fft_pass2_fma(VT* buf, int M, int Ns, int lane, 
 // Full transform: unnormalised, sign -1 (forward) or +1 (INV).  Every thread
 // of the CTA must call it (it synchronises the CTA); starts with a barrier so
 // that callers may fill buf just before.  tw points at the complex table
-// (M entries) followed, d.tab_bytes later, by the TwEnt table.
+// (M entries) followed, d.tab_bytes later, by the TwEnt table.  Inverse
+// transforms of truncated spectra (input zero for K < n < M - K, K = M/3: the
+// inverse transforms of this library) take the pruned first radix-3 pass.
 template <bool INV, typename VT>
 __device__ __forceinline__ void fft_run(VT* buf, const Dims& d, int lane, const VT* __restrict__ tw) {
     using T = decltype(buf[0].x);
@@ -286,7 +341,9 @@ __device__ __forceinline__ void fft_run(VT* buf, const Dims& d, int lane, const 
     for (int p = 0; p < d.npass; ++p) {
         const int R = d.radix[p];
         const int off = d.twoff[p];
-        if (R == 4) {
+        if (INV && p == 0 && R == 3 && 3 * d.K == d.M) {
+            fft_pass3_midzero<INV>(buf, d.M, lane, d.Tg);
+        } else if (R == 4) {
             if (off >= 0) fft_pass4_fma<INV>(buf, d.M, Ns, lane, d.Tg, tab + off);
             else fft_pass<4, INV>(buf, d.M, Ns, lane, d.Tg, tw);
         } else if (R == 2) {
