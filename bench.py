@@ -454,11 +454,13 @@ def main():
         t1 = time.perf_counter()
         el = D.reduce(t1 - t0, "MAX")
         nbytes = w_host.nbytes
+        # in: the retained rectangle of wC (kx <= N/2, |ky| <= N/2); out: wC and psiC whole
+        h2d = (n // 2 + 1) * 16 * (n + 1)
         e2e = {"value": D.reduce(n * n * args.e2e_steps / el / 1e6, "SUM"), "unit": "Mpt*steps/s",
-               "h2d_bytes_per_step": nbytes, "d2h_bytes_per_step": 2 * nbytes,
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 2 * nbytes,
                "steps": args.e2e_steps,
                "path": "s2d_integrate_one_step_host on pinned host arrays "
-                       "(reference-layout wC in; wC, psiC out)"}
+                       "(reference-layout wC in: its retained modes; wC, psiC out)"}
 
     if rank == 0:
         line = {

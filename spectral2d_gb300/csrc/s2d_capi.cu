@@ -216,9 +216,18 @@ int ensure_ref_stage(s2d_handle* h) {
     return S2D_OK;
 }
 
+// Only the retained rectangle of the reference array is read (kx <= K in rows
+// ky = 0..K and ky = -K..-1, i.e. rows 0..K and M-K..M-1): the rest is
+// truncated away, so it is not copied either.
 int upload_ref(s2d_handle* h, const double* wC) {
     S2D_TRY(ensure_ref_stage(h));
-    S2D_CUDA(cudaMemcpyAsync(h->ref_stage, wC, h->ref_bytes, cudaMemcpyHostToDevice, h->stream));
+    const size_t pitch = (size_t)h->grid.cISize * 2 * sizeof(double);
+    const size_t width = (size_t)h->d.KX * 2 * sizeof(double);
+    const int K = h->d.K, M = h->d.M;
+    S2D_CUDA(cudaMemcpy2DAsync(h->ref_stage, pitch, wC, pitch, width, K + 1, cudaMemcpyHostToDevice, h->stream));
+    S2D_CUDA(cudaMemcpy2DAsync((char*)h->ref_stage + (size_t)(M - K) * pitch, pitch,
+                               (const char*)wC + (size_t)(M - K) * pitch, pitch, width, K, cudaMemcpyHostToDevice,
+                               h->stream));
     if (h->prec == S2D_FP64)
         S2D_CUDA(Kern<double>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
     else
