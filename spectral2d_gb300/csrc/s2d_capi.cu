@@ -210,36 +210,24 @@ int check_ref_dims(const s2d_handle* h, int cISize, int nyG) {
     return S2D_OK;
 }
 
-// Staging for reference-layout arrays, and two copy streams: host<->device
-// copies are split across them so that two copy engines share the link.
 int ensure_ref_stage(s2d_handle* h) {
     if (h->ref_stage) return S2D_OK;
-    for (int i = 0; i < 2; ++i)
-        S2D_CUDA(cudaStreamCreateWithFlags(&h->cs[i], cudaStreamNonBlocking));
-    for (int i = 0; i < 3; ++i) S2D_CUDA(cudaEventCreateWithFlags(&h->cev[i], cudaEventDisableTiming));
     S2D_CUDA(cudaMalloc(&h->ref_stage, 2 * h->ref_bytes));
     return S2D_OK;
 }
 
 // Only the retained rectangle of the reference array is read (kx <= K in rows
 // ky = 0..K and ky = -K..-1, i.e. rows 0..K and M-K..M-1): the rest is
-// truncated away, so it is not copied either.  The two row blocks go over the
-// two copy streams; the handle's stream waits for both.
+// truncated away, so it is not copied either.
 int upload_ref(s2d_handle* h, const double* wC) {
     S2D_TRY(ensure_ref_stage(h));
     const size_t pitch = (size_t)h->grid.cISize * 2 * sizeof(double);
     const size_t width = (size_t)h->d.KX * 2 * sizeof(double);
     const int K = h->d.K, M = h->d.M;
-    S2D_CUDA(cudaEventRecord(h->cev[0], h->stream));
-    for (int i = 0; i < 2; ++i) S2D_CUDA(cudaStreamWaitEvent(h->cs[i], h->cev[0], 0));
-    S2D_CUDA(cudaMemcpy2DAsync(h->ref_stage, pitch, wC, pitch, width, K + 1, cudaMemcpyHostToDevice, h->cs[0]));
+    S2D_CUDA(cudaMemcpy2DAsync(h->ref_stage, pitch, wC, pitch, width, K + 1, cudaMemcpyHostToDevice, h->stream));
     S2D_CUDA(cudaMemcpy2DAsync((char*)h->ref_stage + (size_t)(M - K) * pitch, pitch,
                                (const char*)wC + (size_t)(M - K) * pitch, pitch, width, K, cudaMemcpyHostToDevice,
-                               h->cs[1]));
-    for (int i = 0; i < 2; ++i) {
-        S2D_CUDA(cudaEventRecord(h->cev[1 + i], h->cs[i]));
-        S2D_CUDA(cudaStreamWaitEvent(h->stream, h->cev[1 + i], 0));
-    }
+                               h->stream));
     if (h->prec == S2D_FP64)
         S2D_CUDA(Kern<double>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
     else
@@ -258,16 +246,9 @@ int download_ref(s2d_handle* h, const void* S, double* wC, double* psiC) {
     else
         S2D_CUDA(Kern<float>::compact_to_ref(h->d, S, h->grid.cISize, wC ? dW : nullptr, psiC ? dP : nullptr,
                                              h->stream));
-    // each array in two halves, one per copy stream
-    S2D_CUDA(cudaEventRecord(h->cev[0], h->stream));
-    const size_t half = h->ref_bytes / 2 / 16 * 16;
-    for (int i = 0; i < 2; ++i) {
-        S2D_CUDA(cudaStreamWaitEvent(h->cs[i], h->cev[0], 0));
-        const size_t off = i ? half : 0, n = i ? h->ref_bytes - half : half;
-        if (wC) S2D_CUDA(cudaMemcpyAsync((char*)wC + off, (char*)dW + off, n, cudaMemcpyDeviceToHost, h->cs[i]));
-        if (psiC) S2D_CUDA(cudaMemcpyAsync((char*)psiC + off, (char*)dP + off, n, cudaMemcpyDeviceToHost, h->cs[i]));
-    }
-    for (int i = 0; i < 2; ++i) S2D_CUDA(cudaStreamSynchronize(h->cs[i]));
+    if (wC) S2D_CUDA(cudaMemcpyAsync(wC, dW, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
+    if (psiC) S2D_CUDA(cudaMemcpyAsync(psiC, dP, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
     return S2D_OK;
 }
 
@@ -524,13 +505,6 @@ S2D_API void s2d_destroy(s2d_handle* h) {
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab};
     for (void* p : ptrs)
         if (p) cudaFree(p);
-    for (int i = 0; i < 2; ++i)
-        if (h->cs[i]) {
-            cudaStreamSynchronize(h->cs[i]);
-            cudaStreamDestroy(h->cs[i]);
-        }
-    for (int i = 0; i < 3; ++i)
-        if (h->cev[i]) cudaEventDestroy(h->cev[i]);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
 }

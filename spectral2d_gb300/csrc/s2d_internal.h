@@ -153,8 +153,6 @@ struct s2d_handle {
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array
-    cudaStream_t cs[2] = {nullptr, nullptr};          // host<->device copy streams
-    cudaEvent_t cev[3] = {nullptr, nullptr, nullptr}; // their joins with `stream`
     unsigned int* flags = nullptr;
     unsigned long long* red64 = nullptr;  // 8 reduction words
     double* dscratch = nullptr;           // spectrum / partial sums
