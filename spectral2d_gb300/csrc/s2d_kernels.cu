@@ -31,9 +31,12 @@ namespace s2d {
 
 // ------------------------------------------------------------------------
 // K1, K2, K3 of one simulation: one tile per CTA (bodies in s2d_step.cuh).
+// K1 and K2 come in two register budgets: LB3 = CTAs of at most 256 threads,
+// three per SM (80 registers: a third CTA fills the barrier phases of the
+// other two), and the general one (up to 512 threads, M = 6144).
 // ------------------------------------------------------------------------
-template <typename T>
-__global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
+template <typename T, bool LB3>
+__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
                                                const double* __restrict__ rk2, FieldSet fs,
                                                const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -41,8 +44,8 @@ __global__ void __launch_bounds__(512) k_yinv(Dims d, const typename Vec<T>::t* 
     yinv_body<T>(d, S, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(512) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+template <typename T, bool LB3>
+__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
     using VT = typename Vec<T>::t;
@@ -458,7 +461,10 @@ cudaError_t Kern<T>::yinv(const Dims& d, const void* S, const double* rk2, const
                           cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
-    k_yinv<T><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    if (sizeof(T) == 8 && L.threads <= 256)
+        k_yinv<T, true><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    else
+        k_yinv<T, false><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
     return cudaGetLastError();
 }
 
@@ -478,8 +484,12 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
                                const Launch& L) {
     using VT = typename Vec<T>::t;
     const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
-    k_xpass_bas<T><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G,
-                                                                       scale);
+    if (sizeof(T) == 8 && L.threads <= 256)
+        k_xpass_bas<T, true><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
+                                                                                (const VT*)tw, L.G, scale);
+    else
+        k_xpass_bas<T, false><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
+                                                                                 (const VT*)tw, L.G, scale);
     return cudaGetLastError();
 }
 
@@ -603,12 +613,16 @@ cudaError_t configure_kernels(int max_smem_optin) {
         cudaError_t e2 = set_smem(k, max_smem_optin);       \
         if (e2 != cudaSuccess && e == cudaSuccess) e = e2;  \
     } while (0)
-    S2D_SET(k_yinv<double>);
-    S2D_SET(k_yinv<float>);
+    S2D_SET((k_yinv<double, true>));
+    S2D_SET((k_yinv<double, false>));
+    S2D_SET((k_yinv<float, true>));
+    S2D_SET((k_yinv<float, false>));
     S2D_SET(k_xpass_rhs<double>);
     S2D_SET(k_xpass_rhs<float>);
-    S2D_SET(k_xpass_bas<double>);
-    S2D_SET(k_xpass_bas<float>);
+    S2D_SET((k_xpass_bas<double, true>));
+    S2D_SET((k_xpass_bas<double, false>));
+    S2D_SET((k_xpass_bas<float, true>));
+    S2D_SET((k_xpass_bas<float, false>));
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
     S2D_SET(k_xinv_cfl<double>);
