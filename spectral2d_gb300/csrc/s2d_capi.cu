@@ -187,8 +187,17 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
     if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow));
     else S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
     if (ev) S2D_CUDA(cudaEventRecord(ev[2], h->stream));
-    S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->tw, h->flags,
-                               h->stream, h->L_yfwd));
+    if (h->Fv) {
+        // K3 in two launches (FP64, Basdevant): the column FFTs take three
+        // CTAs per SM; the products' spectra go through I[2] (free in this
+        // form) and Fv in the compact layout
+        S2D_CUDA(Kern<T>::yfwd_col(d, h->I[0], h->I[1], h->I[2], h->Fv, h->tw, h->stream, h->L_ycol));
+        S2D_CUDA(Kern<T>::stage(d, h->I[2], h->Fv, h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->flags,
+                                h->stream));
+    } else {
+        S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->tw,
+                                   h->flags, h->stream, h->L_yfwd));
+    }
     if (ev) S2D_CUDA(cudaEventRecord(ev[3], h->stream));
     return S2D_OK;
 }
@@ -428,6 +437,7 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     cudaMemsetAsync((p), 0, (n), h->stream);
     S2D_ALLOC(h->S0, state_bytes);
     S2D_ALLOC(h->S1, state_bytes);
+    if (h->prec == S2D_FP64 && h->ph.form == S2D_NL_BASDEVANT) S2D_ALLOC(h->Fv, state_bytes);
     S2D_ALLOC(h->Ibase, 3 * h->Ibytes);
     h->I[0] = h->Ibase;
     h->I[1] = (char*)h->Ibase + h->Ibytes;
@@ -488,6 +498,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     }
     if ((rr = pick_launch(h, d.Tg, tb, tgt, d.M, &h->L_xrow, "row transform")) != S2D_OK) return bail(rr);
     if ((rr = pick_launch(h, d.Tg, tb, tgt, d.KX, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
+    if ((rr = pick_launch(h, d.Tg, tb, tgt, 2L * d.KX, &h->L_ycol, "forward y-pass (split)")) != S2D_OK)
+        return bail(rr);
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
     *out = h;
@@ -502,7 +514,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
     void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->tw,  h->ref_stage,
-                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab};
+                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
@@ -802,7 +814,7 @@ S2D_API int s2d_time_steps(s2d_handle* h, int32_t n, double dt, double* ms, doub
 
 S2D_API int s2d_kernels_per_step(const s2d_handle* h) {
     if (!h) return fail(S2D_ERR_INVALID, "null handle");
-    return 9;
+    return h->Fv ? 12 : 9;
 }
 
 S2D_API int s2d_host_alloc(size_t bytes, void** ptr) {

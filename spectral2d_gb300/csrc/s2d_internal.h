@@ -100,6 +100,13 @@ struct Kern {
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
                                 void* Sdw, const void* src, int stage, double dt, const Phys& ph,
                                 const void* tw, unsigned int* flags, cudaStream_t st, const Launch& L);
+    // K3 in two launches: forward y-FFT of the columns of both products into
+    // compact arrays Fu, Fv, then the epilogue (dW, stage update, Truncate)
+    static cudaError_t yfwd_col(const Dims& d, const void* Iu, const void* Iv, void* Fu, void* Fv,
+                                const void* tw, cudaStream_t st, const Launch& L);
+    static cudaError_t stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
+                             const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
+                             cudaStream_t st);
     static cudaError_t ref_to_compact(const Dims& d, const double* ref, int C, void* S,
                                       cudaStream_t st);
     static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
@@ -157,7 +164,8 @@ struct s2d_handle {
     unsigned long long* red64 = nullptr;  // 8 reduction words
     double* dscratch = nullptr;           // spectrum / partial sums
     size_t dscratch_n = 0;
-    s2d::Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore;
+    void* Fv = nullptr;   // FP64 Basdevant: second compact array of the split K3 (the first is I[2])
+    s2d::Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore, L_ycol;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0.0;

@@ -68,6 +68,26 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
     if (bad) atomicOr(flags, 1u);
 }
 
+// K3 split in two (FP64 single runs): forward y-FFT of one field's columns
+// into a compact array, then the epilogue of every mode.
+template <typename T, bool LB3>
+__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1)
+    k_yfwd_col(Dims d, const typename Vec<T>::t* __restrict__ Iu, const typename Vec<T>::t* __restrict__ Iv,
+               typename Vec<T>::t* Fu, typename Vec<T>::t* Fv, const typename Vec<T>::t* __restrict__ tw, int G) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    yfwd_col_body<T>(d, Iu, Iv, Fu, Fv, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_stage(Dims d, const typename Vec<T>::t* __restrict__ Fu,
+                                               const typename Vec<T>::t* __restrict__ Fv, typename Vec<T>::t* S0,
+                                               typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
+                                               const typename Vec<T>::t* __restrict__ src, int stage, double dt,
+                                               Phys ph, unsigned int* flags) {
+    if (stage_body<T>(d, Fu, Fv, S0, S1, Sdw, src, stage, dt, ph)) atomicOr(flags, 1u);
+}
+
 // ------------------------------------------------------------------------
 // K2 in the conservative form (the reference's): row pairs (y1, y2) =
 // (2p, 2p+1).  Per group two buffers: W holds omega of both rows (w1 = Re,
@@ -505,6 +525,30 @@ cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, voi
 }
 
 template <typename T>
+cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, void* Fu, void* Fv, const void* tw,
+                              cudaStream_t st, const Launch& L) {
+    using VT = typename Vec<T>::t;
+    const int ncg = (d.KX + L.G - 1) / L.G;
+    if (sizeof(T) == 8 && L.threads <= 256)
+        k_yfwd_col<T, true><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
+                                                               (const VT*)tw, L.G);
+    else
+        k_yfwd_col<T, false><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
+                                                                (const VT*)tw, L.G);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
+                           const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
+                           cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    k_stage<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const VT*)Fu, (const VT*)Fv, (VT*)S0, (VT*)S1,
+                                                                 (VT*)Sdw, (const VT*)src, stage, dt, ph, flags);
+    return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t Kern<T>::ref_to_compact(const Dims& d, const double* ref, int C, void* S, cudaStream_t st) {
     using VT = typename Vec<T>::t;
     k_ref_to_compact<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const double2*)ref, C, (VT*)S);
@@ -623,6 +667,10 @@ cudaError_t configure_kernels(int max_smem_optin) {
     S2D_SET((k_xpass_bas<double, false>));
     S2D_SET((k_xpass_bas<float, true>));
     S2D_SET((k_xpass_bas<float, false>));
+    S2D_SET((k_yfwd_col<double, true>));
+    S2D_SET((k_yfwd_col<double, false>));
+    S2D_SET((k_yfwd_col<float, true>));
+    S2D_SET((k_yfwd_col<float, false>));
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
     S2D_SET(k_xinv_cfl<double>);

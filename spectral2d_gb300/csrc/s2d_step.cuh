@@ -178,6 +178,122 @@ __device__ __forceinline__ void xpass_bas_body(const Dims& d, typename Vec<T>::t
     extract_pair(Z, urow, vrow, d, lane, active, scale);
 }
 
+// One mode (kx, jc) of the K3 epilogue: dW from the two transformed products
+// nx, ny, then the stage update below, Truncate (|k|^2 > K^2 -> 0) and the
+// non-finite check.  Returns true for a non-finite result.
+template <typename T>
+__device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx, typename Vec<T>::t ny, int kx,
+                                            int jc, typename Vec<T>::t* S0, typename Vec<T>::t* S1,
+                                            typename Vec<T>::t* Sdw, const typename Vec<T>::t* __restrict__ src,
+                                            int stage, double dt, const Phys& ph) {
+    using VT = typename Vec<T>::t;
+    const T tdt = (T)dt;
+    const T c34 = (T)0.75, c14 = (T)0.25, c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0);
+    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * 2.0 / 3.0);
+    const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
+    const int ky = ky_of_jc(d, jc);
+    const size_t off = (size_t)kx * d.ldS + jc;
+    const int kk = kx * kx + ky * ky;
+    bool bad = false;
+    VT out;
+    if (kk > d.K * d.K) {
+        out = mk<VT>((T)0, (T)0);
+    } else {
+        const VT w0 = S0[off];
+        const VT win = (stage <= 1) ? w0 : S1[off];
+        const T fkx = (T)kx, fky = (T)ky;
+        const T visc = tnu * (T)kk;
+        T dwx, dwy;
+        if (ph.form == S2D_NL_BASDEVANT) {
+            // dW = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2] - nu k^2 w
+            const T c1 = (T)(kx * kx - ky * ky), c2 = (T)(kx * ky);
+            dwx = c1 * nx.x + c2 * ny.x - visc * win.x;
+            dwy = c1 * nx.y + c2 * ny.y - visc * win.y;
+        } else {
+            // dW = -i kx F[uw] - i ky F[vw] - nu k^2 w  (src/Spectral.F90:464-479)
+            dwx = fkx * nx.y + fky * ny.y - visc * win.x;
+            dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+        }
+        if (talpha != (T)0) {
+            dwx -= talpha * win.x;
+            dwy -= talpha * win.y;
+        }
+        if (ph.fk != 0 && kx == 0 && (ky == ph.fk || ky == -ph.fk)) {
+            dwx += (T)ph.f_re;
+            dwy += (ky > 0) ? (T)ph.f_im : (T)(-ph.f_im);
+        }
+        if (src) {
+            const VT e = src[off];
+            dwx += e.x;
+            dwy += e.y;
+        }
+        if (stage == 0) {
+            out = mk<VT>(dwx, dwy);
+        } else if (stage == 1) {
+            out = mk<VT>(w0.x + tdt * dwx, w0.y + tdt * dwy);
+        } else if (stage == 2) {
+            out = mk<VT>(c34 * w0.x + c14 * win.x + dt4 * dwx, c34 * w0.y + c14 * win.y + dt4 * dwy);
+        } else {
+            out = mk<VT>(c13 * w0.x + c23 * win.x + dt23 * dwx, c13 * w0.y + c23 * win.y + dt23 * dwy);
+        }
+        bad = bits_nonfinite(out.x) | bits_nonfinite(out.y);
+    }
+    if (stage == 0) Sdw[off] = out;
+    else if (stage == 3) S0[off] = out;
+    else S1[off] = out;
+    return bad;
+}
+
+// K3 split in two for a third CTA per SM (the single-run FP64 path): the
+// forward y-FFT of one field's columns, its retained rows stored in the
+// compact layout (Out[kx][jc])...
+template <typename T>
+__device__ __forceinline__ void yfwd_col_body(const Dims& d, const typename Vec<T>::t* __restrict__ Iu,
+                                              const typename Vec<T>::t* __restrict__ Iv, typename Vec<T>::t* OutU,
+                                              typename Vec<T>::t* OutV, const typename Vec<T>::t* __restrict__ tw,
+                                              int G, int blk, typename Vec<T>::t* bufs) {
+    using VT = typename Vec<T>::t;
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int ncg = (d.KX + G - 1) / G;
+    const int f = blk / ncg;
+    const int kx0 = (blk - f * ncg) * G;
+    const int gtot = min(G, d.KX - kx0);
+    const VT* I = f ? Iv : Iu;
+    VT* Out = f ? OutV : OutU;
+    for (int idx = threadIdx.x; idx < G * d.M; idx += blockDim.x) {
+        const int gg = idx % G;
+        const int y = idx / G;
+        bufs[(size_t)gg * d.M + y] = gg < gtot ? __ldcg(&I[(size_t)y * d.ldI + kx0 + gg]) : mk<VT>((T)0, (T)0);
+    }
+    fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = idx / d.KY;
+        const int jc = idx - gg * d.KY;
+        const int n = jc <= d.K ? jc : ky_of_jc(d, jc) + d.M;
+        Out[(size_t)(kx0 + gg) * d.ldS + jc] = bufs[(size_t)gg * d.M + n];
+    }
+}
+
+// ... and the epilogue of every mode from the two compact arrays.
+template <typename T>
+__device__ __forceinline__ bool stage_body(const Dims& d, const typename Vec<T>::t* __restrict__ Fu,
+                                           const typename Vec<T>::t* __restrict__ Fv, typename Vec<T>::t* S0,
+                                           typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
+                                           const typename Vec<T>::t* __restrict__ src, int stage, double dt,
+                                           const Phys& ph) {
+    bool bad = false;
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const size_t off = (size_t)kx * d.ldS + jc;
+        bad |= stage_point<T>(d, __ldcg(&Fu[off]), __ldcg(&Fv[off]), kx, jc, S0, S1, Sdw, src, stage, dt, ph);
+    }
+    return bad;
+}
+
 // ------------------------------------------------------------------------
 // K3: forward y-pass of the two products + RK3 stage epilogue on columns
 // [blk*G, blk*G+G): 2G transforms (G columns x two product fields: {u v,
@@ -218,68 +334,14 @@ __device__ __forceinline__ bool yfwd_body(const Dims& d, const typename Vec<T>::
     for (int t0 = 0; t0 < 2 * G; t0 += nconc) fft_run<false>(bufs + (size_t)(t0 + t) * d.M, d, lane, tw);
     __syncthreads();
 
-    const T tdt = (T)dt;
-    const T c34 = (T)0.75, c14 = (T)0.25, c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0);
-    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * 2.0 / 3.0);
-    const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
-    const int K2 = d.K * d.K;
     bool bad = false;
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
         const int gg = idx / d.KY;
         const int jc = idx - gg * d.KY;
-        const int kx = kx0 + gg;
         const int ky = ky_of_jc(d, jc);
         const int n = jc <= d.K ? jc : ky + d.M;
-        const size_t off = (size_t)kx * d.ldS + jc;
-        const int kk = kx * kx + ky * ky;
-        VT out;
-        if (kk > K2) {
-            out = mk<VT>((T)0, (T)0);
-        } else {
-            const VT nx = bufs[(size_t)gg * d.M + n];
-            const VT ny = bufs[(size_t)(G + gg) * d.M + n];
-            const VT w0 = S0[off];
-            const VT win = (stage <= 1) ? w0 : S1[off];
-            const T fkx = (T)kx, fky = (T)ky;
-            const T visc = tnu * (T)kk;
-            T dwx, dwy;
-            if (ph.form == S2D_NL_BASDEVANT) {
-                // dW = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2] - nu k^2 w
-                const T c1 = (T)(kx * kx - ky * ky), c2 = (T)(kx * ky);
-                dwx = c1 * nx.x + c2 * ny.x - visc * win.x;
-                dwy = c1 * nx.y + c2 * ny.y - visc * win.y;
-            } else {
-                // dW = -i kx F[uw] - i ky F[vw] - nu k^2 w  (src/Spectral.F90:464-479)
-                dwx = fkx * nx.y + fky * ny.y - visc * win.x;
-                dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
-            }
-            if (talpha != (T)0) {
-                dwx -= talpha * win.x;
-                dwy -= talpha * win.y;
-            }
-            if (ph.fk != 0 && kx == 0 && (ky == ph.fk || ky == -ph.fk)) {
-                dwx += (T)ph.f_re;
-                dwy += (ky > 0) ? (T)ph.f_im : (T)(-ph.f_im);
-            }
-            if (src) {
-                const VT e = src[off];
-                dwx += e.x;
-                dwy += e.y;
-            }
-            if (stage == 0) {
-                out = mk<VT>(dwx, dwy);
-            } else if (stage == 1) {
-                out = mk<VT>(w0.x + tdt * dwx, w0.y + tdt * dwy);
-            } else if (stage == 2) {
-                out = mk<VT>(c34 * w0.x + c14 * win.x + dt4 * dwx, c34 * w0.y + c14 * win.y + dt4 * dwy);
-            } else {
-                out = mk<VT>(c13 * w0.x + c23 * win.x + dt23 * dwx, c13 * w0.y + c23 * win.y + dt23 * dwy);
-            }
-            bad |= bits_nonfinite(out.x) | bits_nonfinite(out.y);
-        }
-        if (stage == 0) Sdw[off] = out;
-        else if (stage == 3) S0[off] = out;
-        else S1[off] = out;
+        bad |= stage_point<T>(d, bufs[(size_t)gg * d.M + n], bufs[(size_t)(G + gg) * d.M + n], kx0 + gg, jc, S0, S1,
+                              Sdw, src, stage, dt, ph);
     }
     return bad;
 }
