@@ -432,12 +432,16 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     const size_t state_bytes = (size_t)d.KX * d.ldS * h->vsz;
     h->Ibytes = (size_t)d.M * d.ldI * h->vsz;
 #define S2D_ALLOC(p, n)                                                                                   \
-    if (cudaMalloc((void**)&(p), (n)) != cudaSuccess)                                                    \
-        return bail(fail(S2D_ERR_NOMEM, "cudaMalloc of %zu bytes failed", (size_t)(n)));                 \
-    cudaMemsetAsync((p), 0, (n), h->stream);
+    do {                                                                                                  \
+        if (cudaMalloc((void**)&(p), (n)) != cudaSuccess)                                                \
+            return bail(fail(S2D_ERR_NOMEM, "cudaMalloc of %zu bytes failed", (size_t)(n)));             \
+        cudaMemsetAsync((p), 0, (n), h->stream);                                                          \
+    } while (0)
     S2D_ALLOC(h->S0, state_bytes);
     S2D_ALLOC(h->S1, state_bytes);
-    if (h->prec == S2D_FP64 && h->ph.form == S2D_NL_BASDEVANT) S2D_ALLOC(h->Fv, state_bytes);
+    if (h->prec == S2D_FP64 && h->ph.form == S2D_NL_BASDEVANT) {
+        S2D_ALLOC(h->Fv, state_bytes);
+    }
     S2D_ALLOC(h->Ibase, 3 * h->Ibytes);
     h->I[0] = h->Ibase;
     h->I[1] = (char*)h->Ibase + h->Ibytes;
