@@ -308,3 +308,24 @@ def test_kolmogorov_4096_one_step_vs_oracle(S2D):
     err, err32 = O.rel_l2(w1, wr), O.rel_l2(w32, wr)
     print(f"4096^2 Kolmogorov one step: FP64 rel-L2 {err:.3e}, FP32 rel-L2 {err32:.3e}")
     assert err < 1e-12 and err32 < 1e-5
+
+
+@pytest.mark.parametrize("n", [256, 2048])
+def test_inviscid_rhs_conserves_energy_and_enstrophy(S2D, n):
+    """A size-independent property at the full workload size: with nu = 0 the
+    dealiased nonlinear term of the truncated system conserves energy and
+    enstrophy, sum Re(conj(psi) dW) = sum Re(conj(w) dW) = 0 (half-spectrum
+    weights 1 at kx = 0, 2 elsewhere), to round-off.  The seeded
+    k^4 exp(-2 (k/10)^2) state has no energy at |k| = N/2."""
+    g = O.get_grid_size(n, n)
+    with S2D(n, nu=0.0) as s:
+        s.set_turbulent_velocity(seed=7, spectrum="k4gauss", k0=10.0, tke=0.5)
+        w, psi = s.get_state()
+        dW = s.compute_rhs()
+    wt = np.where(g.kxG[None, :] == 0, 1.0, 2.0)
+    dE = np.sum(wt * (np.conj(psi) * dW).real)
+    dZ = np.sum(wt * (np.conj(w) * dW).real)
+    rel_e = abs(dE) / np.sum(wt * np.abs(psi) * np.abs(dW))
+    rel_z = abs(dZ) / np.sum(wt * np.abs(w) * np.abs(dW))
+    print(f"N={n}: inviscid dE/dt rel {rel_e:.2e}, dZ/dt rel {rel_z:.2e}")
+    assert rel_e < 1e-12 and rel_z < 1e-12
