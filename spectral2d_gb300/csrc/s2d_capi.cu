@@ -96,7 +96,7 @@ std::vector<TwEnt<T>> fma_tables(Dims* d) {
     for (int p = 0; p < d->npass; ++p) {
         const int R = d->radix[p];
         d->twoff[p] = -1;
-        if (p > 0 && (R == 4 || R == 2) && d->E == kElemsPerThread) {
+        if (p > 0 && (R == 4 || R == 2)) {
             d->twoff[p] = (int)tab.size();
             const long long step = d->M / (Ns * R);
             for (int k = 0; k < Ns; ++k) {
@@ -119,31 +119,17 @@ std::vector<TwEnt<T>> fma_tables(Dims* d) {
     return tab;
 }
 
-// Radix plan of an M = 2^a 3^b transform.  12 elements per thread (FP64, and
-// FP32 when 24 does not divide M): passes 3..3, (2), 4..4.  24 elements per
-// thread (FP32, 24 | M): 3..3, then 3 * 2^(a mod 3) (3, 6 or 12), then a/3
-// radix-8 passes -- 4 passes instead of 6 at M = 3072, so a third less
-// shared-memory traffic and fewer barriers.
-bool factor_plan(int M, bool fp32, Dims* d) {
+bool factor_plan(int M, Dims* d) {
     int m = M, a = 0, b = 0;
     while (m % 2 == 0) { m /= 2; ++a; }
     while (m % 3 == 0) { m /= 3; ++b; }
     if (m != 1 || M % kElemsPerThread != 0) return false;
     int np = 0;
-    if (fp32 && M % kElemsFP32 == 0) {
-        for (int i = 0; i < b - 1; ++i) d->radix[np++] = 3;
-        d->radix[np++] = 3 << (a % 3);
-        for (int i = 0; i < a / 3; ++i) d->radix[np++] = 8;
-        d->E = kElemsFP32;
-    } else {
-        for (int i = 0; i < b; ++i) d->radix[np++] = 3;
-        if (a % 2) d->radix[np++] = 2;
-        for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
-        d->E = kElemsPerThread;
-    }
+    for (int i = 0; i < b; ++i) d->radix[np++] = 3;
+    if (a % 2) d->radix[np++] = 2;
+    for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
     if (np > kMaxPasses) return false;
     d->npass = np;
-    d->Tg = M / d->E;
     return true;
 }
 
@@ -393,10 +379,11 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     d.M = h->grid.nxG;
     d.ldS = d.KY + 1;                  // even pitch: 16-byte aligned FP32 columns
     d.ldI = (d.KX + 3) / 4 * 4;
-    if (!factor_plan(d.M, h->prec == S2D_FP32, &d)) {
+    if (!factor_plan(d.M, &d)) {
         delete h;
         return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", d.M);
     }
+    d.Tg = d.M / kElemsPerThread;
     h->ph.nu = cfg->nu;
     h->ph.alpha = cfg->alpha;
     h->ph.form = cfg->nonlinear_form;
@@ -496,10 +483,9 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
     // launch shapes: about 256 threads per CTA so that at least two CTAs
-    // share an SM and one CTA's barrier phases overlap the other's FP64 work;
-    // 128 for the FP32 24-element threads (~96 registers: five CTAs per SM)
+    // share an SM and one CTA's barrier phases overlap the other's FP64 work
     const size_t tb = (size_t)d.M * h->vsz;
-    const int tgt = d.E == kElemsFP32 ? 128 : 256;
+    const int tgt = 256;
     int rr;
     const int nf = h->ph.form == S2D_NL_BASDEVANT ? 2 : 3;
     if ((rr = pick_launch(h, d.Tg, tb, tgt, (long)nf * d.KX, &h->L_yinv, "inverse y-pass")) != S2D_OK)

@@ -114,95 +114,18 @@ __device__ __forceinline__ void bf4(VT* v) {
     }
 }
 
-// ---- register DFTs of radix 6, 8, 12 (the FP32 engine, 24 elements/thread) --
-// cos(2 pi j / 48) for j in [0, 12] (7.5-degree steps).
-template <typename T>
-__device__ __forceinline__ constexpr T cos48q(int j) {
-    return j == 0    ? (T)1.0
-           : j == 1  ? (T)0.99144486137381041114
-           : j == 2  ? (T)0.96592582628906828675
-           : j == 3  ? (T)0.92387953251128675613
-           : j == 4  ? (T)0.86602540378443864676
-           : j == 5  ? (T)0.79335334029123516458
-           : j == 6  ? (T)0.70710678118654752440
-           : j == 7  ? (T)0.60876142900872063942
-           : j == 8  ? (T)0.5
-           : j == 9  ? (T)0.38268343236508977173
-           : j == 10 ? (T)0.25881904510252076235
-           : j == 11 ? (T)0.13052619222005159155
-                     : (T)0.0;
-}
-// cos(2 pi j / 48) for any integer j
-template <typename T>
-__device__ __forceinline__ constexpr T cos48(int j) {
-    j %= 48;
-    if (j < 0) j += 48;
-    if (j > 24) j = 48 - j;
-    return j <= 12 ? cos48q<T>(j) : -cos48q<T>(24 - j);
-}
-
-// a * exp(-/+ 2 pi i j / 48) (forward / inverse); j is a compile-time
-// constant after unrolling, so the branches and constants fold.
-template <bool INV, typename VT>
-__device__ __forceinline__ VT mul_w48(VT a, int j) {
-    using T = decltype(a.x);
-    j %= 48;
-    if (j < 0) j += 48;
-    if (INV) j = (48 - j) % 48;   // exp(+2 pi i j/48) = exp(-2 pi i (48-j)/48)
-    if (j == 0) return a;
-    if (j == 12) return mk<VT>(a.y, -a.x);    // * (-i)
-    if (j == 24) return mk<VT>(-a.x, -a.y);
-    if (j == 36) return mk<VT>(-a.y, a.x);    // * (+i)
-    const T c = cos48<T>(j), s = -cos48<T>(j - 12);   // exp(-2 pi i j/48) = c + i s
-    return mk<VT>(a.x * c - a.y * s, a.x * s + a.y * c);
-}
-
-template <int R, bool INV, typename VT>
-__device__ __forceinline__ void butterfly(VT* v);
-
-// Cooley-Tukey in registers: R = R1 * R2, input n = R2 n1 + n2, output
-// k = k1 + R1 k2; R2 DFTs of size R1, twiddles exp(-+2 pi i n2 k1 / R), R1
-// DFTs of size R2.  Natural order in and out.
-template <int R1, int R2, bool INV, typename VT>
-__device__ __forceinline__ void dft_ct(VT* v) {
-    constexpr int R = R1 * R2;
-    VT t[R];
-#pragma unroll
-    for (int n2 = 0; n2 < R2; ++n2) {
-        VT a[R1];
-#pragma unroll
-        for (int n1 = 0; n1 < R1; ++n1) a[n1] = v[R2 * n1 + n2];
-        butterfly<R1, INV>(a);
-#pragma unroll
-        for (int k1 = 0; k1 < R1; ++k1) t[n2 * R1 + k1] = mul_w48<INV>(a[k1], (48 / R) * n2 * k1);
-    }
-#pragma unroll
-    for (int k1 = 0; k1 < R1; ++k1) {
-        VT b[R2];
-#pragma unroll
-        for (int n2 = 0; n2 < R2; ++n2) b[n2] = t[n2 * R1 + k1];
-        butterfly<R2, INV>(b);
-#pragma unroll
-        for (int k2 = 0; k2 < R2; ++k2) v[k1 + R1 * k2] = b[k2];
-    }
-}
-
 template <int R, bool INV, typename VT>
 __device__ __forceinline__ void butterfly(VT* v) {
     if constexpr (R == 2) bf2<INV>(v);
     else if constexpr (R == 3) bf3<INV>(v);
-    else if constexpr (R == 4) bf4<INV>(v);
-    else if constexpr (R == 6) dft_ct<3, 2, INV>(v);
-    else if constexpr (R == 8) dft_ct<4, 2, INV>(v);
-    else dft_ct<3, 4, INV>(v);   // 12
+    else bf4<INV>(v);
 }
 
-// One in-place Stockham pass of radix R over the transform in buf; each of
-// the Tg threads holds E elements (E/R butterflies).
-template <int R, bool INV, typename VT, int E = kElemsPerThread>
+// One in-place Stockham pass of radix R over the transform in buf.
+template <int R, bool INV, typename VT>
 __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int Tg,
                                          const VT* __restrict__ tw) {
-    constexpr int NB = E / R;
+    constexpr int NB = kElemsPerThread / R;
     VT v[NB][R];
     const int stride = M / R;
 #pragma unroll
@@ -415,24 +338,6 @@ __device__ __forceinline__ void fft_run(VT* buf, const Dims& d, int lane, const 
     const TwEnt<T>* tab = reinterpret_cast<const TwEnt<T>*>(reinterpret_cast<const char*>(tw) + d.tab_bytes);
     __syncthreads();
     int Ns = 1;
-    if constexpr (sizeof(T) == 4) {
-        if (d.E == kElemsFP32) {
-            // FP32 with 24 | M: 24 elements per thread, radix-8 passes
-            for (int p = 0; p < d.npass; ++p) {
-                const int R = d.radix[p];
-                switch (R) {
-                    case 2: fft_pass<2, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                    case 3: fft_pass<3, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                    case 4: fft_pass<4, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                    case 6: fft_pass<6, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                    case 8: fft_pass<8, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                    default: fft_pass<12, INV, VT, kElemsFP32>(buf, d.M, Ns, lane, d.Tg, tw); break;
-                }
-                Ns *= R;
-            }
-            return;
-        }
-    }
     for (int p = 0; p < d.npass; ++p) {
         const int R = d.radix[p];
         const int off = d.twoff[p];

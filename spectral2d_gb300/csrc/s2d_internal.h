@@ -22,7 +22,6 @@ namespace s2d {
 
 constexpr int kMaxPasses = 16;
 constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
-constexpr int kElemsFP32 = 24;        // FP32 when 24 | M: radix-8 passes in registers
 
 // Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
 // w_r = i^q_r * c_r * (1 + i t_r) with |t_r| <= 1, so that x*w_r costs two
@@ -45,8 +44,7 @@ struct Dims {
     int M;      // padded grid points per direction (3/2 rule)
     int ldS;    // compact column pitch (elements)
     int ldI;    // half-spectral row pitch (elements)
-    int Tg;     // threads per transform = M / E
-    int E;      // elements per thread: kElemsPerThread, or kElemsFP32
+    int Tg;     // threads per transform = M / kElemsPerThread
     int npass;  // FFT passes
     int radix[kMaxPasses];
     // per pass: offset (entries) of its TwEnt block, -1 if the pass uses the

@@ -67,7 +67,6 @@ bool plan_noalloc(int nx, Dims* d) {
     if (a % 2) d->radix[np++] = 2;
     for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
     d->npass = np;
-    d->E = kElemsPerThread;
     d->Tg = d->M / kElemsPerThread;
     return true;
 }
