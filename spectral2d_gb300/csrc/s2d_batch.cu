@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstddef>
 #include <cstring>
@@ -333,7 +334,7 @@ S2D_API int s2d_batch_create(int32_t nruns, const s2d_config* cfgs, s2d_batch** 
         b->runs.push_back(h);
     }
     {
-        static bool attr[64] = {false};
+        static std::atomic<bool> attr[64];  // per device, set once the attributes are (a second setter only repeats them)
         if (b->device >= 0 && b->device < 64 && !attr[b->device]) {
             const int dyn = b->max_smem - (int)sizeof(RunDev<double>) - 64;
             if (cudaFuncSetAttribute(k_batch_stage<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=

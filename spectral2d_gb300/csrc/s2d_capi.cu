@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -415,7 +416,7 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     h->max_smem = (int)prop.sharedMemPerBlockOptin - 1024;
     h->sms = prop.multiProcessorCount;
     {
-        static bool configured[64] = {false};
+        static std::atomic<bool> configured[64];  // per device, set once the attributes are (a second setter only repeats them)
         if (h->device >= 0 && h->device < 64 && !configured[h->device]) {
             if (configure_kernels(h->max_smem) != cudaSuccess)
                 return bail(fail(S2D_ERR_CUDA, "cudaFuncSetAttribute failed"));

@@ -29,6 +29,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -984,7 +985,7 @@ int state_to_phys(s2d_handle* h, const void* S, T* ow, T* op, bool with_psi) {
 }
 
 int ensure_les_buffers(s2d_handle* h) {
-    static bool attr[64] = {false};
+    static std::atomic<bool> attr[64];  // per device, set once the attributes are (a second setter only repeats them)
     if (h->device >= 0 && h->device < 64 && !attr[h->device]) {
         C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
         C_CUDA(cudaFuncSetAttribute(k_xinv_phys2<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, h->max_smem));
@@ -1132,7 +1133,7 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
     if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(cerr(S2D_ERR_CUDA, "stream creation failed"));
     {
-        static bool attr[64] = {false};
+        static std::atomic<bool> attr[64];  // per device, set once the attributes are (a second setter only repeats them)
         if (device >= 0 && device < 64 && !attr[device]) {
             const cudaFuncAttribute A = cudaFuncAttributeMaxDynamicSharedMemorySize;
             const bool set =
