@@ -373,7 +373,7 @@ def main():
     ap.add_argument("--workload", default="dns", choices=["dns", "ensemble", "les-batch"])
     ap.add_argument("--les-runs", type=int, default=256)
     ap.add_argument("--ens-check-steps", type=int, default=0)
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget", type=float, default=25.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -460,7 +460,8 @@ def main():
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 2 * nbytes,
                "steps": args.e2e_steps,
                "path": "s2d_integrate_one_step_host on pinned host arrays "
-                       "(reference-layout wC in: its retained modes; wC, psiC out)"}
+                       "(reference-layout wC in: its retained modes; wC, psiC out, their truncated "
+                       "part written from a second stream during the step)"}
 
     if rank == 0:
         line = {

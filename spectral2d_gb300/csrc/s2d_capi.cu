@@ -3,8 +3,10 @@
 // Host logic: grid setup (GetGridSize, src/Spectral.F90:117-219), FFT plans
 // and twiddle tables, device buffers, launch shapes, the RK3 step
 // (IntegrateOneStep, src/TimeIntegration.F90:130-210) as 9 kernel launches
-// (3 stages x {inverse y-pass, x-pass, forward y-pass + stage update}), its
-// CUDA graph, host I/O in the reference layout, diagnostics and initial
+// (3 stages x {inverse y-pass, x-pass, forward y-pass + stage update}; 12
+// when the forward y-pass and the stage update are split), its CUDA graph,
+// host I/O in the reference layout (the truncated part of an output array is
+// written on a second stream while the step runs), diagnostics and initial
 // conditions.  No framework types cross this boundary.
 #include "s2d.h"
 #include "s2d_internal.h"
@@ -16,6 +18,7 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -226,39 +229,131 @@ int ensure_ref_stage(s2d_handle* h) {
     return S2D_OK;
 }
 
+// A host array of a host-array call, as the kernels reach it: in place
+// through a device-usable address (page-locked memory; pageable memory where
+// the device reads the host page tables, as on Grace; device memory), or,
+// with dev null, through the staging arrays and copies.
+struct HostArray {
+    double* host = nullptr;
+    double* dev = nullptr;
+    bool pageable = false;   // in place through the host page tables
+};
+
+HostArray host_array(const s2d_handle* h, const double* p) {
+    HostArray a;
+    a.host = const_cast<double*>(p);
+    if (!p || h->io_copy_only) return a;
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return a;
+    }
+    if (at.type == cudaMemoryTypeHost) {
+        a.dev = (double*)at.devicePointer;
+    } else if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        if (at.device == h->device) a.dev = a.host;
+    } else if (h->pageable_direct) {
+        a.dev = a.host;
+        a.pageable = true;
+    }
+    return a;
+}
+
 // Only the retained rectangle of the reference array is read (kx <= K in rows
 // ky = 0..K and ky = -K..-1, i.e. rows 0..K and M-K..M-1): the rest is
-// truncated away, so it is not copied either.
-int upload_ref(s2d_handle* h, const double* wC) {
-    S2D_TRY(ensure_ref_stage(h));
-    const size_t pitch = (size_t)h->grid.cISize * 2 * sizeof(double);
-    const size_t width = (size_t)h->d.KX * 2 * sizeof(double);
-    const int K = h->d.K, M = h->d.M;
-    S2D_CUDA(cudaMemcpy2DAsync(h->ref_stage, pitch, wC, pitch, width, K + 1, cudaMemcpyHostToDevice, h->stream));
-    S2D_CUDA(cudaMemcpy2DAsync((char*)h->ref_stage + (size_t)(M - K) * pitch, pitch,
-                               (const char*)wC + (size_t)(M - K) * pitch, pitch, width, K, cudaMemcpyHostToDevice,
-                               h->stream));
+// truncated away, so it is neither read nor copied.
+int upload_ref(s2d_handle* h, const HostArray& w) {
+    const double* src = w.dev;
+    if (!src) {
+        S2D_TRY(ensure_ref_stage(h));
+        const size_t pitch = (size_t)h->grid.cISize * 2 * sizeof(double);
+        const size_t width = (size_t)h->d.KX * 2 * sizeof(double);
+        const size_t lo = (size_t)(h->d.M - h->d.K) * pitch;
+        const int K = h->d.K;
+        S2D_CUDA(cudaMemcpy2DAsync(h->ref_stage, pitch, w.host, pitch, width, K + 1, cudaMemcpyDefault,
+                                   h->stream));
+        S2D_CUDA(cudaMemcpy2DAsync((char*)h->ref_stage + lo, pitch, (const char*)w.host + lo, pitch, width, K,
+                                   cudaMemcpyDefault, h->stream));
+        src = h->ref_stage;
+    }
     if (h->prec == S2D_FP64)
-        S2D_CUDA(Kern<double>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
+        S2D_CUDA(Kern<double>::rect_to_compact(h->d, src, h->grid.cISize, h->S0, h->stream));
     else
-        S2D_CUDA(Kern<float>::ref_to_compact(h->d, h->ref_stage, h->grid.cISize, h->S0, h->stream));
+        S2D_CUDA(Kern<float>::rect_to_compact(h->d, src, h->grid.cISize, h->S0, h->stream));
     return S2D_OK;
 }
 
-int download_ref(s2d_handle* h, const void* S, double* wC, double* psiC) {
-    if (!wC && !psiC) return S2D_OK;
-    S2D_TRY(ensure_ref_stage(h));
-    double* dW = h->ref_stage;
-    double* dP = (double*)((char*)h->ref_stage + h->ref_bytes);
+// Outputs in the reference layout are zero outside the retained rectangle
+// (Truncate, src/Spectral.F90:788-802): columns kx > K of rows 0..K and
+// M-K..M-1, and the whole rows K+1..M-K-1.  That part does not depend on the
+// state, so it is written on the handle's second stream, which a host-array
+// step issues before the step and so overlaps with it: by a small kernel for
+// pageable arrays reached in place (a copy into pageable memory may hold the
+// host until it ends), else by copies from a device buffer of zeros.
+int send_zeros(s2d_handle* h, const HostArray& a, const HostArray& b) {
+    if (!a.host && !b.host) return S2D_OK;
+    const int K = h->d.K, M = h->d.M, C = h->grid.cISize;
+    if (!h->xstream) S2D_CUDA(cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking));
+    if (a.pageable || b.pageable)
+        S2D_CUDA(launch_zero_truncated(h->d, C, a.pageable ? a.dev : nullptr, b.pageable ? b.dev : nullptr, 48,
+                                       h->xstream));
+    const size_t pitch = (size_t)C * 2 * sizeof(double);
+    const size_t kx_off = (size_t)h->d.KX * 2 * sizeof(double);
+    const size_t tail = pitch - kx_off;                       // columns K+1..C-1 of one row
+    const size_t mid = (size_t)(M - 2 * K - 1) * pitch;       // rows K+1..M-K-1
+    for (const HostArray* x : {&a, &b}) {
+        if (!x->host || x->pageable) continue;
+        if (!h->zeros) {
+            h->zeros_bytes = std::max(mid, tail);
+            S2D_CUDA(cudaMalloc(&h->zeros, h->zeros_bytes));
+            S2D_CUDA(cudaMemsetAsync(h->zeros, 0, h->zeros_bytes, h->xstream));
+        }
+        char* c = (char*)x->host;
+        S2D_CUDA(cudaMemcpy2DAsync(c + kx_off, pitch, h->zeros, tail, tail, K + 1, cudaMemcpyDefault,
+                                   h->xstream));
+        S2D_CUDA(cudaMemcpy2DAsync(c + (size_t)(M - K) * pitch + kx_off, pitch, h->zeros, tail, tail, K,
+                                   cudaMemcpyDefault, h->xstream));
+        if (mid) S2D_CUDA(cudaMemcpyAsync(c + (size_t)(K + 1) * pitch, h->zeros, mid, cudaMemcpyDefault,
+                                          h->xstream));
+    }
+    return S2D_OK;
+}
+
+// Waits for the second stream on every exit of a host-array call, so that
+// no write into the caller's arrays is left in flight when it returns.
+struct CopyStreamJoin {
+    s2d_handle* h;
+    ~CopyStreamJoin() {
+        if (h->xstream) cudaStreamSynchronize(h->xstream);
+    }
+};
+
+// Reference-layout outputs: the retained rectangle written in place by the
+// conversion kernel, or into the staging arrays and copied; the rest by
+// send_zeros, which the caller issues first.
+int download_ref(s2d_handle* h, const void* S, const HostArray& w, const HostArray& p) {
+    if (!w.host && !p.host) return S2D_OK;
+    if ((w.host && !w.dev) || (p.host && !p.dev)) S2D_TRY(ensure_ref_stage(h));
+    double* dW = w.dev ? w.dev : (w.host ? h->ref_stage : nullptr);
+    double* dP = p.dev ? p.dev : (p.host ? (double*)((char*)h->ref_stage + h->ref_bytes) : nullptr);
     if (h->prec == S2D_FP64)
-        S2D_CUDA(Kern<double>::compact_to_ref(h->d, S, h->grid.cISize, wC ? dW : nullptr, psiC ? dP : nullptr,
-                                              h->stream));
+        S2D_CUDA(Kern<double>::compact_to_rect(h->d, S, h->grid.cISize, dW, dP, h->stream));
     else
-        S2D_CUDA(Kern<float>::compact_to_ref(h->d, S, h->grid.cISize, wC ? dW : nullptr, psiC ? dP : nullptr,
-                                             h->stream));
-    if (wC) S2D_CUDA(cudaMemcpyAsync(wC, dW, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
-    if (psiC) S2D_CUDA(cudaMemcpyAsync(psiC, dP, h->ref_bytes, cudaMemcpyDeviceToHost, h->stream));
+        S2D_CUDA(Kern<float>::compact_to_rect(h->d, S, h->grid.cISize, dW, dP, h->stream));
+    const size_t pitch = (size_t)h->grid.cISize * 2 * sizeof(double);
+    const size_t width = (size_t)h->d.KX * 2 * sizeof(double);
+    const size_t lo = (size_t)(h->d.M - h->d.K) * pitch;
+    const int K = h->d.K;
+    for (int f = 0; f < 2; ++f) {
+        const HostArray& x = f == 0 ? w : p;
+        if (!x.host || x.dev) continue;
+        char* dst = (char*)x.host;
+        const char* src = (const char*)(f == 0 ? dW : dP);
+        S2D_CUDA(cudaMemcpy2DAsync(dst, pitch, src, pitch, width, K + 1, cudaMemcpyDefault, h->stream));
+        S2D_CUDA(cudaMemcpy2DAsync(dst + lo, pitch, src + lo, pitch, width, K, cudaMemcpyDefault, h->stream));
+    }
     S2D_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->xstream) S2D_CUDA(cudaStreamSynchronize(h->xstream));
     return S2D_OK;
 }
 
@@ -416,6 +511,14 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     h->max_smem = (int)prop.sharedMemPerBlockOptin - 1024;
     h->sms = prop.multiProcessorCount;
     {
+        const char* io = std::getenv("S2D_HOST_IO");
+        h->io_copy_only = io && std::strcmp(io, "copy") == 0;
+        int pageable = 0;
+        if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, h->device) != cudaSuccess)
+            pageable = 0;
+        h->pageable_direct = pageable == 1 && !h->io_copy_only;
+    }
+    {
         static std::atomic<bool> configured[64];  // per device, set once the attributes are (a second setter only repeats them)
         if (h->device >= 0 && h->device < 64 && !configured[h->device]) {
             if (configure_kernels(h->max_smem) != cudaSuccess)
@@ -519,9 +622,12 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
     void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->tw,  h->ref_stage,
-                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv};
+                    h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
+                    h->zeros};
+    if (h->xstream) cudaStreamSynchronize(h->xstream);
     for (void* p : ptrs)
         if (p) cudaFree(p);
+    if (h->xstream) cudaStreamDestroy(h->xstream);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
 }
@@ -530,7 +636,7 @@ S2D_API int s2d_set_state(s2d_handle* h, const double* wC, int32_t cISize, int32
     if (!h || !wC) return fail(S2D_ERR_INVALID, "null argument");
     S2D_TRY(check_ref_dims(h, cISize, nyG));
     S2D_CUDA(cudaSetDevice(h->device));
-    S2D_TRY(upload_ref(h, wC));
+    S2D_TRY(upload_ref(h, host_array(h, wC)));
     S2D_CUDA(cudaStreamSynchronize(h->stream));
     return S2D_OK;
 }
@@ -539,7 +645,10 @@ S2D_API int s2d_get_state(s2d_handle* h, double* wC, double* psiC, int32_t cISiz
     if (!h) return fail(S2D_ERR_INVALID, "null handle");
     S2D_TRY(check_ref_dims(h, cISize, nyG));
     S2D_CUDA(cudaSetDevice(h->device));
-    return download_ref(h, h->S0, wC, psiC);
+    CopyStreamJoin join{h};
+    const HostArray w = host_array(h, wC), p = host_array(h, psiC);
+    S2D_TRY(send_zeros(h, w, p));
+    return download_ref(h, h->S0, w, p);
 }
 
 S2D_API int s2d_integrate_one_step(s2d_handle* h, double dt) {
@@ -564,9 +673,12 @@ S2D_API int s2d_integrate_one_step_host(s2d_handle* h, double* wC, double* psiC,
     if (!h || !wC) return fail(S2D_ERR_INVALID, "null argument");
     S2D_TRY(check_ref_dims(h, cISize, nyG));
     S2D_CUDA(cudaSetDevice(h->device));
-    S2D_TRY(upload_ref(h, wC));
+    CopyStreamJoin join{h};
+    const HostArray w = host_array(h, wC), p = host_array(h, psiC);
+    S2D_TRY(send_zeros(h, w, p));  // only the truncated part: disjoint from the rectangle read in
+    S2D_TRY(upload_ref(h, w));
     S2D_TRY(launch_step(h, dt));
-    return download_ref(h, h->S0, wC, psiC);
+    return download_ref(h, h->S0, w, p);
 }
 
 S2D_API int s2d_compute_rhs(s2d_handle* h, double* dW, int32_t cISize, int32_t nyG) {
@@ -574,8 +686,11 @@ S2D_API int s2d_compute_rhs(s2d_handle* h, double* dW, int32_t cISize, int32_t n
     S2D_TRY(check_ref_dims(h, cISize, nyG));
     S2D_CUDA(cudaSetDevice(h->device));
     if (!h->Sdw) S2D_CUDA(cudaMalloc(&h->Sdw, (size_t)h->d.KX * h->d.ldS * h->vsz));
+    CopyStreamJoin join{h};
+    const HostArray x = host_array(h, dW);
+    S2D_TRY(send_zeros(h, x, HostArray{}));
     S2D_TRY(launch_rhs_stage_any(h, 0, 0.0, nullptr));
-    return download_ref(h, h->Sdw, dW, nullptr);
+    return download_ref(h, h->Sdw, x, HostArray{});
 }
 
 S2D_API int s2d_spectrum_bins(const s2d_handle* h) {

@@ -111,6 +111,11 @@ struct Kern {
                                       cudaStream_t st);
     static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
                                       double* refPsi, cudaStream_t st);
+    // the retained rectangle only, by 32 x 32 tiles (ref may be a host array
+    // the device reaches directly)
+    static cudaError_t rect_to_compact(const Dims& d, const double* ref, int C, void* S, cudaStream_t st);
+    static cudaError_t compact_to_rect(const Dims& d, const void* S, int C, double* refW, double* refPsi,
+                                       cudaStream_t st);
     static cudaError_t spectrum(const Dims& d, const void* S, double* Ek, cudaStream_t st);
     static cudaError_t enstrophy_partial(const Dims& d, const void* S, double* part, int nblocks,
                                          cudaStream_t st);
@@ -165,6 +170,16 @@ struct s2d_handle {
     double* dscratch = nullptr;           // spectrum / partial sums
     size_t dscratch_n = 0;
     void* Fv = nullptr;   // FP64 Basdevant: second compact array of the split K3 (the first is I[2])
+    // host-array calls: the truncated part of an output array (outside the
+    // retained rectangle) is copied from this buffer of zeros on xstream,
+    // concurrently with the step on stream
+    void* zeros = nullptr;
+    size_t zeros_bytes = 0;
+    cudaStream_t xstream = nullptr;
+    // kernels may read and write pageable host arrays in place (the device
+    // reads the host page tables); false also when S2D_HOST_IO=copy
+    bool pageable_direct = false;
+    bool io_copy_only = false;   // S2D_HOST_IO=copy: every host array through copies
     s2d::Launch L_yinv, L_xpass, L_yfwd, L_xrow, L_ystore, L_ycol;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
@@ -206,5 +221,9 @@ int set_error(int code, const char* msg);
 int handle_nx(const s2d_handle* h);
 
 cudaError_t launch_fp64_probe(double* sink, int blocks, int threads, int iters, cudaStream_t st);
+
+// Zeros of the truncated part (outside the retained rectangle) of one or two
+// reference-layout arrays a, b (either may be null), blocks x 2 CTAs.
+cudaError_t launch_zero_truncated(const Dims& d, int C, double* a, double* b, int blocks, cudaStream_t st);
 
 }  // namespace s2d

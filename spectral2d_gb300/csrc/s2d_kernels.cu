@@ -180,6 +180,100 @@ __global__ void k_compact_to_ref(Dims d, const typename Vec<T>::t* __restrict__ 
 }
 
 // ------------------------------------------------------------------------
+// Host-array I/O of the retained rectangle (kx <= K, |ky| <= K; row n = ky
+// mod M, pitch C) through 32 x 32 tiles in shared memory, so that both the
+// compact columns and the reference rows are read and written in 512-byte
+// runs.  ref may be the caller's host array itself (page-locked, or pageable
+// memory reached through the host page tables), where scattered 16-byte
+// accesses would each cost a transaction on the host link.
+// ------------------------------------------------------------------------
+constexpr int kIoTile = 32;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_rect_to_compact(Dims d, const double2* __restrict__ ref, int C,
+                                                         typename Vec<T>::t* __restrict__ S) {
+    using VT = typename Vec<T>::t;
+    __shared__ double2 tile[kIoTile][kIoTile + 1];
+    const int kx0 = blockIdx.x * kIoTile, jc0 = blockIdx.y * kIoTile;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int i = ty; i < kIoTile; i += 8) {
+        const int jc = jc0 + i, kx = kx0 + tx;
+        double2 v = make_double2(0.0, 0.0);
+        if (jc < d.KY && kx < d.KX) {
+            const int ky = ky_of_jc(d, jc);
+            if (kx * kx + ky * ky <= d.K * d.K) v = ref[(size_t)(ky >= 0 ? ky : ky + d.M) * C + kx];
+        }
+        tile[i][tx] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < kIoTile; i += 8) {
+        const int kx = kx0 + i, jc = jc0 + tx;
+        if (kx < d.KX && jc < d.KY) {
+            const double2 v = tile[tx][i];
+            S[(size_t)kx * d.ldS + jc] = mk<VT>((T)v.x, (T)v.y);
+        }
+    }
+}
+
+// omega and psi = omega / (kx^2 + ky^2), psi(0,0) = 0 (src/Spectral.F90:508-560)
+// on the rectangle; either output may be null.
+template <typename T>
+__global__ void __launch_bounds__(256) k_compact_to_rect(Dims d, const typename Vec<T>::t* __restrict__ S, int C,
+                                                         double2* refW, double2* refPsi) {
+    __shared__ double2 tile[kIoTile][kIoTile + 1];
+    const int kx0 = blockIdx.x * kIoTile, jc0 = blockIdx.y * kIoTile;
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    for (int i = ty; i < kIoTile; i += 8) {
+        const int kx = kx0 + i, jc = jc0 + tx;
+        double2 v = make_double2(0.0, 0.0);
+        if (kx < d.KX && jc < d.KY) {
+            const auto s = S[(size_t)kx * d.ldS + jc];
+            v = make_double2((double)s.x, (double)s.y);
+        }
+        tile[i][tx] = v;
+    }
+    __syncthreads();
+    for (int i = ty; i < kIoTile; i += 8) {
+        const int jc = jc0 + i, kx = kx0 + tx;
+        if (jc < d.KY && kx < d.KX) {
+            const int ky = ky_of_jc(d, jc);
+            const size_t o = (size_t)(ky >= 0 ? ky : ky + d.M) * C + kx;
+            const double2 w = tile[tx][i];
+            if (refW) refW[o] = w;
+            if (refPsi) {
+                const double k2 = (double)kx * kx + (double)ky * ky;
+                refPsi[o] = (k2 == 0.0) ? make_double2(0.0, 0.0) : make_double2(w.x / k2, w.y / k2);
+            }
+        }
+    }
+}
+
+// Zeros of the truncated part of a reference array (blockIdx.y selects a or
+// b): columns kx > K of the rectangle's rows, then rows K+1..M-K-1 whole.
+__global__ void __launch_bounds__(256) k_zero_truncated(Dims d, int C, double2* a, double2* b) {
+    double2* p = blockIdx.y == 0 ? a : b;
+    if (!p) return;
+    const int w = C - d.KX;
+    const long strip = (long)d.KY * w;
+    const long total = strip + (long)(d.M - d.KY) * C;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        size_t o;
+        if (i < strip) {
+            const int r = (int)i / w, c = (int)i - ((int)i / w) * w;
+            o = (size_t)(r <= d.K ? r : r - d.KY + d.M) * C + d.KX + c;
+        } else {
+            o = (size_t)(d.K + 1) * C + (size_t)(i - strip);
+        }
+        p[o] = make_double2(0.0, 0.0);
+    }
+}
+
+cudaError_t launch_zero_truncated(const Dims& d, int C, double* a, double* b, int blocks, cudaStream_t st) {
+    k_zero_truncated<<<dim3(blocks, 2), 256, 0, st>>>(d, C, (double2*)a, (double2*)b);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------
 // Diagnostics
 // ------------------------------------------------------------------------
 __device__ __forceinline__ int isqrt_floor(int c) {
@@ -552,6 +646,23 @@ template <typename T>
 cudaError_t Kern<T>::ref_to_compact(const Dims& d, const double* ref, int C, void* S, cudaStream_t st) {
     using VT = typename Vec<T>::t;
     k_ref_to_compact<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const double2*)ref, C, (VT*)S);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::rect_to_compact(const Dims& d, const double* ref, int C, void* S, cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    const dim3 grid((d.KX + kIoTile - 1) / kIoTile, (d.KY + kIoTile - 1) / kIoTile);
+    k_rect_to_compact<T><<<grid, 256, 0, st>>>(d, (const double2*)ref, C, (VT*)S);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::compact_to_rect(const Dims& d, const void* S, int C, double* refW, double* refPsi,
+                                     cudaStream_t st) {
+    using VT = typename Vec<T>::t;
+    const dim3 grid((d.KX + kIoTile - 1) / kIoTile, (d.KY + kIoTile - 1) / kIoTile);
+    k_compact_to_rect<T><<<grid, 256, 0, st>>>(d, (const VT*)S, C, (double2*)refW, (double2*)refPsi);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@ import numpy as np
 import pytest
 
 import oracle as O
+from spectral2d_gb300 import _lib as L
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -180,6 +181,54 @@ def test_host_array_step_equals_device_step(S2D):
         s.integrate_one_step(1e-3)
         w2, p2 = s.get_state()
     assert np.array_equal(w1, w2) and np.array_equal(p1, p2)
+
+
+def _host_buf(shape, mem):
+    from spectral2d_gb300.solver import pinned_array
+    a = pinned_array(shape) if mem == "pinned" else np.empty(shape, dtype=np.complex128)
+    a[...] = np.nan + 1j * np.nan
+    return a
+
+
+@pytest.mark.parametrize("n", [8, 96])
+@pytest.mark.parametrize("mem", ["pageable", "pinned"])
+@pytest.mark.parametrize("io", ["in_place", "copy"])
+def test_host_array_io_paths(S2D, n, mem, io, monkeypatch):
+    """Host-array calls on pageable and page-locked arrays, read and written
+    in place by the kernels or (S2D_HOST_IO=copy) through staging copies: the
+    truncated part of every output is zero whatever the array held, the
+    truncated part of the input is not read, and all paths give the same bits
+    as the device-resident step."""
+    from spectral2d_gb300.solver import _dptr
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 5, decay=0.1)
+    K, M = n // 2, g.nyG
+    keep = np.zeros(w.shape, dtype=bool)
+    keep[: K + 1, : K + 1] = True
+    keep[M - K:, : K + 1] = True
+    with S2D(n, nu=0.01) as r:
+        r.set_state(w)
+        dW_ref = r.compute_rhs()
+        r.integrate_one_step(1e-3)
+        w_ref, p_ref = r.get_state()
+    if io == "copy":
+        monkeypatch.setenv("S2D_HOST_IO", "copy")
+    with S2D(n, nu=0.01) as s:
+        ny, cx = w.shape
+        wh = _host_buf(w.shape, mem)
+        wh[keep] = w[keep]
+        ph = _host_buf(w.shape, mem)
+        s.set_state(wh)                     # reads the rectangle only
+        dh = _host_buf(w.shape, mem)
+        L.check(s._L.s2d_compute_rhs(s._h, _dptr(dh.view(np.float64)), cx, ny))
+        s.integrate_one_step_host(wh, 1e-3, ph, inplace=True)
+        gw, gp = _host_buf(w.shape, mem), _host_buf(w.shape, mem)
+        L.check(s._L.s2d_get_state(s._h, _dptr(gw.view(np.float64)), _dptr(gp.view(np.float64)), cx, ny))
+    for a in (wh, ph, dh, gw, gp):
+        assert not (a[~keep] != 0).any()
+    assert np.array_equal(dh, dW_ref)
+    assert np.array_equal(wh, w_ref) and np.array_equal(ph, p_ref)
+    assert np.array_equal(gw, w_ref) and np.array_equal(gp, p_ref)
 
 
 def test_spectrum_minmax_enstrophy_vs_oracle(S2D):
