@@ -31,12 +31,16 @@ namespace s2d {
 
 // ------------------------------------------------------------------------
 // K1, K2, K3 of one simulation: one tile per CTA (bodies in s2d_step.cuh).
-// K1 and K2 come in two register budgets: LB3 = CTAs of at most 256 threads,
-// three per SM (80 registers: a third CTA fills the barrier phases of the
-// other two), and the general one (up to 512 threads, M = 6144).
+// K1, K2 and the split K3 come in two register budgets: LB > 0 = CTAs of at
+// most 256 threads, LB of them per SM (FP64: three, 80 registers, a third
+// CTA fills the barrier phases of the other two; FP32: four, 64 registers),
+// and the general one (LB = 0: up to 512 threads, M = 6144).
 // ------------------------------------------------------------------------
-template <typename T, bool LB3>
-__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
+template <typename T>
+constexpr int kMinBlocks256 = sizeof(T) == 8 ? 3 : 4;
+
+template <typename T, int LB>
+__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
                                                const double* __restrict__ rk2, FieldSet fs,
                                                const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -44,8 +48,8 @@ __global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1) k_yinv(Dims d, c
     yinv_body<T>(d, S, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
-template <typename T, bool LB3>
-__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+template <typename T, int LB>
+__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
     using VT = typename Vec<T>::t;
@@ -70,8 +74,8 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
 
 // K3 split in two (FP64 single runs): forward y-FFT of one field's columns
 // into a compact array, then the epilogue of every mode.
-template <typename T, bool LB3>
-__global__ void __launch_bounds__(LB3 ? 256 : 512, LB3 ? 3 : 1)
+template <typename T, int LB>
+__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1)
     k_yfwd_col(Dims d, const typename Vec<T>::t* __restrict__ Iu, const typename Vec<T>::t* __restrict__ Iv,
                typename Vec<T>::t* Fu, typename Vec<T>::t* Fv, const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -575,10 +579,10 @@ cudaError_t Kern<T>::yinv(const Dims& d, const void* S, const double* rk2, const
                           cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
-    if (sizeof(T) == 8 && L.threads <= 256)
-        k_yinv<T, true><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    if (L.threads <= 256)
+        k_yinv<T, kMinBlocks256<T>><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
     else
-        k_yinv<T, false><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+        k_yinv<T, 0><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
     return cudaGetLastError();
 }
 
@@ -598,11 +602,11 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
                                const Launch& L) {
     using VT = typename Vec<T>::t;
     const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
-    if (sizeof(T) == 8 && L.threads <= 256)
-        k_xpass_bas<T, true><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
+    if (L.threads <= 256)
+        k_xpass_bas<T, kMinBlocks256<T>><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
                                                                                 (const VT*)tw, L.G, scale);
     else
-        k_xpass_bas<T, false><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
+        k_xpass_bas<T, 0><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
                                                                                  (const VT*)tw, L.G, scale);
     return cudaGetLastError();
 }
@@ -623,11 +627,11 @@ cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, voi
                               cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
-    if (sizeof(T) == 8 && L.threads <= 256)
-        k_yfwd_col<T, true><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
+    if (L.threads <= 256)
+        k_yfwd_col<T, kMinBlocks256<T>><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
                                                                (const VT*)tw, L.G);
     else
-        k_yfwd_col<T, false><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
+        k_yfwd_col<T, 0><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
                                                                 (const VT*)tw, L.G);
     return cudaGetLastError();
 }
@@ -768,20 +772,20 @@ cudaError_t configure_kernels(int max_smem_optin) {
         cudaError_t e2 = set_smem(k, max_smem_optin);       \
         if (e2 != cudaSuccess && e == cudaSuccess) e = e2;  \
     } while (0)
-    S2D_SET((k_yinv<double, true>));
-    S2D_SET((k_yinv<double, false>));
-    S2D_SET((k_yinv<float, true>));
-    S2D_SET((k_yinv<float, false>));
+    S2D_SET((k_yinv<double, kMinBlocks256<double>>));
+    S2D_SET((k_yinv<double, 0>));
+    S2D_SET((k_yinv<float, kMinBlocks256<float>>));
+    S2D_SET((k_yinv<float, 0>));
     S2D_SET(k_xpass_rhs<double>);
     S2D_SET(k_xpass_rhs<float>);
-    S2D_SET((k_xpass_bas<double, true>));
-    S2D_SET((k_xpass_bas<double, false>));
-    S2D_SET((k_xpass_bas<float, true>));
-    S2D_SET((k_xpass_bas<float, false>));
-    S2D_SET((k_yfwd_col<double, true>));
-    S2D_SET((k_yfwd_col<double, false>));
-    S2D_SET((k_yfwd_col<float, true>));
-    S2D_SET((k_yfwd_col<float, false>));
+    S2D_SET((k_xpass_bas<double, kMinBlocks256<double>>));
+    S2D_SET((k_xpass_bas<double, 0>));
+    S2D_SET((k_xpass_bas<float, kMinBlocks256<float>>));
+    S2D_SET((k_xpass_bas<float, 0>));
+    S2D_SET((k_yfwd_col<double, kMinBlocks256<double>>));
+    S2D_SET((k_yfwd_col<double, 0>));
+    S2D_SET((k_yfwd_col<float, kMinBlocks256<float>>));
+    S2D_SET((k_yfwd_col<float, 0>));
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
     S2D_SET(k_xinv_cfl<double>);

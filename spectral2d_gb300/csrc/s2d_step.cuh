@@ -87,7 +87,11 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
 
     const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
     const double* rcol = rk2 + (size_t)(active ? kx : 0) * d.ldS;
-    for (int n = lane; n < d.M; n += d.Tg) {
+    // M = kElemsPerThread * Tg: a fixed trip count lets every load of the
+    // column be in flight at once (the loads are latency-bound)
+#pragma unroll
+    for (int i = 0; i < kElemsPerThread; ++i) {
+        const int n = lane + i * d.Tg;
         VT val = mk<VT>((T)0, (T)0);
         int jc = -1, ky = 0;
         if (n <= d.K) {
@@ -118,7 +122,11 @@ template <typename VT>
 __device__ __forceinline__ void build_pair(VT* buf, const VT* __restrict__ X, const VT* __restrict__ Y,
                                            const Dims& d, int lane, bool active) {
     using T = decltype(buf[0].x);
-    for (int n = lane; n < d.M; n += d.Tg) {
+    // M = kElemsPerThread * Tg; all loads in flight for FP32 (FP64 K2 would
+    // spill at its 80-register budget)
+#pragma unroll(sizeof(T) == 8 ? 1 : kElemsPerThread)
+    for (int i = 0; i < kElemsPerThread; ++i) {
+        const int n = lane + i * d.Tg;
         VT z = mk<VT>((T)0, (T)0);
         if (active) {
             if (n == 0) {
@@ -244,6 +252,46 @@ __device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx
     return bad;
 }
 
+// Columns kx0 .. kx0+G-1 of the half-spectral rows of one or two fields
+// (X, then Y) into bufs[(field * G + gg) * M + y], zero past gtot; n =
+// G * M elements of X alone, 2 G M of both.  One element per row is a
+// strided gather, so each thread keeps kU loads in flight before it
+// stores them.
+template <typename T>
+__device__ __forceinline__ void gather_columns(const Dims& d, const typename Vec<T>::t* __restrict__ X,
+                                               const typename Vec<T>::t* __restrict__ Y, int G, int gtot, int kx0,
+                                               int n, typename Vec<T>::t* bufs) {
+    using VT = typename Vec<T>::t;
+    constexpr int kU = sizeof(T) == 8 ? 4 : 8;
+    for (int base = threadIdx.x; base < n; base += kU * blockDim.x) {
+        VT v[kU];
+        int dst[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            const int idx = base + u * blockDim.x;
+            v[u] = mk<VT>((T)0, (T)0);
+            dst[u] = -1;
+            if (idx < n) {
+                int gg = 0, y, fld;
+                if (G == 1) {
+                    fld = idx >= d.M;
+                    y = idx - fld * d.M;
+                } else {
+                    gg = idx % G;
+                    const int rest = idx / G;
+                    y = rest % d.M;
+                    fld = rest / d.M;
+                }
+                dst[u] = (fld * G + gg) * d.M + y;
+                if (gg < gtot) v[u] = __ldcg(&(fld ? Y : X)[(size_t)y * d.ldI + kx0 + gg]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u)
+            if (dst[u] >= 0) bufs[dst[u]] = v[u];
+    }
+}
+
 // K3 split in two for a third CTA per SM (the single-run FP64 path): the
 // forward y-FFT of one field's columns, its retained rows stored in the
 // compact layout (Out[kx][jc])...
@@ -261,11 +309,7 @@ __device__ __forceinline__ void yfwd_col_body(const Dims& d, const typename Vec<
     const int gtot = min(G, d.KX - kx0);
     const VT* I = f ? Iv : Iu;
     VT* Out = f ? OutV : OutU;
-    for (int idx = threadIdx.x; idx < G * d.M; idx += blockDim.x) {
-        const int gg = idx % G;
-        const int y = idx / G;
-        bufs[(size_t)gg * d.M + y] = gg < gtot ? __ldcg(&I[(size_t)y * d.ldI + kx0 + gg]) : mk<VT>((T)0, (T)0);
-    }
+    gather_columns<T>(d, I, I, G, gtot, kx0, G * d.M, bufs);
     fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
     __syncthreads();
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
@@ -321,15 +365,7 @@ __device__ __forceinline__ bool yfwd_body(const Dims& d, const typename Vec<T>::
     const int kx0 = blk * G;
     const int gtot = min(G, d.KX - kx0);
 
-    for (int idx = threadIdx.x; idx < 2 * G * d.M; idx += blockDim.x) {
-        const int gg = idx % G;
-        const int rest = idx / G;
-        const int y = rest % d.M;
-        const int fld = rest / d.M;
-        VT v = mk<VT>((T)0, (T)0);
-        if (gg < gtot) v = __ldcg(&(fld ? Iv : Iu)[(size_t)y * d.ldI + kx0 + gg]);
-        bufs[(size_t)(fld * G + gg) * d.M + y] = v;
-    }
+    gather_columns<T>(d, Iu, Iv, G, gtot, kx0, 2 * G * d.M, bufs);
     const int nconc = blockDim.x / d.Tg;
     for (int t0 = 0; t0 < 2 * G; t0 += nconc) fft_run<false>(bufs + (size_t)(t0 + t) * d.M, d, lane, tw);
     __syncthreads();
