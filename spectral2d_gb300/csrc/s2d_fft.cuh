@@ -121,6 +121,19 @@ __device__ __forceinline__ void butterfly(VT* v) {
     else bf4<INV>(v);
 }
 
+// j mod Ns by a multiply-high: q = floor(j mg / 2^32) with mg = ceil(2^32 /
+// Ns) is floor(j / Ns) exactly while j (mg Ns - 2^32) < 2^32, i.e. for every
+// j < 2^32 / Ns (here j < M <= 6144).  One reciprocal per pass instead of an
+// integer division per butterfly (the FP32 passes are issue-bound).
+struct ModNs {
+    int Ns;
+    unsigned mg;
+    __device__ __forceinline__ explicit ModNs(int ns) : Ns(ns), mg(ns > 1 ? 0xFFFFFFFFu / (unsigned)ns + 1u : 0u) {}
+    __device__ __forceinline__ int operator()(int j) const {
+        return Ns == 1 ? 0 : j - (int)__umulhi((unsigned)j, mg) * Ns;
+    }
+};
+
 // One in-place Stockham pass of radix R over the transform in buf.
 template <int R, bool INV, typename VT>
 __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int Tg,
@@ -136,10 +149,11 @@ __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int T
     }
     __syncthreads();
     const int tstep = M / (Ns * R);
+    const ModNs mod(Ns);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
-        const int k = j % Ns;
+        const int k = mod(j);
         if (Ns > 1) {
             const int ts = k * tstep;
 #pragma unroll
@@ -253,10 +267,11 @@ __device__ __forceinline__ void fft_pass4_fma(VT* buf, int M, int Ns, int lane, 
         for (int r = 0; r < 4; ++r) v[b][r] = buf[j + r * stride];
     }
     __syncthreads();
+    const ModNs mod(Ns);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
-        const int k = j % Ns;
+        const int k = mod(j);
         const TwEnt<T> e = tab[k];
         const VT a = v[b][0];
         const VT B = tw_fma<INV>(v[b][1], e.t1, e.q & 3);
@@ -306,10 +321,11 @@ __device__ __forceinline__ void fft_pass2_fma(VT* buf, int M, int Ns, int lane, 
         v[b][1] = buf[j + stride];
     }
     __syncthreads();
+    const ModNs mod(Ns);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
-        const int k = j % Ns;
+        const int k = mod(j);
         const T t1 = tab[k].t1, c1 = tab[k].c1;
         const int q = tab[k].q;
         const VT a = v[b][0];
