@@ -134,6 +134,7 @@ bool factor_plan(int M, Dims* d) {
     for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
     if (np > kMaxPasses) return false;
     d->npass = np;
+    set_pass_constants(d);
     return true;
 }
 

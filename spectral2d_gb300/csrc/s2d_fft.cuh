@@ -122,13 +122,14 @@ __device__ __forceinline__ void butterfly(VT* v) {
 }
 
 // j mod Ns by a multiply-high: q = floor(j mg / 2^32) with mg = ceil(2^32 /
-// Ns) is floor(j / Ns) exactly while j (mg Ns - 2^32) < 2^32, i.e. for every
-// j < 2^32 / Ns (here j < M <= 6144).  One reciprocal per pass instead of an
-// integer division per butterfly (the FP32 passes are issue-bound).
+// Ns) (Dims::mg, set on the host) is floor(j / Ns) exactly while
+// j (mg Ns - 2^32) < 2^32, i.e. for every j < 2^32 / Ns (here j < M <= 6144).
+// No integer division on the device: on GB300 it competes with the FP64
+// pipe (the FP64 step ran 3 % faster without one per butterfly).
 struct ModNs {
     int Ns;
     unsigned mg;
-    __device__ __forceinline__ explicit ModNs(int ns) : Ns(ns), mg(ns > 1 ? 0xFFFFFFFFu / (unsigned)ns + 1u : 0u) {}
+    __device__ __forceinline__ ModNs(int ns, unsigned m) : Ns(ns), mg(m) {}
     __device__ __forceinline__ int operator()(int j) const {
         return Ns == 1 ? 0 : j - (int)__umulhi((unsigned)j, mg) * Ns;
     }
@@ -136,7 +137,7 @@ struct ModNs {
 
 // One in-place Stockham pass of radix R over the transform in buf.
 template <int R, bool INV, typename VT>
-__device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int Tg,
+__device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, unsigned mg, int tstep, int lane, int Tg,
                                          const VT* __restrict__ tw) {
     constexpr int NB = kElemsPerThread / R;
     VT v[NB][R];
@@ -148,8 +149,7 @@ __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, int lane, int T
         for (int r = 0; r < R; ++r) v[b][r] = buf[j + r * stride];
     }
     __syncthreads();
-    const int tstep = M / (Ns * R);
-    const ModNs mod(Ns);
+    const ModNs mod(Ns, mg);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
@@ -255,7 +255,7 @@ __device__ __forceinline__ VT tw_fma(VT x, T t, int q) {
 // Radix-4 Stockham pass with FMA-form twiddles (Ns > 1): 22 FP64
 // instructions per butterfly instead of 12 (3 complex products) + 16.
 template <bool INV, typename VT, typename T>
-__device__ __forceinline__ void fft_pass4_fma(VT* buf, int M, int Ns, int lane, int Tg,
+__device__ __forceinline__ void fft_pass4_fma(VT* buf, int M, int Ns, unsigned mg, int lane, int Tg,
                                               const TwEnt<T>* __restrict__ tab) {
     constexpr int NB = kElemsPerThread / 4;
     VT v[NB][4];
@@ -267,7 +267,7 @@ __device__ __forceinline__ void fft_pass4_fma(VT* buf, int M, int Ns, int lane, 
         for (int r = 0; r < 4; ++r) v[b][r] = buf[j + r * stride];
     }
     __syncthreads();
-    const ModNs mod(Ns);
+    const ModNs mod(Ns, mg);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
@@ -309,7 +309,7 @@ __device__ __forceinline__ void fft_pass4_fma(VT* buf, int M, int Ns, int lane, 
 
 // Radix-2 Stockham pass with an FMA-form twiddle (Ns > 1): y = a +- c1 B.
 template <bool INV, typename VT, typename T>
-__device__ __forceinline__ void fft_pass2_fma(VT* buf, int M, int Ns, int lane, int Tg,
+__device__ __forceinline__ void fft_pass2_fma(VT* buf, int M, int Ns, unsigned mg, int lane, int Tg,
                                               const TwEnt<T>* __restrict__ tab) {
     constexpr int NB = kElemsPerThread / 2;
     VT v[NB][2];
@@ -321,7 +321,7 @@ __device__ __forceinline__ void fft_pass2_fma(VT* buf, int M, int Ns, int lane, 
         v[b][1] = buf[j + stride];
     }
     __syncthreads();
-    const ModNs mod(Ns);
+    const ModNs mod(Ns, mg);
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
         const int j = lane + b * Tg;
@@ -357,16 +357,17 @@ __device__ __forceinline__ void fft_run(VT* buf, const Dims& d, int lane, const 
     for (int p = 0; p < d.npass; ++p) {
         const int R = d.radix[p];
         const int off = d.twoff[p];
+        const unsigned mg = d.mg[p];
         if (INV && p == 0 && R == 3 && 3 * d.K == d.M) {
             fft_pass3_midzero<INV>(buf, d.M, lane, d.Tg);
         } else if (R == 4) {
-            if (off >= 0) fft_pass4_fma<INV>(buf, d.M, Ns, lane, d.Tg, tab + off);
-            else fft_pass<4, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+            if (off >= 0) fft_pass4_fma<INV>(buf, d.M, Ns, mg, lane, d.Tg, tab + off);
+            else fft_pass<4, INV>(buf, d.M, Ns, mg, d.tstep[p], lane, d.Tg, tw);
         } else if (R == 2) {
-            if (off >= 0) fft_pass2_fma<INV>(buf, d.M, Ns, lane, d.Tg, tab + off);
-            else fft_pass<2, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+            if (off >= 0) fft_pass2_fma<INV>(buf, d.M, Ns, mg, lane, d.Tg, tab + off);
+            else fft_pass<2, INV>(buf, d.M, Ns, mg, d.tstep[p], lane, d.Tg, tw);
         } else {
-            fft_pass<3, INV>(buf, d.M, Ns, lane, d.Tg, tw);
+            fft_pass<3, INV>(buf, d.M, Ns, mg, d.tstep[p], lane, d.Tg, tw);
         }
         Ns *= R;
     }

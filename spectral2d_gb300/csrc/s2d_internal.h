@@ -51,7 +51,21 @@ struct Dims {
     // plain complex table (first pass, or a radix-3 pass after the first)
     int twoff[kMaxPasses];
     long long tab_bytes;  // byte offset of the TwEnt table after the complex table
+    // per pass, with Ns the product of the earlier radices: ceil(2^32 / Ns)
+    // (0 for Ns = 1), for j mod Ns by a multiply-high, and M / (Ns R)
+    unsigned mg[kMaxPasses];
+    int tstep[kMaxPasses];
 };
+
+// mg[] and tstep[] of a plan whose M, npass and radix[] are set.
+inline void set_pass_constants(Dims* d) {
+    int ns = 1;
+    for (int p = 0; p < d->npass; ++p) {
+        d->mg[p] = ns > 1 ? 0xFFFFFFFFu / (unsigned)ns + 1u : 0u;
+        d->tstep[p] = d->M / (ns * d->radix[p]);
+        ns *= d->radix[p];
+    }
+}
 
 // Terms of dW beyond the reference's (drag and a Kolmogorov source).
 struct Phys {

@@ -641,7 +641,7 @@ cudaError_t Kern<T>::stage(const Dims& d, const void* Fu, const void* Fv, void* 
                            const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
                            cudaStream_t st) {
     using VT = typename Vec<T>::t;
-    k_stage<T><<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, (const VT*)Fu, (const VT*)Fv, (VT*)S0, (VT*)S1,
+    k_stage<T><<<dim3((d.KY + 255) / 256, d.KX), 256, 0, st>>>(d, (const VT*)Fu, (const VT*)Fv, (VT*)S0, (VT*)S1,
                                                                  (VT*)Sdw, (const VT*)src, stage, dt, ph, flags);
     return cudaGetLastError();
 }

@@ -67,6 +67,7 @@ bool plan_noalloc(int nx, Dims* d) {
     if (a % 2) d->radix[np++] = 2;
     for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
     d->npass = np;
+    set_pass_constants(d);
     d->Tg = d->M / kElemsPerThread;
     return true;
 }

@@ -108,10 +108,14 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
 
     VT* out = reinterpret_cast<VT*>(outp);
     const int gtot = min(G, d.KX - kx0);
-    for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
-        const int y = idx / G;
-        const int gg = idx - y * G;
-        if (gg < gtot) out[(size_t)y * d.ldI + kx0 + gg] = bufs[(size_t)gg * d.M + y];
+    if (G == 1) {   // no integer division per element (it competes with the FP64 pipe)
+        for (int y = threadIdx.x; y < d.M; y += blockDim.x) out[(size_t)y * d.ldI + kx0] = bufs[y];
+    } else {
+        for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
+            const int y = idx / G;
+            const int gg = idx - y * G;
+            if (gg < gtot) out[(size_t)y * d.ldI + kx0 + gg] = bufs[(size_t)gg * d.M + y];
+        }
     }
 }
 
@@ -313,29 +317,26 @@ __device__ __forceinline__ void yfwd_col_body(const Dims& d, const typename Vec<
     fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
     __syncthreads();
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
-        const int gg = idx / d.KY;
+        const int gg = gtot == 1 ? 0 : idx / d.KY;
         const int jc = idx - gg * d.KY;
         const int n = jc <= d.K ? jc : ky_of_jc(d, jc) + d.M;
         Out[(size_t)(kx0 + gg) * d.ldS + jc] = bufs[(size_t)gg * d.M + n];
     }
 }
 
-// ... and the epilogue of every mode from the two compact arrays.
+// ... and the epilogue of every mode from the two compact arrays: column kx
+// = blockIdx.y, rows jc = blockIdx.x * blockDim.x + threadIdx.x.
 template <typename T>
 __device__ __forceinline__ bool stage_body(const Dims& d, const typename Vec<T>::t* __restrict__ Fu,
                                            const typename Vec<T>::t* __restrict__ Fv, typename Vec<T>::t* S0,
                                            typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
                                            const typename Vec<T>::t* __restrict__ src, int stage, double dt,
                                            const Phys& ph) {
-    bool bad = false;
-    const int total = d.KX * d.KY;
-    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
-        const int kx = idx / d.KY;
-        const int jc = idx - kx * d.KY;
-        const size_t off = (size_t)kx * d.ldS + jc;
-        bad |= stage_point<T>(d, __ldcg(&Fu[off]), __ldcg(&Fv[off]), kx, jc, S0, S1, Sdw, src, stage, dt, ph);
-    }
-    return bad;
+    const int kx = blockIdx.y;
+    const int jc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (kx >= d.KX || jc >= d.KY) return false;
+    const size_t off = (size_t)kx * d.ldS + jc;
+    return stage_point<T>(d, __ldcg(&Fu[off]), __ldcg(&Fv[off]), kx, jc, S0, S1, Sdw, src, stage, dt, ph);
 }
 
 // ------------------------------------------------------------------------
@@ -372,7 +373,7 @@ __device__ __forceinline__ bool yfwd_body(const Dims& d, const typename Vec<T>::
 
     bool bad = false;
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
-        const int gg = idx / d.KY;
+        const int gg = gtot == 1 ? 0 : idx / d.KY;
         const int jc = idx - gg * d.KY;
         const int ky = ky_of_jc(d, jc);
         const int n = jc <= d.K ? jc : ky + d.M;
