@@ -24,33 +24,41 @@ __device__ __forceinline__ bool bits_nonfinite(float x) {
 // compact row jc -> ky
 __device__ __forceinline__ int ky_of_jc(const Dims& d, int jc) { return jc <= d.K ? jc : jc - d.KY; }
 
+// w times the real factor s computed in FP64: in FP64 as is; in FP32 the
+// factor is rounded once and the product taken in FP32, so that the FP32
+// variant spends 3 FP64-pipe instructions per element (ky -> double, the
+// product with 1/k^2, the rounding) instead of 8.
+// With rot, i s w = (-s w.y, s w.x).
+template <typename VT>
+__device__ __forceinline__ VT scale_by(VT w, double s, bool rot) {
+    using T = decltype(w.x);
+    if constexpr (sizeof(T) == 4) {
+        const T f = (T)s;
+        return rot ? mk<VT>(-f * w.y, f * w.x) : mk<VT>(f * w.x, f * w.y);
+    } else {
+        return rot ? mk<VT>(-s * w.y, s * w.x) : mk<VT>(s * w.x, s * w.y);
+    }
+}
+
 // Apply a spectral operator to omega of mode (kx, ky); 1/k^2 is FP64.
 template <typename VT>
 __device__ __forceinline__ VT apply_op(int op, VT w, int kx, int ky, double rk2) {
     using T = decltype(w.x);
     switch (op) {
-        case OP_U: {  // u = i ky psi = (-ky psi.y, ky psi.x)
-            const double s = (double)ky * rk2;
-            return mk<VT>((T)(-s * (double)w.y), (T)(s * (double)w.x));
-        }
-        case OP_V: {  // v = -i kx psi = (kx psi.y, -kx psi.x)
-            const double s = (double)kx * rk2;
-            return mk<VT>((T)(s * (double)w.y), (T)(-s * (double)w.x));
-        }
+        case OP_U:  // u = i ky psi = (-ky psi.y, ky psi.x)
+            return scale_by(w, (double)ky * rk2, true);
+        case OP_V:  // v = -i kx psi = (kx psi.y, -kx psi.x)
+            return scale_by(w, -(double)kx * rk2, true);
         case OP_PSI:
-            return mk<VT>((T)(rk2 * (double)w.x), (T)(rk2 * (double)w.y));
+            return scale_by(w, rk2, false);
         case OP_WX:
             return mk<VT>((T)(-kx) * w.y, (T)kx * w.x);
         case OP_WY:
             return mk<VT>((T)(-ky) * w.y, (T)ky * w.x);
-        case OP_UX: {  // i kx u = -kx ky psi
-            const double s = -(double)kx * (double)ky * rk2;
-            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
-        }
-        case OP_VY: {  // i ky v = kx ky psi
-            const double s = (double)kx * (double)ky * rk2;
-            return mk<VT>((T)(s * (double)w.x), (T)(s * (double)w.y));
-        }
+        case OP_UX:  // i kx u = -kx ky psi
+            return scale_by(w, -(double)kx * (double)ky * rk2, false);
+        case OP_VY:  // i ky v = kx ky psi
+            return scale_by(w, (double)kx * (double)ky * rk2, false);
         default:
             return w;
     }
