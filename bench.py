@@ -178,12 +178,13 @@ def dist_env():
 
 
 # ---------------------------------------------------------------------------
-def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float):
-    """Time the oracle (FP64 CPU restatement) on all host cores.  Returns
-    (Mpt*steps/s, timed steps, cores, seconds per step)."""
+def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float, cores: int | None = None):
+    """Time the oracle (FP64 CPU restatement) on all host cores (or on
+    ``cores`` threads).  Returns (Mpt*steps/s, timed steps, cores, seconds per
+    step)."""
     import numpy as np  # noqa: F401
     import oracle as O
-    cores = O.cpu_count()
+    cores = cores or O.cpu_count()
     O.set_workers(cores)
     g = O.get_grid_size(n, n)
     w, psi = O.set_turbulent(g, SEED, kind=O.SPECTRUM_K4_GAUSS, k0=10.0, tke_target=0.5)
@@ -394,6 +395,9 @@ def main():
         cpu = {"value": rate, "unit": "Mpt*steps/s", "cores": cores, "kind": "port",
                "sample": f"{done} RK3 step(s) of the {args.n}^2 FP64 workload, numpy/scipy.fft "
                          f"restatement of the reference on {cores} threads ({sps:.2f} s/step)"}
+        if cores > 1:
+            r1, _, _, s1 = cpu_step_rate(args.n, 1, 0, budget_s=args.cpu_budget, cores=1)
+            cpu["one_core"] = {"value": r1, "unit": "Mpt*steps/s", "cores": 1, "s_per_step": s1}
 
     import numpy as np
     from spectral2d_gb300 import Spectral2D, probe_fp64_peak
