@@ -143,9 +143,9 @@ S2D_API int s2d_integrate_steps(s2d_handle* h, int32_t n, double dt);
  *
  * Host arrays in every call of this header (set/get_state, compute_rhs, this
  * one) are read and written in place by the kernels where the device can
- * address them: page-locked memory, and ordinary pageable memory on systems
- * whose GPU reads the host page tables (Grace, cudaDevAttrPageableMemoryAccess);
- * otherwise through staging copies.  The environment variable S2D_HOST_IO=copy,
+ * address them: page-locked memory, and ordinary pageable memory whose pages
+ * are resident on systems whose GPU reads the host page tables (Grace,
+ * cudaDevAttrPageableMemoryAccess); otherwise through staging copies.  The environment variable S2D_HOST_IO=copy,
  * read by s2d_create, forces the copies for that handle. */
 S2D_API int s2d_integrate_one_step_host(s2d_handle* h, double* wC, double* psiC,
                                         int32_t cISize, int32_t nyG, double dt);

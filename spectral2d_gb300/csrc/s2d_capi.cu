@@ -12,11 +12,14 @@
 #include "s2d_internal.h"
 
 #include <cuda_runtime.h>
+#include <sys/mman.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -240,6 +243,25 @@ struct HostArray {
     bool pageable = false;   // in place through the host page tables
 };
 
+// Whether 16 pages spread over [p, p + n) are resident.  The device writes
+// pageable memory in place only where its pages exist already: a page the
+// GPU touches first is faulted in by the host (45 ms for the 84 MB of fresh
+// np.zeros pages of a 2048^2 output pair on GB300, against 0.4 ms resident),
+// while a staging copy lets the CPU populate them.
+bool pages_resident(const void* p, size_t n) {
+    const long ps = sysconf(_SC_PAGESIZE);
+    if (ps <= 0 || n == 0) return false;
+    const uintptr_t mask = ~(uintptr_t)(ps - 1);
+    const uintptr_t first = (uintptr_t)p & mask, last = ((uintptr_t)p + n - 1) & mask;
+    constexpr int kSamples = 16;
+    for (int i = 0; i < kSamples; ++i) {
+        const uintptr_t q = (first + (last - first) / (kSamples - 1) * (uintptr_t)i) & mask;
+        unsigned char v = 0;
+        if (mincore((void*)q, (size_t)ps, &v) != 0 || !(v & 1)) return false;
+    }
+    return true;
+}
+
 HostArray host_array(const s2d_handle* h, const double* p) {
     HostArray a;
     a.host = const_cast<double*>(p);
@@ -253,7 +275,7 @@ HostArray host_array(const s2d_handle* h, const double* p) {
         a.dev = (double*)at.devicePointer;
     } else if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
         if (at.device == h->device) a.dev = a.host;
-    } else if (h->pageable_direct) {
+    } else if (h->pageable_direct && pages_resident(p, h->ref_bytes)) {
         a.dev = a.host;
         a.pageable = true;
     }

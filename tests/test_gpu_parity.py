@@ -184,14 +184,18 @@ def test_host_array_step_equals_device_step(S2D):
 
 
 def _host_buf(shape, mem):
+    """NaN-filled host array; "fresh" is an untouched np.zeros array (its pages
+    are not resident yet, so the library stages it through copies)."""
     from spectral2d_gb300.solver import pinned_array
+    if mem == "fresh":
+        return np.zeros(shape, dtype=np.complex128)
     a = pinned_array(shape) if mem == "pinned" else np.empty(shape, dtype=np.complex128)
     a[...] = np.nan + 1j * np.nan
     return a
 
 
 @pytest.mark.parametrize("n", [8, 96])
-@pytest.mark.parametrize("mem", ["pageable", "pinned"])
+@pytest.mark.parametrize("mem", ["pageable", "pinned", "fresh"])
 @pytest.mark.parametrize("io", ["in_place", "copy"])
 def test_host_array_io_paths(S2D, n, mem, io, monkeypatch):
     """Host-array calls on pageable and page-locked arrays, read and written
@@ -215,7 +219,7 @@ def test_host_array_io_paths(S2D, n, mem, io, monkeypatch):
         monkeypatch.setenv("S2D_HOST_IO", "copy")
     with S2D(n, nu=0.01) as s:
         ny, cx = w.shape
-        wh = _host_buf(w.shape, mem)
+        wh = _host_buf(w.shape, "pageable" if mem == "fresh" else mem)
         wh[keep] = w[keep]
         ph = _host_buf(w.shape, mem)
         s.set_state(wh)                     # reads the rectangle only
