@@ -31,16 +31,26 @@ namespace s2d {
 
 // ------------------------------------------------------------------------
 // K1, K2, K3 of one simulation: one tile per CTA (bodies in s2d_step.cuh).
-// K1, K2 and the split K3 come in two register budgets: LB > 0 = CTAs of at
-// most 256 threads, LB of them per SM (FP64: three, 80 registers, a third
-// CTA fills the barrier phases of the other two; FP32: four, 64 registers),
-// and the general one (LB = 0: up to 512 threads, M = 6144).
+// K1, K2 and the split K3 come in register budgets B, chosen from the CTA
+// size by budget<T>():
+//   B = 1: CTAs of at most 256 threads, FP64 three per SM (80 registers: a
+//          third CTA fills the barrier phases of the other two), FP32 four
+//          (64 registers);
+//   B = 2: FP32 CTAs of at most 512 threads (M = 6144), two per SM (64
+//          registers);
+//   B = 0: one CTA of up to 512 threads per SM.
 // ------------------------------------------------------------------------
+template <int B>
+constexpr int kMaxThreads = B == 1 ? 256 : 512;
+template <typename T, int B>
+constexpr int kMinBlocks = B == 1 ? (sizeof(T) == 8 ? 3 : 4) : (B == 2 ? 2 : 1);
 template <typename T>
-constexpr int kMinBlocks256 = sizeof(T) == 8 ? 3 : 4;
+int budget(int threads) {
+    return threads <= 256 ? 1 : (sizeof(T) == 4 ? 2 : 0);
+}
 
-template <typename T, int LB>
-__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
+template <typename T, int B>
+__global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_yinv(Dims d, const typename Vec<T>::t* __restrict__ S,
                                                const double* __restrict__ rk2, FieldSet fs,
                                                const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -48,8 +58,8 @@ __global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1) k_yinv(Dims d, co
     yinv_body<T>(d, S, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
-template <typename T, int LB>
-__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
+template <typename T, int B>
+__global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_xpass_bas(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
                                                     const typename Vec<T>::t* __restrict__ tw, int G,
                                                     T scale) {
     using VT = typename Vec<T>::t;
@@ -74,8 +84,8 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
 
 // K3 split in two (FP64 single runs): forward y-FFT of one field's columns
 // into a compact array, then the epilogue of every mode.
-template <typename T, int LB>
-__global__ void __launch_bounds__(LB ? 256 : 512, LB ? LB : 1)
+template <typename T, int B>
+__global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>))
     k_yfwd_col(Dims d, const typename Vec<T>::t* __restrict__ Iu, const typename Vec<T>::t* __restrict__ Iv,
                typename Vec<T>::t* Fu, typename Vec<T>::t* Fv, const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
@@ -579,10 +589,15 @@ cudaError_t Kern<T>::yinv(const Dims& d, const void* S, const double* rk2, const
                           cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
-    if (L.threads <= 256)
-        k_yinv<T, kMinBlocks256<T>><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
-    else
-        k_yinv<T, 0><<<ncg * fs.nf, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    const int nb = ncg * fs.nf;
+    switch (budget<T>(L.threads)) {
+        case 1: k_yinv<T, 1><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G); break;
+        case 2:
+            if constexpr (sizeof(T) == 4)
+                k_yinv<T, 2><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+            break;
+        default: k_yinv<T, 0><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+    }
     return cudaGetLastError();
 }
 
@@ -602,12 +617,15 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
                                const Launch& L) {
     using VT = typename Vec<T>::t;
     const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
-    if (L.threads <= 256)
-        k_xpass_bas<T, kMinBlocks256<T>><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
-                                                                                (const VT*)tw, L.G, scale);
-    else
-        k_xpass_bas<T, 0><<<(d.M + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv,
-                                                                                 (const VT*)tw, L.G, scale);
+    const int nb = (d.M + L.G - 1) / L.G;
+    switch (budget<T>(L.threads)) {
+        case 1: k_xpass_bas<T, 1><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale); break;
+        case 2:
+            if constexpr (sizeof(T) == 4)
+                k_xpass_bas<T, 2><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale);
+            break;
+        default: k_xpass_bas<T, 0><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale);
+    }
     return cudaGetLastError();
 }
 
@@ -627,12 +645,16 @@ cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, voi
                               cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
-    if (L.threads <= 256)
-        k_yfwd_col<T, kMinBlocks256<T>><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
-                                                               (const VT*)tw, L.G);
-    else
-        k_yfwd_col<T, 0><<<2 * ncg, L.threads, L.smem, st>>>(d, (const VT*)Iu, (const VT*)Iv, (VT*)Fu, (VT*)Fv,
-                                                                (const VT*)tw, L.G);
+    const VT* u = (const VT*)Iu;
+    const VT* v = (const VT*)Iv;
+    switch (budget<T>(L.threads)) {
+        case 1: k_yfwd_col<T, 1><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G); break;
+        case 2:
+            if constexpr (sizeof(T) == 4)
+                k_yfwd_col<T, 2><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G);
+            break;
+        default: k_yfwd_col<T, 0><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G);
+    }
     return cudaGetLastError();
 }
 
@@ -772,19 +794,22 @@ cudaError_t configure_kernels(int max_smem_optin) {
         cudaError_t e2 = set_smem(k, max_smem_optin);       \
         if (e2 != cudaSuccess && e == cudaSuccess) e = e2;  \
     } while (0)
-    S2D_SET((k_yinv<double, kMinBlocks256<double>>));
+    S2D_SET((k_yinv<double, 1>));
     S2D_SET((k_yinv<double, 0>));
-    S2D_SET((k_yinv<float, kMinBlocks256<float>>));
+    S2D_SET((k_yinv<float, 1>));
+    S2D_SET((k_yinv<float, 2>));
     S2D_SET((k_yinv<float, 0>));
     S2D_SET(k_xpass_rhs<double>);
     S2D_SET(k_xpass_rhs<float>);
-    S2D_SET((k_xpass_bas<double, kMinBlocks256<double>>));
+    S2D_SET((k_xpass_bas<double, 1>));
     S2D_SET((k_xpass_bas<double, 0>));
-    S2D_SET((k_xpass_bas<float, kMinBlocks256<float>>));
+    S2D_SET((k_xpass_bas<float, 1>));
+    S2D_SET((k_xpass_bas<float, 2>));
     S2D_SET((k_xpass_bas<float, 0>));
-    S2D_SET((k_yfwd_col<double, kMinBlocks256<double>>));
+    S2D_SET((k_yfwd_col<double, 1>));
     S2D_SET((k_yfwd_col<double, 0>));
-    S2D_SET((k_yfwd_col<float, kMinBlocks256<float>>));
+    S2D_SET((k_yfwd_col<float, 1>));
+    S2D_SET((k_yfwd_col<float, 2>));
     S2D_SET((k_yfwd_col<float, 0>));
     S2D_SET(k_yfwd_rk3<double>);
     S2D_SET(k_yfwd_rk3<float>);
