@@ -53,9 +53,32 @@ __device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
     __nv_bfloat162 h = *reinterpret_cast<__nv_bfloat162*>(&u);
     return __bfloat1622float2(h);
 }
-__device__ __forceinline__ float gelu_f(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+// GELU (erf form) with erf from Abramowitz & Stegun 7.1.26 (Hastings): for
+// z >= 0, 1 - erf(z) = t (a1 + t (a2 + t (a3 + t (a4 + t a5)))) exp(-z^2) with
+// t = 1 / (1 + p z), |error| <= 1.5e-7 (3.3e-7 for gelu in FP32 arithmetic),
+// far below the BF16 resolution of the activations, in about a third of the
+// instructions of erff.  With z = |x| / sqrt(2), q = 1 - erf(z) and e =
+// exp(-x^2 / 2): gelu(x) = x (1 - q/2) for x >= 0, x q / 2 for x < 0, and
+// gelu'(x) = Phi(x) + x e / sqrt(2 pi) with Phi(x) = 1 - q/2 or q/2.
+struct GeluQE {
+    float q, e;
+};
+__device__ __forceinline__ GeluQE gelu_qe(float x) {
+    const float z = fabsf(x) * 0.70710678118654752f;
+    const float t = __fdividef(1.0f, fmaf(0.3275911f, z, 1.0f));
+    const float pt = fmaf(fmaf(fmaf(fmaf(1.061405429f, t, -1.453152027f), t, 1.421413741f), t, -0.284496736f), t,
+                          0.254829592f);
+    const float e = __expf(-0.5f * x * x);
+    return {t * pt * e, e};
+}
+__device__ __forceinline__ float gelu_f(float x) {
+    const float hq = 0.5f * gelu_qe(x).q;
+    return x >= 0.0f ? x - x * hq : x * hq;
+}
 __device__ __forceinline__ float gelu_grad_f(float x) {
-    return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+    const GeluQE g = gelu_qe(x);
+    const float cdf = x >= 0.0f ? 1.0f - 0.5f * g.q : 0.5f * g.q;
+    return cdf + x * 0.39894228040143268f * g.e;
 }
 
 // ---- tcgen05 (5th-generation tensor core) helpers -----------------------
