@@ -59,6 +59,30 @@ def test_cnn_forward_and_gradients_vs_oracle(S):
         assert eW < 5e-2 and eb < 5e-2
 
 
+@pytest.mark.parametrize("grid, B", [(8, 3), (20, 2), (40, 1)])
+def test_cnn_forward_edge_tiles_vs_oracle(S, grid, B):
+    """The tensor-core convolution at grids whose 8 x 16 tiles are ragged or
+    whose halo wraps twice (8: every pixel is an edge pixel), against the
+    oracle's circular convolution, forward and gradients."""
+    rng = np.random.default_rng(grid)
+    with S.ClosureNet(grid, max_batch=4, seed=5) as net:
+        net.set_scales([1.0, 1.0, 1.0])
+        p = net.get_params()
+        x = rng.standard_normal((B, grid, grid, 2)).astype(np.float32)
+        t = (0.3 * rng.standard_normal((B, grid, grid))).astype(np.float32)
+        y = net.forward(x)
+        loss, g = net.grad(x, t)
+    params = _oracle_params(p)
+    xb = CO.bf16(x)
+    yo, _ = CO.forward(params, xb)
+    assert _rel(y, yo) < 2e-2
+    lo, go, _ = CO.loss_and_grads(params, xb, t.astype(np.float64))
+    assert abs(loss - lo) < 2e-2 * lo
+    gp = _oracle_params(g, bf=False)
+    for l in range(6):
+        assert _rel(gp[l][0], go[l][0]) < 5e-2 and _rel(gp[l][1], go[l][1]) < 5e-2
+
+
 def test_subgrid_flux_vs_oracle(S):
     nd, nl, nu = 64, 16, 2e-3
     gd, gl = O.get_grid_size(nd, nd), O.get_grid_size(nl, nl)
