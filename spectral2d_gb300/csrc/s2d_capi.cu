@@ -499,8 +499,9 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     d.ldS = d.KY + 1;                  // even pitch: 16-byte aligned FP32 columns
     d.ldI = (d.KX + 3) / 4 * 4;
     if (!factor_plan(d.M, &d)) {
+        const int M = d.M;
         delete h;
-        return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", d.M);
+        return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", M);
     }
     d.Tg = d.M / kElemsPerThread;
     h->ph.nu = cfg->nu;
@@ -512,8 +513,9 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     }
     h->ph.fk = cfg->forcing_amp != 0.0 ? cfg->forcing_k : 0;
     if (h->ph.fk < 0 || h->ph.fk > d.K) {
+        const int K = d.K;
         delete h;
-        return fail(S2D_ERR_INVALID, "forcing wavenumber %d outside [0, %d]", cfg->forcing_k, d.K);
+        return fail(S2D_ERR_INVALID, "forcing wavenumber %d outside [0, %d]", cfg->forcing_k, K);
     }
     {
         // amp cos(kf y) on the 1-based grid y_j = 2 pi j / nyG: coefficient

@@ -63,6 +63,20 @@ def test_create_rejects_bad_config_before_touching_a_gpu(gpu_lib, cfg):
     assert not h.value
 
 
+@pytest.mark.parametrize("cfg, msg", [
+    (dict(nx=40), "padded grid 60 "),                              # 60 = 4 * 15: no FFT plan
+    (dict(nx=16, forcing_amp=1.0, forcing_k=99), "outside [0, 8]"),
+])
+def test_create_error_messages_name_the_rejected_values(gpu_lib, cfg, msg):
+    """The messages of rejected handles report values read before the
+    half-built handle is freed."""
+    c = L.S2DConfig(nx=cfg["nx"], ny=cfg["nx"], dealias=1, precision=0, nu=0.01, alpha=0.0,
+                    forcing_amp=cfg.get("forcing_amp", 0.0), forcing_k=cfg.get("forcing_k", 0), device=0)
+    h = C.c_void_p()
+    assert gpu_lib.s2d_create(C.byref(c), C.byref(h)) != 0
+    assert msg in L.last_error(), L.last_error()
+
+
 def test_null_arguments_are_rejected(gpu_lib):
     assert gpu_lib.s2d_get_grid_size(16, 16, 1, None) == L.S2D_ERR_INVALID
     assert gpu_lib.s2d_create(None, None) == L.S2D_ERR_INVALID
