@@ -54,10 +54,13 @@ void usage() {
                  "spectral2d_run [--nx N] [--ny N] [--nu NU] [--dt DT] [--steps N | --end-time T]\n"
                  "  [--cfl C] [--ic tg|schumann|k4gauss] [--k0 K0] [--urms U] [--tke E] [--seed S]\n"
                  "  [--print-period N] [--stat-period N] [--write-period N] [--precision fp64|fp32]\n"
-                 "  [--out DIR] [--resume CKPT] [--checkpoint CKPT]\n");
+                 "  [--out DIR] [--resume CKPT] [--checkpoint CKPT]\n"
+                 "  (--nx sets ny too unless --ny is given)\n");
 }
 
+// --nx sets both sizes (the library runs square grids) unless --ny is given.
 bool parse(int argc, char** argv, Params& p) {
+    bool ny_given = false;
     for (int i = 1; i < argc; ++i) {
         const std::string a = argv[i];
         auto val = [&](const char* name) -> const char* {
@@ -68,7 +71,7 @@ bool parse(int argc, char** argv, Params& p) {
             return argv[++i];
         };
         if (a == "--nx") p.nx = std::atoi(val("--nx"));
-        else if (a == "--ny") p.ny = std::atoi(val("--ny"));
+        else if (a == "--ny") { p.ny = std::atoi(val("--ny")); ny_given = true; }
         else if (a == "--nu") p.nu = std::atof(val("--nu"));
         else if (a == "--dt") p.dt = std::atof(val("--dt"));
         else if (a == "--steps") { p.stepEnd = std::atol(val("--steps")); p.endMethod = FIXED_STEP_COUNT; }
@@ -93,6 +96,7 @@ bool parse(int argc, char** argv, Params& p) {
         else if (a == "--checkpoint") p.checkpoint = val("--checkpoint");
         else return false;
     }
+    if (!ny_given) p.ny = p.nx;
     return p.printPeriod > 0 && p.statPeriod > 0 && p.writePeriod > 0;
 }
 

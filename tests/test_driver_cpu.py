@@ -33,3 +33,12 @@ def test_invalid_grid_is_rejected_by_create(driver, tmp_path, nx):
     p = _run(driver, "--nx", nx, "--ny", nx, "--out", tmp_path)
     assert p.returncode == 1 and "s2d_create" in p.stdout and "multiple of 8" in p.stdout
     assert not (tmp_path / "EULERIAN.DAT").exists()
+
+
+def test_nx_alone_sets_both_sizes(driver, tmp_path):
+    """--nx without --ny gives a square grid: the rejection of nx = 60 is the
+    grid's own (not a size mismatch), and a differing --ny is a mismatch."""
+    p = _run(driver, "--nx", 60, "--out", tmp_path)
+    assert p.returncode == 1 and "multiple of 8" in p.stdout
+    p = _run(driver, "--nx", 16, "--ny", 32, "--out", tmp_path)
+    assert p.returncode == 1 and "nx must equal ny" in p.stdout
