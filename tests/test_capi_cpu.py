@@ -3,12 +3,16 @@ symbol include/*.h declares, and its host-only entry points agree with the
 oracle.  No compute call here touches a GPU."""
 
 import ctypes as C
+import os
+import re
 
 import numpy as np
 import pytest
 
 import oracle as O
 from spectral2d_gb300 import _lib as L
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def test_library_exports_every_header_symbol(built_lib):
@@ -91,3 +95,34 @@ def test_product_package_does_not_import_the_oracle():
     for p in pkg.rglob("*"):
         if p.suffix in (".py", ".cu", ".cpp", ".h", ".cuh"):
             assert "oracle" not in p.read_text().replace("the oracle", ""), p
+
+
+def _header_params():
+    """name -> (return type, parameter count) of every S2D_API declaration."""
+    hdr = open(os.path.join(ROOT, "include", "s2d.h")).read()
+    out = {}
+    for m in re.finditer(r"S2D_API\s+(.+?)\b(s2d_\w+)\s*\(([^;]*?)\)\s*;", hdr, re.S):
+        ret, name, params = m.group(1).strip(), m.group(2), m.group(3).strip()
+        out[name] = (ret, 0 if params in ("", "void") else params.count(",") + 1)
+    return out
+
+
+def test_fortran_interfaces_match_the_header(built_lib):
+    """Every BIND(C) interface of the Fortran module names an exported entry
+    point of the header, with its argument count, as a FUNCTION when the C
+    function returns a value and a SUBROUTINE when it returns void (no
+    Fortran compiler is available to check the module itself)."""
+    src = open(os.path.join(ROOT, "spectral2d_gb300", "fortran", "s2d_mod.F90")).read()
+    src = re.sub(r"&\s*\n\s*&?", " ", src)   # join continuation lines
+    pat = re.compile(r"(INTEGER\(C_INT\)\s+FUNCTION|SUBROUTINE)\s+(\w+)\s*\(([^)]*)\)\s*BIND\(C,\s*NAME='(\w+)'\)")
+    found = pat.findall(src)
+    assert len(found) >= 20
+    hdr = _header_params()
+    lib = C.CDLL(built_lib)
+    for kind, fname, args, cname in found:
+        assert fname == cname and cname in hdr, cname
+        nargs = len([a for a in args.split(",") if a.strip()])
+        ret, nparams = hdr[cname]
+        assert nargs == nparams, (cname, nargs, nparams)
+        assert ("SUBROUTINE" in kind) == (ret == "void"), (cname, kind, ret)
+        assert hasattr(lib, cname), cname
