@@ -12,12 +12,14 @@ total energy 0.5).  Metric: Mpt*steps/s = N^2 * steps/s / 1e6.
   with CUDA events on the solver's stream between two synchronisations.
 * ``e2e``: the same metric through the C-ABI drop-in for the reference's
   IntegrateOneStep with host arrays (s2d_integrate_one_step_host): every step
-  copies wC in from pinned host memory and wC, psiC out.
+  moves wC's retained modes in from page-locked host memory and wC, psiC out
+  over the host link (the kernels read and write the host arrays in place).
 * ``roofline``: the dominant kernel's algorithmic bytes per launch (byte model
   below) over its CUDA-event launch time, against the measured HBM peak; the
   FP64-ALU view of the same kernel is reported beside it.
 * ``cpu_baseline``: the FP64 CPU restatement of the reference (scipy/pocketfft
-  on all host cores) timed on a bounded sample of the same workload.
+  on all host cores, and on one core) timed on a bounded sample of the same
+  workload.
 * ``--impl reference``: that CPU restatement as the reference arm (the
   reference itself, Fortran + FFTW-MPI, cannot be built on these machines).
 
