@@ -382,3 +382,36 @@ def test_inviscid_rhs_conserves_energy_and_enstrophy(S2D, n):
     rel_z = abs(dZ) / np.sum(wt * np.abs(w) * np.abs(dW))
     print(f"N={n}: inviscid dE/dt rel {rel_e:.2e}, dZ/dt rel {rel_z:.2e}")
     assert rel_e < 1e-12 and rel_z < 1e-12
+
+
+def test_handles_from_several_host_threads(S2D):
+    """Handles created, stepped and read from four host threads at once (the
+    per-device one-time kernel set-up is shared) give the serial bits."""
+    import threading
+    n = 64
+    g = O.get_grid_size(n, n)
+    states = [O.random_state(g, 40 + i, decay=0.1) for i in range(4)]
+
+    def run(w):
+        with S2D(n, nu=0.01) as s:
+            s.set_state(w)
+            s.integrate_steps(5, 1e-3)
+            return s.get_state()[0]
+
+    serial = [run(w) for w in states]
+    out, errs = [None] * 4, []
+
+    def worker(i):
+        try:
+            out[i] = run(states[i])
+        except Exception as e:  # reported below
+            errs.append(e)
+
+    ts = [threading.Thread(target=worker, args=(i,)) for i in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join(timeout=120)
+    assert not errs, errs
+    for a, b in zip(out, serial):
+        assert np.array_equal(a, b)
