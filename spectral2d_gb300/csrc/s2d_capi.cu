@@ -176,8 +176,11 @@ int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_gro
     return S2D_OK;
 }
 
+// join: an event on another stream that the epilogue (the first kernel that
+// reads h->src) waits for; the kernels before it run concurrently with that
+// stream's work
 template <typename T>
-int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
+int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr) {
     const Dims& d = h->d;
     const bool bas = h->ph.form == S2D_NL_BASDEVANT;
     FieldSet fs{};
@@ -200,19 +203,26 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
         // CTAs per SM; the products' spectra go through I[2] (free in this
         // form) and Fv in the compact layout
         S2D_CUDA(Kern<T>::yfwd_col(d, h->I[0], h->I[1], h->I[2], h->Fv, h->tw, h->stream, h->L_ycol));
+        // the epilogue after a cross-stream join is an ordinary launch
+        if (join) S2D_CUDA(cudaStreamWaitEvent(h->stream, join, 0));
         S2D_CUDA(Kern<T>::stage(d, h->I[2], h->Fv, h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->flags,
-                                h->stream));
+                                h->stream, h->L_ycol.pdl && !join));
     } else {
+        Launch L = h->L_yfwd;
+        if (join) {
+            S2D_CUDA(cudaStreamWaitEvent(h->stream, join, 0));
+            L.pdl = false;
+        }
         S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->tw,
-                                   h->flags, h->stream, h->L_yfwd));
+                                   h->flags, h->stream, L));
     }
     if (ev) S2D_CUDA(cudaEventRecord(ev[3], h->stream));
     return S2D_OK;
 }
 
-int launch_rhs_stage_any(s2d_handle* h, int stage, double dt, cudaEvent_t* ev) {
-    return h->prec == S2D_FP64 ? launch_rhs_stage<double>(h, stage, dt, ev)
-                               : launch_rhs_stage<float>(h, stage, dt, ev);
+int launch_rhs_stage_any(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr) {
+    return h->prec == S2D_FP64 ? launch_rhs_stage<double>(h, stage, dt, ev, join)
+                               : launch_rhs_stage<float>(h, stage, dt, ev, join);
 }
 
 int launch_step(s2d_handle* h, double dt) {
@@ -633,9 +643,25 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     if ((rr = pick_launch(h, d.Tg, tb, tgt, d.KX, &h->L_ystore, "column transform")) != S2D_OK) return bail(rr);
     if ((rr = pick_launch(h, d.Tg, tb, tgt, 2L * d.KX, &h->L_ycol, "forward y-pass (split)")) != S2D_OK)
         return bail(rr);
+    // every kernel of a step is launched as a programmatic dependent of the
+    // one before it (S2D_PDL=0: plain stream order)
+    {
+        const char* e = std::getenv("S2D_PDL");
+        const bool pdl = !(e && e[0] == '0');
+        for (Launch* L : {&h->L_yinv, &h->L_xpass, &h->L_yfwd, &h->L_xrow, &h->L_ystore, &h->L_ycol}) L->pdl = pdl;
+    }
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
     *out = h;
+    return S2D_OK;
+}
+
+// One RK3 step whose source term h->src is produced on another stream: the
+// first stage's inverse y-pass and x-pass run concurrently with that work,
+// its epilogue waits for src_ready.
+int s2d::launch_step_sourced(s2d_handle* h, double dt, cudaEvent_t src_ready) {
+    S2D_TRY(launch_rhs_stage_any(h, 1, dt, nullptr, src_ready));
+    for (int s = 2; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr));
     return S2D_OK;
 }
 
@@ -648,11 +674,15 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     drop_graph(h);
     void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
-                    h->zeros};
+                    h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);
+    if (h->clstream) cudaStreamSynchronize(h->clstream);
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (h->xstream) cudaStreamDestroy(h->xstream);
+    if (h->clstream) cudaStreamDestroy(h->clstream);
+    if (h->ev_fork) cudaEventDestroy(h->ev_fork);
+    if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
 }

@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
     __shared__ uint32_t tmem_base;
     __shared__ int s_ok;
 
+    pdl_enter();   // before the TMEM allocation: a waiting CTA holds no columns
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
     const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
@@ -474,15 +475,14 @@ cudaError_t conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* act, int B, i
 template <int KC, int NC, int SIGN, int EPI>
 cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
                         const __nv_bfloat16* zprev, __nv_bfloat16* z, __nv_bfloat16* a, float* yout, int B, int H,
-                        int Wd, unsigned int* err, int sms, cudaStream_t st) {
+                        int Wd, unsigned int* err, int sms, cudaStream_t st, bool pdl = false) {
     CUtensorMap map;
     const cudaError_t e = conv_tensor_map<KC>(&map, in, B, H, Wd);
     if (e != cudaSuccess) return e;
     const long ntiles = (long)((Wd + kConvTX - 1) / kConvTX) * ((H + kConvTY - 1) / kConvTY) * B;
     const int grid = (int)std::min<long>(ntiles, 4L * sms);
-    k_conv_tc<KC, NC, SIGN, EPI><<<grid, kConvThreads, ConvTile<KC, NC>::SMEM, st>>>(map, in, W, bias, zprev, z, a,
-                                                                                    yout, B, H, Wd, err);
-    return cudaGetLastError();
+    return launch_k(k_conv_tc<KC, NC, SIGN, EPI>, grid, kConvThreads, ConvTile<KC, NC>::SMEM, st, pdl, map, in, W,
+                    bias, zprev, z, a, yout, B, H, Wd, err);
 }
 
 // Weight and bias gradient of one layer on the FP32 pipes:
@@ -749,13 +749,17 @@ struct LesRun {
     T* pw;          // physical w on the M x M collocation grid
     T* pp;          // physical psi
     typename Vec<T>::t* src;   // -Pi^ (compact layout)
-    double* part;   // sums of w^2 per row tile of k_cl_xinv
+    double* part;   // sums of w^2 per row tile of k_cl_xinv; part[nparts]: their mean per point
 };
 
-// sum of the nparts partial sums, in order (one thread): w^2 summed over the grid
-__device__ __forceinline__ double ordered_sum(const double* __restrict__ part, int nparts) {
+// Sum of the nparts partial sums by one warp in a fixed order (lane l adds
+// part[l], part[l + 32], ... in turn, then an xor butterfly over the lanes):
+// every lane returns the same value, on every call.
+__device__ __forceinline__ double warp_ordered_sum(const double* __restrict__ part, int nparts, int lane) {
     double s = 0.0;
-    for (int i = 0; i < nparts; ++i) s += __ldcg(&part[i]);
+    for (int i = lane; i < nparts; i += 32) s += __ldcg(&part[i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
     return s;
 }
 
@@ -766,6 +770,7 @@ __global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __rest
                                                   const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
     FieldSet fs{};
     fs.nf = 2;
@@ -783,6 +788,7 @@ __global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __rest
                                                   const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
     VT* bufs = reinterpret_cast<VT*>(smem_raw);
     const int g = threadIdx.x / d.Tg;
@@ -815,21 +821,28 @@ __global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __rest
     if (threadIdx.x == 0) R.part[blockIdx.x] = red[0];
 }
 
-// Network input of every run: (w / (a s0), psi / (a s1)), a = rms w of the run.
+// Network input of every run: (w / (a s0), psi / (a s1)), a = rms w of the
+// run; the mean of w^2 is kept in part[nparts] for k_cl_xfwd.  Only channels
+// 0 and 1 of x are written: channels 2..15 of the input buffer are zero from
+// its allocation on, and every writer of it keeps them so.
 template <typename T>
 __global__ void k_cl_pack(const LesRun<T>* __restrict__ runs, int nparts, long HW, float r0, float r1,
                           __nv_bfloat16* x) {
     __shared__ double s_ia;
+    pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
-    if (threadIdx.x == 0) s_ia = 1.0 / sqrt(ordered_sum(R.part, nparts) / (double)HW);
-    __syncthreads();
-    const double ia = s_ia;
-    __nv_bfloat16* xb = x + (size_t)blockIdx.y * HW * 16;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x) {
-        uint32_t* xr = reinterpret_cast<uint32_t*>(xb + i * 16);
-        xr[0] = pack_bf16((float)((double)R.pw[i] * r0 * ia), (float)((double)R.pp[i] * r1 * ia));
-        for (int c = 1; c < 8; ++c) xr[c] = 0u;
+    if (threadIdx.x < 32) {
+        const double mean = warp_ordered_sum(R.part, nparts, threadIdx.x) / (double)HW;
+        if (threadIdx.x == 0) {
+            s_ia = 1.0 / sqrt(mean);
+            if (blockIdx.x == 0) R.part[nparts] = mean;
+        }
     }
+    __syncthreads();
+    const T a0 = (T)((double)r0 * s_ia), a1 = (T)((double)r1 * s_ia);
+    __nv_bfloat16* xb = x + (size_t)blockIdx.y * HW * 16;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x)
+        *reinterpret_cast<uint32_t*>(xb + i * 16) = pack_bf16((float)(R.pw[i] * a0), (float)(R.pp[i] * a1));
 }
 
 // Network output -> -Pi on the grid (scale a^2 y, scale = -s2), forward x-FFT
@@ -840,12 +853,10 @@ __global__ void __launch_bounds__(512) k_cl_xfwd(Dims d, const LesRun<T>* __rest
                                                   const typename Vec<T>::t* __restrict__ tw, int G, T xscale) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ double s_s;
+    pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
     const long HW = (long)d.M * d.M;
-    if (threadIdx.x == 0) s_s = scale * (ordered_sum(R.part, nparts) / (double)HW);
-    __syncthreads();
-    const double s = s_s;
+    const T s = (T)(scale * __ldcg(&R.part[nparts]));
     VT* bufs = reinterpret_cast<VT*>(smem_raw);
     const int g = threadIdx.x / d.Tg;
     const int lane = threadIdx.x - g * d.Tg;
@@ -856,7 +867,7 @@ __global__ void __launch_bounds__(512) k_cl_xfwd(Dims d, const LesRun<T>* __rest
     const float* r1 = Y + (size_t)blockIdx.y * HW + (size_t)y1 * d.M;
     const float* r2 = r1 + d.M;
     for (int n = lane; n < d.M; n += d.Tg)
-        Z[n] = active ? mk<VT>((T)(s * (double)r1[n]), (T)(s * (double)r2[n])) : mk<VT>((T)0, (T)0);
+        Z[n] = active ? mk<VT>(s * (T)r1[n], s * (T)r2[n]) : mk<VT>((T)0, (T)0);
     fft_run<false>(Z, d, lane, tw);
     extract_pair(Z, R.I2 + (size_t)y1 * d.ldI, R.I2 + (size_t)(y1 + 1) * d.ldI, d, lane, active, xscale);
 }
@@ -869,6 +880,7 @@ __global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __re
                                                     double kmin2) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
     VT* bufs = reinterpret_cast<VT*>(smem_raw);
     const int g = threadIdx.x / d.Tg;
@@ -977,16 +989,16 @@ int refresh_all(s2d_cnn* c) {
 
 // forward of the batch in X0 (B images); the pre-activations z are kept only
 // when a backward pass follows
-int forward(s2d_cnn* c, int B, bool keep_z) {
+int forward(s2d_cnn* c, int B, bool keep_z, bool pdl = false) {
     const float* bias[kLayers];
     for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
     C_CUDA((launch_conv<16, 32, 1, 0>(c->X0, c->Wb[0], bias[0], nullptr, keep_z ? c->Z[0] : nullptr, c->A[0],
-                                      nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
+                                      nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream, pdl)));
     for (int l = 1; l < kLayers - 1; ++l)
         C_CUDA((launch_conv<32, 32, 1, 0>(c->A[l - 1], c->Wb[l], bias[l], nullptr, keep_z ? c->Z[l] : nullptr,
-                                          c->A[l], nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
+                                          c->A[l], nullptr, B, c->H, c->Wd, c->cflags, c->sms, c->stream, pdl)));
     C_CUDA((launch_conv<32, 16, 1, 1>(c->A[kLayers - 2], c->Wb[kLayers - 1], bias[kLayers - 1], nullptr, nullptr,
-                                      nullptr, c->Y, B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
+                                      nullptr, c->Y, B, c->H, c->Wd, c->cflags, c->sms, c->stream, pdl)));
     return S2D_OK;
 }
 
@@ -1155,21 +1167,24 @@ int closure_table_impl(s2d_handle* const* runs, int n, void** tab) {
     const int nparts = (h0->d.M + h0->L_xrow.G - 1) / h0->L_xrow.G;
     const size_t head = (size_t)n * sizeof(LesRun<double>);
     void* t = nullptr;
-    C_CUDA(cudaMalloc(&t, head + (size_t)n * nparts * sizeof(double)));
+    C_CUDA(cudaMalloc(&t, head + (size_t)n * (nparts + 1) * sizeof(double)));
     std::vector<LesRun<double>> rows(n);
     const long HW = (long)h0->d.M * h0->d.M;
     for (int i = 0; i < n; ++i) {
         s2d_handle* h = runs[i];
         LesRun<double>& R = rows[i];
         R.S0 = (const double2*)h->S0;
-        R.I0 = (double2*)h->I[0];
-        R.I1 = (double2*)h->I[1];
-        R.I2 = (double2*)h->I[2];
+        // a handle stepped with its closure on a second stream has its own
+        // transform buffers; the batch (one stream) uses the handles' I
+        char* ib = (char*)h->cl_I;
+        R.I0 = (double2*)(ib ? ib : h->I[0]);
+        R.I1 = (double2*)(ib ? ib + h->Ibytes : h->I[1]);
+        R.I2 = (double2*)(ib ? ib + 2 * h->Ibytes : h->I[2]);
         // phys holds M*M 8-byte elements per field; FP32 runs use the front half
         R.pw = (double*)h->phys;
         R.pp = h->prec == S2D_FP64 ? R.pw + HW : (double*)((float*)h->phys + HW);
         R.src = (double2*)h->src;
-        R.part = (double*)((char*)t + head) + (size_t)i * nparts;
+        R.part = (double*)((char*)t + head) + (size_t)i * (nparts + 1);
     }
     const cudaError_t e = cudaMemcpy(t, rows.data(), head, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -1192,23 +1207,23 @@ int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab,
     const Launch& Ls = h0->L_ystore;
     const int nparts = (d.M + Lx.G - 1) / Lx.G;
     const VT* tw = (const VT*)h0->tw;
-    k_cl_yinv<T><<<dim3(2 * ((d.KX + Ly.G - 1) / Ly.G), n), Ly.threads, Ly.smem, st>>>(d, R, h0->rk2, tw, Ly.G);
-    k_cl_xinv<T><<<dim3(nparts, n), Lx.threads, Lx.smem, st>>>(d, R, tw, Lx.G);
+    const bool pdl = Ly.pdl;
+    C_CUDA(launch_k(k_cl_yinv<T>, dim3(2 * ((d.KX + Ly.G - 1) / Ly.G), n), Ly.threads, Ly.smem, st, pdl, d, R,
+                    h0->rk2, tw, Ly.G));
+    C_CUDA(launch_k(k_cl_xinv<T>, dim3(nparts, n), Lx.threads, Lx.smem, st, pdl, d, R, tw, Lx.G));
     const int chunks = (int)std::min<long>((HW + 255) / 256, 64);
-    k_cl_pack<T><<<dim3(chunks, n), 256, 0, st>>>(R, nparts, HW, (float)(1.0 / c->scale[0]),
-                                                  (float)(1.0 / c->scale[1]), c->X0);
-    C_CUDA(cudaGetLastError());
+    C_CUDA(launch_k(k_cl_pack<T>, dim3(chunks, n), 256, 0, st, pdl, R, nparts, HW, (float)(1.0 / c->scale[0]),
+                    (float)(1.0 / c->scale[1]), c->X0));
     // the network runs on the caller's stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
     c->stream = st;
-    const int r = forward(c, n, false);
+    const int r = forward(c, n, false, pdl);
     c->stream = saved;
     if (r != S2D_OK) return r;
-    k_cl_xfwd<T><<<dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st>>>(
-        d, R, nparts, c->Y, -c->scale[2], tw, Lx.G, (T)(0.5 / ((double)d.M * (double)d.M)));
-    k_cl_ystore<T><<<dim3((d.KX + Ls.G - 1) / Ls.G, n), Ls.threads, Ls.smem, st>>>(d, R, tw, Ls.G,
-                                                                                 c->k_min * c->k_min);
-    C_CUDA(cudaGetLastError());
+    C_CUDA(launch_k(k_cl_xfwd<T>, dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st, pdl, d, R,
+                    nparts, (const float*)c->Y, -c->scale[2], tw, Lx.G, (T)(0.5 / ((double)d.M * (double)d.M))));
+    C_CUDA(launch_k(k_cl_ystore<T>, dim3((d.KX + Ls.G - 1) / Ls.G, n), Ls.threads, Ls.smem, st, pdl, d, R, tw,
+                    Ls.G, c->k_min * c->k_min));
     return S2D_OK;
 }
 
@@ -1309,6 +1324,7 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
               cudaMalloc(&c->m, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&c->v, off * sizeof(float)) == cudaSuccess &&
               cudaMalloc(&c->X0, P * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMemset(c->X0, 0, P * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->dZ6, P * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->dZa, P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->dZb, P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
@@ -1679,6 +1695,10 @@ S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
     if (c) {
         int r = s2d::ensure_closure_buffers(les);
         if (r != S2D_OK) return r;
+        if (!les->cl_I) C_CUDA(cudaMalloc(&les->cl_I, 3 * les->Ibytes));
+        if (!les->clstream) C_CUDA(cudaStreamCreateWithFlags(&les->clstream, cudaStreamNonBlocking));
+        if (!les->ev_fork) C_CUDA(cudaEventCreateWithFlags(&les->ev_fork, cudaEventDisableTiming));
+        if (!les->ev_join) C_CUDA(cudaEventCreateWithFlags(&les->ev_join, cudaEventDisableTiming));
         if (!les->les_tab) {
             r = closure_table_impl(&les, 1, &les->les_tab);
             if (r != S2D_OK) return r;
@@ -1689,6 +1709,8 @@ S2D_API int s2d_les_set_closure(s2d_handle* les, s2d_cnn* c) {
         les->src = nullptr;
         cudaFree(les->les_tab);
         les->les_tab = nullptr;
+        cudaFree(les->cl_I);
+        les->cl_I = nullptr;
     }
     les->cnn = c;
     return S2D_OK;
@@ -1704,12 +1726,26 @@ S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {
     if (!les || n < 0) return cerr(S2D_ERR_INVALID, "bad argument");
     if (!les->cnn) return s2d_integrate_steps(les, n, dt);
     if (n == 0) return S2D_OK;
+    if (!std::isfinite(dt)) return cerr(S2D_ERR_INVALID, "dt must be finite");
+    if (!les->src || !les->les_tab || !les->clstream) return cerr(S2D_ERR_INVALID, "no closure set");
     C_CUDA(cudaSetDevice(les->device));
-    // one step (closure term + RK3 step) captured as a CUDA graph, rebuilt
-    // on every call so that it picks up new network scales and dt
+    // one step captured as a CUDA graph, rebuilt on every call so that it
+    // picks up new network scales and dt: the closure term of the state at the
+    // start of the step on clstream, concurrently with the first stage's
+    // inverse y-pass and x-pass on the handle's stream; the first stage's
+    // epilogue (the first reader of src) waits for it
     C_CUDA(cudaStreamBeginCapture(les->stream, cudaStreamCaptureModeThreadLocal));
-    int r = s2d_les_closure_term(les);
-    if (r == S2D_OK) r = s2d_integrate_one_step(les, dt);
+    int r = S2D_OK;
+    cudaError_t ec = cudaEventRecord(les->ev_fork, les->stream);
+    if (ec == cudaSuccess) ec = cudaStreamWaitEvent(les->clstream, les->ev_fork, 0);
+    if (ec == cudaSuccess) {
+        r = s2d::closure_terms(les->cnn, &les, 1, les->les_tab, les->clstream);
+        // the join is recorded even after a failure, so that the capture can end
+        ec = cudaEventRecord(les->ev_join, les->clstream);
+    }
+    if (ec != cudaSuccess && r == S2D_OK) r = cerr(S2D_ERR_CUDA, cudaGetErrorString(ec));
+    if (r == S2D_OK) r = s2d::launch_step_sourced(les, dt, les->ev_join);
+    else cudaStreamWaitEvent(les->stream, les->ev_join, 0);
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(les->stream, &g);
     if (r != S2D_OK || e != cudaSuccess) {

@@ -95,12 +95,47 @@ struct FieldSet {
 };
 
 // Launch shape for one kernel: G groups of Tg threads, dynamic smem bytes.
+// pdl: launched as a programmatic dependent of the previous kernel on the
+// stream (see pdl_enter / launch_k below).
 struct Launch {
     int G;
     int threads;
     size_t smem;
     int blocks;
+    bool pdl = false;
 };
+
+#ifdef __CUDACC__
+// Programmatic dependent launch.  A kernel launched with the programmatic
+// stream-serialization attribute may be scheduled while the previous kernel
+// on the stream still runs; every such kernel calls pdl_enter() first, in
+// every thread: it waits until the previous grid has completed and its
+// writes are visible (so the order of the whole chain stays transitive),
+// then lets the next grid be scheduled behind this one.  Launched without
+// the attribute both instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+#endif
+
+// <<<grid, block, smem, st>>> with the programmatic stream-serialization
+// attribute when pdl is set; the kernel must begin with pdl_enter().
+template <typename... P, typename... A>
+inline cudaError_t launch_k(void (*k)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, bool pdl,
+                            A&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k, static_cast<A&&>(args)...);
+}
 
 // ---- kernel launchers (s2d_kernels.cu); T = float or double -------------
 template <typename T>
@@ -120,7 +155,7 @@ struct Kern {
                                 const void* tw, cudaStream_t st, const Launch& L);
     static cudaError_t stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
                              const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
-                             cudaStream_t st);
+                             cudaStream_t st, bool pdl = false);
     static cudaError_t ref_to_compact(const Dims& d, const double* ref, int C, void* S,
                                       cudaStream_t st);
     static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
@@ -172,6 +207,12 @@ struct s2d_handle {
     void* phys = nullptr;          // 3 physical fields on the collocation grid (closure), 8 B/element
     struct s2d_cnn* cnn = nullptr; // closure network used by s2d_les_integrate_steps
     void* les_tab = nullptr;       // device table of closure_terms for this handle alone
+    // s2d_les_integrate_steps: the closure term runs on clstream (forked at
+    // ev_fork, joined at ev_join) with its own transform buffers cl_I (three
+    // arrays of Ibytes), concurrently with the first stage's transforms
+    void* cl_I = nullptr;
+    cudaStream_t clstream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     void* Ibase = nullptr;
     void* I[3] = {nullptr, nullptr, nullptr};
     size_t Ibytes = 0;
@@ -224,6 +265,9 @@ int physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, vo
 int ensure_closure_buffers(s2d_handle* h);
 int closure_table(s2d_handle* const* runs, int n, void** tab);
 int closure_terms(struct s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab, cudaStream_t st);
+// One RK3 step of h whose source h->src is written on another stream: the
+// first stage's epilogue waits for src_ready (s2d_capi.cu).
+int launch_step_sourced(s2d_handle* h, double dt, cudaEvent_t src_ready);
 // the network's grid and batch capacity
 int cnn_grid(const struct s2d_cnn* c);
 int cnn_max_batch(const struct s2d_cnn* c);

@@ -55,6 +55,7 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_yinv(Dim
                                                const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     yinv_body<T>(d, S, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
@@ -64,6 +65,7 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_xpass_ba
                                                     T scale) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     xpass_bas_body<T>(d, Iu, Iv, tw, G, scale, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
@@ -77,6 +79,7 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
                                                    int G, unsigned int* flags) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     const bool bad = yfwd_body<T>(d, Iu, Iv, S0, S1, Sdw, src, stage, dt, ph, tw, G, blockIdx.x,
                                   reinterpret_cast<VT*>(smem_raw));
     if (bad) atomicOr(flags, 1u);
@@ -90,6 +93,7 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>))
                typename Vec<T>::t* Fu, typename Vec<T>::t* Fv, const typename Vec<T>::t* __restrict__ tw, int G) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     yfwd_col_body<T>(d, Iu, Iv, Fu, Fv, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
@@ -99,6 +103,7 @@ __global__ void __launch_bounds__(256) k_stage(Dims d, const typename Vec<T>::t*
                                                typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
                                                const typename Vec<T>::t* __restrict__ src, int stage, double dt,
                                                Phys ph, unsigned int* flags) {
+    pdl_enter();
     if (stage_body<T>(d, Fu, Fv, S0, S1, Sdw, src, stage, dt, ph)) atomicOr(flags, 1u);
 }
 
@@ -116,6 +121,7 @@ __global__ void __launch_bounds__(512) k_xpass_rhs(Dims d, typename Vec<T>::t* I
                                                     T scale) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    pdl_enter();
     VT* bufs = reinterpret_cast<VT*>(smem_raw);
     const int g = threadIdx.x / d.Tg;
     const int lane = threadIdx.x - g * d.Tg;
@@ -590,15 +596,16 @@ cudaError_t Kern<T>::yinv(const Dims& d, const void* S, const double* rk2, const
     using VT = typename Vec<T>::t;
     const int ncg = (d.KX + L.G - 1) / L.G;
     const int nb = ncg * fs.nf;
+    const VT* s = (const VT*)S;
+    const VT* t = (const VT*)tw;
     switch (budget<T>(L.threads)) {
-        case 1: k_yinv<T, 1><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G); break;
+        case 1: return launch_k(k_yinv<T, 1>, nb, L.threads, L.smem, st, L.pdl, d, s, rk2, fs, t, L.G);
         case 2:
             if constexpr (sizeof(T) == 4)
-                k_yinv<T, 2><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
-            break;
-        default: k_yinv<T, 0><<<nb, L.threads, L.smem, st>>>(d, (const VT*)S, rk2, fs, (const VT*)tw, L.G);
+                return launch_k(k_yinv<T, 2>, nb, L.threads, L.smem, st, L.pdl, d, s, rk2, fs, t, L.G);
+            return cudaErrorInvalidConfiguration;
+        default: return launch_k(k_yinv<T, 0>, nb, L.threads, L.smem, st, L.pdl, d, s, rk2, fs, t, L.G);
     }
-    return cudaGetLastError();
 }
 
 template <typename T>
@@ -607,9 +614,8 @@ cudaError_t Kern<T>::xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw
     using VT = typename Vec<T>::t;
     const int pairs = d.M / 2;
     const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
-    k_xpass_rhs<T><<<(pairs + L.G - 1) / L.G, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)Iw,
-                                                                         (const VT*)tw, L.G, scale);
-    return cudaGetLastError();
+    return launch_k(k_xpass_rhs<T>, (pairs + L.G - 1) / L.G, L.threads, L.smem, st, L.pdl, d, (VT*)Iu, (VT*)Iv,
+                    (const VT*)Iw, (const VT*)tw, L.G, scale);
 }
 
 template <typename T>
@@ -618,15 +624,17 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
     using VT = typename Vec<T>::t;
     const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
     const int nb = (d.M + L.G - 1) / L.G;
+    VT* u = (VT*)Iu;
+    VT* v = (VT*)Iv;
+    const VT* t = (const VT*)tw;
     switch (budget<T>(L.threads)) {
-        case 1: k_xpass_bas<T, 1><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale); break;
+        case 1: return launch_k(k_xpass_bas<T, 1>, nb, L.threads, L.smem, st, L.pdl, d, u, v, t, L.G, scale);
         case 2:
             if constexpr (sizeof(T) == 4)
-                k_xpass_bas<T, 2><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale);
-            break;
-        default: k_xpass_bas<T, 0><<<nb, L.threads, L.smem, st>>>(d, (VT*)Iu, (VT*)Iv, (const VT*)tw, L.G, scale);
+                return launch_k(k_xpass_bas<T, 2>, nb, L.threads, L.smem, st, L.pdl, d, u, v, t, L.G, scale);
+            return cudaErrorInvalidConfiguration;
+        default: return launch_k(k_xpass_bas<T, 0>, nb, L.threads, L.smem, st, L.pdl, d, u, v, t, L.G, scale);
     }
-    return cudaGetLastError();
 }
 
 template <typename T>
@@ -634,10 +642,9 @@ cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, voi
                               const void* src, int stage, double dt, const Phys& ph, const void* tw,
                               unsigned int* flags, cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
-    k_yfwd_rk3<T><<<(d.KX + L.G - 1) / L.G, L.threads, L.smem, st>>>(
-        d, (const VT*)Iu, (const VT*)Iv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw,
-        L.G, flags);
-    return cudaGetLastError();
+    return launch_k(k_yfwd_rk3<T>, (d.KX + L.G - 1) / L.G, L.threads, L.smem, st, L.pdl, d, (const VT*)Iu,
+                    (const VT*)Iv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G,
+                    flags);
 }
 
 template <typename T>
@@ -647,25 +654,29 @@ cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, voi
     const int ncg = (d.KX + L.G - 1) / L.G;
     const VT* u = (const VT*)Iu;
     const VT* v = (const VT*)Iv;
+    const VT* t = (const VT*)tw;
     switch (budget<T>(L.threads)) {
-        case 1: k_yfwd_col<T, 1><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G); break;
+        case 1:
+            return launch_k(k_yfwd_col<T, 1>, 2 * ncg, L.threads, L.smem, st, L.pdl, d, u, v, (VT*)Fu, (VT*)Fv, t,
+                            L.G);
         case 2:
             if constexpr (sizeof(T) == 4)
-                k_yfwd_col<T, 2><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G);
-            break;
-        default: k_yfwd_col<T, 0><<<2 * ncg, L.threads, L.smem, st>>>(d, u, v, (VT*)Fu, (VT*)Fv, (const VT*)tw, L.G);
+                return launch_k(k_yfwd_col<T, 2>, 2 * ncg, L.threads, L.smem, st, L.pdl, d, u, v, (VT*)Fu,
+                                (VT*)Fv, t, L.G);
+            return cudaErrorInvalidConfiguration;
+        default:
+            return launch_k(k_yfwd_col<T, 0>, 2 * ncg, L.threads, L.smem, st, L.pdl, d, u, v, (VT*)Fu, (VT*)Fv, t,
+                            L.G);
     }
-    return cudaGetLastError();
 }
 
 template <typename T>
 cudaError_t Kern<T>::stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
                            const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
-                           cudaStream_t st) {
+                           cudaStream_t st, bool pdl) {
     using VT = typename Vec<T>::t;
-    k_stage<T><<<dim3((d.KY + 255) / 256, d.KX), 256, 0, st>>>(d, (const VT*)Fu, (const VT*)Fv, (VT*)S0, (VT*)S1,
-                                                                 (VT*)Sdw, (const VT*)src, stage, dt, ph, flags);
-    return cudaGetLastError();
+    return launch_k(k_stage<T>, dim3((d.KY + 255) / 256, d.KX), dim3(256), 0, st, pdl, d, (const VT*)Fu,
+                    (const VT*)Fv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, flags);
 }
 
 template <typename T>
