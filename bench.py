@@ -353,6 +353,70 @@ def run_les_batch(args, rank, world):
     return 0
 
 
+def run_les(args, rank, world):
+    """Single-run closure LES against the DNS (not the headline line): the
+    128^2 FP32 LES (192^2 collocation grid) with the trained closure
+    (spectral2d_gb300/data/closure_les128.npz; a seeded random network of the
+    same shape if absent), the same LES without it, and the 2048^2 FP64 DNS,
+    all from the filtered state of one seeded DNS initial condition (nu = 1e-4,
+    the DNS's CFL-0.5 dt for all three), timed with CUDA events on their
+    streams after the warm-up steps.  value = DNS ms/step over closure-LES
+    ms/step; the E(k) error of the closure at this ratio comes from the
+    20000-step evaluation (python -m spectral2d_gb300.closure)."""
+    import os
+    from spectral2d_gb300 import (ClosureNet, Spectral2D, closure, filter_state, les_integrate_steps,
+                                  les_set_closure, les_time_steps)
+    nd, nl, nu = 2048, 128, 1e-4
+    net = ClosureNet(3 * nl // 2, max_batch=1, seed=0)
+    wpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "spectral2d_gb300", "data",
+                         "closure_les128.npz")
+    if os.path.exists(wpath):
+        closure.load_weights(net, wpath)
+        weights = "trained 128^2 closure (spectral2d_gb300/data/closure_les128.npz)"
+    else:
+        net.set_scales([1.0, 1.0, 1.0])
+        weights = "seeded random network"
+    dns = Spectral2D(nd, nu=nu)
+    les = Spectral2D(nl, nu=nu, precision="fp32")
+    bare = Spectral2D(nl, nu=nu, precision="fp32")
+    dns.set_turbulent_velocity(seed=SEED + rank, spectrum="k4gauss", k0=10.0, tke=0.5)
+    dt = dns.compute_time_step(CFL)
+    filter_state(dns, les)
+    filter_state(dns, bare)
+    les_set_closure(les, net)
+    les_integrate_steps(les, args.warmup, dt)
+    bare.integrate_steps(args.warmup, dt)
+    dns.integrate_steps(args.warmup, dt)
+    for h in (les, bare, dns):   # nothing of another handle runs beside a timed one
+        h.synchronize()
+    ms_les = les_time_steps(les, args.steps, dt) / args.steps
+    ms_bare = bare.time_steps(args.steps, dt) / args.steps
+    kd = max(3, min(args.steps, 50))
+    ms_dns = dns.time_steps(kd, dt) / kd
+    les.check_finite()
+    net.status()
+    if rank == 0:
+        print(json.dumps({
+            "metric": "128^2 LES + learned closure: wall-clock per step vs the 2048^2 FP64 DNS at the same dt",
+            "value": ms_dns / ms_les, "unit": "x", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_les, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (LES), bf16 network, f64 (DNS)",
+            "data": "synthetic (seeded random-phase IC)",
+            "config": {"workload": "single 128^2 FP32 LES with the learned closure, one CUDA graph per step "
+                                   "(closure term on a second stream beside the first stage's transforms)",
+                       "n_les": nl, "n_dns": nd, "nu": nu, "cfl": CFL, "network": weights},
+            "ms_per_step_dns": ms_dns, "ms_per_step_les_no_closure": ms_bare,
+            "speedup_no_closure": ms_dns / ms_bare,
+            "speedup_at_10x_dns_dt": 10.0 * ms_dns / ms_les,
+            # per step: the RK3 kernels plus the closure's five transform and six convolution kernels
+            "gpu_launches": (les.kernels_per_step() + 11) * args.steps}), flush=True)
+    les_set_closure(les, None)
+    for h in (les, bare, dns):
+        h.close()
+    net.close()
+    return 0
+
+
 def workload_config(n, precision="fp64"):
     w = 16 if precision == "fp64" else 8
     ws = 2 * (n // 2 + 1) * (3 * n // 2) * w / 1e9   # the two half-spectral intermediates
@@ -373,7 +437,7 @@ def main():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--form", default="basdevant", choices=["basdevant", "conservative"])
-    ap.add_argument("--workload", default="dns", choices=["dns", "ensemble", "les-batch"])
+    ap.add_argument("--workload", default="dns", choices=["dns", "ensemble", "les-batch", "les"])
     ap.add_argument("--les-runs", type=int, default=256)
     ap.add_argument("--ens-check-steps", type=int, default=0)
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -389,6 +453,8 @@ def main():
         return run_ensemble(args, rank, world)
     if args.workload == "les-batch":
         return run_les_batch(args, rank, world)
+    if args.workload == "les":
+        return run_les(args, rank, world)
 
     # CPU baseline first (no GPU context yet in this process)
     cpu = None

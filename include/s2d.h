@@ -324,6 +324,9 @@ S2D_API int s2d_les_closure_term(s2d_handle* les);
 /* n steps; with a closure attached, -Pi^ of the state at the start of each
  * step is added to dW in its three RK3 stages */
 S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt);
+/* as s2d_les_integrate_steps with a closure attached, timed: *ms = device
+ * time of the n steps on the handle's stream (CUDA events) */
+S2D_API int s2d_les_time_steps(s2d_handle* les, int32_t n, double dt, double* ms);
 /* attach (c != NULL) or detach one closure network for every run of a batch:
  * all runs on the network's grid, at most its max_batch runs.  Each batch
  * step then starts with the closure terms of all runs -- one network forward

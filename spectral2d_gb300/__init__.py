@@ -7,7 +7,7 @@ hand-written CUDA kernels in ``libspectral2d_gb300.so`` behind the C-ABI of
 
 from ._lib import S2DError, lib  # noqa: F401
 from .solver import (ClosureNet, Ensemble, Spectral2D, filter_state, get_grid_size,  # noqa: F401
-                     les_integrate_steps, les_set_closure, probe_fp64_peak, subgrid_flux,
+                     les_integrate_steps, les_set_closure, les_time_steps, probe_fp64_peak, subgrid_flux,
                      turbulent_ic_host)
 
 __all__ = ["Spectral2D", "Ensemble", "get_grid_size", "turbulent_ic_host", "probe_fp64_peak", "S2DError", "lib"]

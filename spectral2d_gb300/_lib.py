@@ -123,6 +123,7 @@ SIGNATURES = {
     "s2d_les_set_closure": (C.c_int, [C.c_void_p, C.c_void_p]),
     "s2d_les_closure_term": (C.c_int, [C.c_void_p]),
     "s2d_les_integrate_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_double]),
+    "s2d_les_time_steps": (C.c_int, [C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double)]),
     "s2d_batch_set_closure": (C.c_int, [C.c_void_p, C.c_void_p]),
     "s2d_skewness": (C.c_int, [_h, _dp, _dp]),
     "s2d_checkpoint_write": (C.c_int, [_h, C.c_char_p, C.c_int64, C.c_double]),

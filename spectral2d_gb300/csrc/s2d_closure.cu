@@ -887,15 +887,16 @@ __global__ void __launch_bounds__(512) k_cl_ystore(Dims d, const LesRun<T>* __re
     const int lane = threadIdx.x - g * d.Tg;
     const int kx0 = blockIdx.x * G;
     const int gtot = min(G, d.KX - kx0);
+    const DivBy byG(G), byKY(d.KY);
     for (int idx = threadIdx.x; idx < G * d.M; idx += blockDim.x) {
-        const int gg = idx % G;
-        const int y = idx / G;
+        const int y = byG(idx);
+        const int gg = idx - y * G;
         bufs[(size_t)gg * d.M + y] = gg < gtot ? __ldcg(&R.I2[(size_t)y * d.ldI + kx0 + gg]) : mk<VT>((T)0, (T)0);
     }
     fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
     __syncthreads();
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
-        const int gg = idx / d.KY;
+        const int gg = byKY(idx);
         const int jc = idx - gg * d.KY;
         const int kx = kx0 + gg;
         const int ky = ky_of_jc(d, jc);
@@ -1270,6 +1271,39 @@ int s2d::cnn_max_batch(const s2d_cnn* c) { return c->maxB; }
 int s2d::physical_pair(s2d_handle* h, const void* S, int opA, int opB, void* outA, void* outB) {
     return h->prec == S2D_FP64 ? physical_pair_t<double>(h, S, opA, opB, outA, outB)
                                : physical_pair_t<float>(h, S, opA, opB, outA, outB);
+}
+
+// One LES step as an executable CUDA graph: the closure term of the state at
+// the start of the step on clstream, concurrently with the first stage's
+// inverse y-pass and x-pass on the handle's stream; the first stage's
+// epilogue (the first reader of src) waits for it.  Rebuilt by every caller,
+// so that it picks up new network scales and dt.
+static int les_step_graph(s2d_handle* les, double dt, cudaGraphExec_t* out) {
+    if (!std::isfinite(dt)) return cerr(S2D_ERR_INVALID, "dt must be finite");
+    if (!les->src || !les->les_tab || !les->clstream) return cerr(S2D_ERR_INVALID, "no closure set");
+    C_CUDA(cudaSetDevice(les->device));
+    C_CUDA(cudaStreamBeginCapture(les->stream, cudaStreamCaptureModeThreadLocal));
+    int r = S2D_OK;
+    cudaError_t ec = cudaEventRecord(les->ev_fork, les->stream);
+    if (ec == cudaSuccess) ec = cudaStreamWaitEvent(les->clstream, les->ev_fork, 0);
+    if (ec == cudaSuccess) {
+        r = s2d::closure_terms(les->cnn, &les, 1, les->les_tab, les->clstream);
+        // the join is recorded even after a failure, so that the capture can end
+        ec = cudaEventRecord(les->ev_join, les->clstream);
+    }
+    if (ec != cudaSuccess && r == S2D_OK) r = cerr(S2D_ERR_CUDA, cudaGetErrorString(ec));
+    if (r == S2D_OK) r = s2d::launch_step_sourced(les, dt, les->ev_join);
+    else cudaStreamWaitEvent(les->stream, les->ev_join, 0);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(les->stream, &g);
+    if (r != S2D_OK || e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return r != S2D_OK ? r : cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const cudaError_t e2 = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    if (e2 != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e2));
+    return S2D_OK;
 }
 
 extern "C" {
@@ -1726,40 +1760,37 @@ S2D_API int s2d_les_integrate_steps(s2d_handle* les, int32_t n, double dt) {
     if (!les || n < 0) return cerr(S2D_ERR_INVALID, "bad argument");
     if (!les->cnn) return s2d_integrate_steps(les, n, dt);
     if (n == 0) return S2D_OK;
-    if (!std::isfinite(dt)) return cerr(S2D_ERR_INVALID, "dt must be finite");
-    if (!les->src || !les->les_tab || !les->clstream) return cerr(S2D_ERR_INVALID, "no closure set");
-    C_CUDA(cudaSetDevice(les->device));
-    // one step captured as a CUDA graph, rebuilt on every call so that it
-    // picks up new network scales and dt: the closure term of the state at the
-    // start of the step on clstream, concurrently with the first stage's
-    // inverse y-pass and x-pass on the handle's stream; the first stage's
-    // epilogue (the first reader of src) waits for it
-    C_CUDA(cudaStreamBeginCapture(les->stream, cudaStreamCaptureModeThreadLocal));
-    int r = S2D_OK;
-    cudaError_t ec = cudaEventRecord(les->ev_fork, les->stream);
-    if (ec == cudaSuccess) ec = cudaStreamWaitEvent(les->clstream, les->ev_fork, 0);
-    if (ec == cudaSuccess) {
-        r = s2d::closure_terms(les->cnn, &les, 1, les->les_tab, les->clstream);
-        // the join is recorded even after a failure, so that the capture can end
-        ec = cudaEventRecord(les->ev_join, les->clstream);
-    }
-    if (ec != cudaSuccess && r == S2D_OK) r = cerr(S2D_ERR_CUDA, cudaGetErrorString(ec));
-    if (r == S2D_OK) r = s2d::launch_step_sourced(les, dt, les->ev_join);
-    else cudaStreamWaitEvent(les->stream, les->ev_join, 0);
-    cudaGraph_t g = nullptr;
-    const cudaError_t e = cudaStreamEndCapture(les->stream, &g);
-    if (r != S2D_OK || e != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        return r != S2D_OK ? r : cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
-    }
     cudaGraphExec_t x = nullptr;
-    const cudaError_t e2 = cudaGraphInstantiate(&x, g, 0);
-    cudaGraphDestroy(g);
-    if (e2 != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e2));
-    cudaError_t e3 = cudaSuccess;
-    for (int i = 0; i < n && e3 == cudaSuccess; ++i) e3 = cudaGraphLaunch(x, les->stream);
+    const int r = les_step_graph(les, dt, &x);
+    if (r != S2D_OK) return r;
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaGraphLaunch(x, les->stream);
     cudaGraphExecDestroy(x);
-    if (e3 != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e3));
+    if (e != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    return S2D_OK;
+}
+
+S2D_API int s2d_les_time_steps(s2d_handle* les, int32_t n, double dt, double* ms) {
+    if (!les || n <= 0 || !ms) return cerr(S2D_ERR_INVALID, "bad argument");
+    if (!les->cnn) return cerr(S2D_ERR_INVALID, "no closure set");
+    cudaGraphExec_t x = nullptr;
+    int r = les_step_graph(les, dt, &x);
+    if (r != S2D_OK) return r;
+    cudaEvent_t a = nullptr, b = nullptr;
+    cudaError_t e = cudaEventCreate(&a);
+    if (e == cudaSuccess) e = cudaEventCreate(&b);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(les->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(a, les->stream);
+    for (int i = 0; i < n && e == cudaSuccess; ++i) e = cudaGraphLaunch(x, les->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(b, les->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(b);
+    float f = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&f, a, b);
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    cudaGraphExecDestroy(x);
+    if (e != cudaSuccess) return cerr(S2D_ERR_CUDA, cudaGetErrorString(e));
+    *ms = f;
     return S2D_OK;
 }
 

@@ -135,6 +135,19 @@ struct ModNs {
     }
 };
 
+// floor(n / d) by the same multiply-high with m = ceil(2^32 / d), built once
+// per thread (one division) and used per element: exact while
+// n (m d - 2^32) < 2^32, which holds for the index splits of the column
+// gathers and stores (n < 2^17, d < 2^14).  Small plans take G > 1
+// transforms per CTA, and a division per element there was a third of the
+// instructions of their latency-bound column kernels.
+struct DivBy {
+    int d;
+    unsigned m;
+    __device__ __forceinline__ explicit DivBy(int dd) : d(dd), m(dd > 1 ? 0xFFFFFFFFu / (unsigned)dd + 1u : 0u) {}
+    __device__ __forceinline__ int operator()(int n) const { return d == 1 ? n : (int)__umulhi((unsigned)n, m); }
+};
+
 // One in-place Stockham pass of radix R over the transform in buf.
 template <int R, bool INV, typename VT>
 __device__ __forceinline__ void fft_pass(VT* buf, int M, int Ns, unsigned mg, int tstep, int lane, int Tg,

@@ -119,8 +119,9 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
     if (G == 1) {   // no integer division per element (it competes with the FP64 pipe)
         for (int y = threadIdx.x; y < d.M; y += blockDim.x) out[(size_t)y * d.ldI + kx0] = bufs[y];
     } else {
+        const DivBy byG(G);
         for (int idx = threadIdx.x; idx < d.M * G; idx += blockDim.x) {
-            const int y = idx / G;
+            const int y = byG(idx);
             const int gg = idx - y * G;
             if (gg < gtot) out[(size_t)y * d.ldI + kx0 + gg] = bufs[(size_t)gg * d.M + y];
         }
@@ -275,6 +276,7 @@ __device__ __forceinline__ void gather_columns(const Dims& d, const typename Vec
                                                int n, typename Vec<T>::t* bufs) {
     using VT = typename Vec<T>::t;
     constexpr int kU = sizeof(T) == 8 ? 4 : 8;
+    const DivBy byG(G), byM(d.M);
     for (int base = threadIdx.x; base < n; base += kU * blockDim.x) {
         VT v[kU];
         int dst[kU];
@@ -289,10 +291,10 @@ __device__ __forceinline__ void gather_columns(const Dims& d, const typename Vec
                     fld = idx >= d.M;
                     y = idx - fld * d.M;
                 } else {
-                    gg = idx % G;
-                    const int rest = idx / G;
-                    y = rest % d.M;
-                    fld = rest / d.M;
+                    const int rest = byG(idx);
+                    gg = idx - rest * G;
+                    fld = byM(rest);
+                    y = rest - fld * d.M;
                 }
                 dst[u] = (fld * G + gg) * d.M + y;
                 if (gg < gtot) v[u] = __ldcg(&(fld ? Y : X)[(size_t)y * d.ldI + kx0 + gg]);
@@ -324,8 +326,9 @@ __device__ __forceinline__ void yfwd_col_body(const Dims& d, const typename Vec<
     gather_columns<T>(d, I, I, G, gtot, kx0, G * d.M, bufs);
     fft_run<false>(bufs + (size_t)g * d.M, d, lane, tw);
     __syncthreads();
+    const DivBy byKY(d.KY);
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
-        const int gg = gtot == 1 ? 0 : idx / d.KY;
+        const int gg = gtot == 1 ? 0 : byKY(idx);
         const int jc = idx - gg * d.KY;
         const int n = jc <= d.K ? jc : ky_of_jc(d, jc) + d.M;
         Out[(size_t)(kx0 + gg) * d.ldS + jc] = bufs[(size_t)gg * d.M + n];
@@ -380,8 +383,9 @@ __device__ __forceinline__ bool yfwd_body(const Dims& d, const typename Vec<T>::
     __syncthreads();
 
     bool bad = false;
+    const DivBy byKY(d.KY);
     for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
-        const int gg = gtot == 1 ? 0 : idx / d.KY;
+        const int gg = gtot == 1 ? 0 : byKY(idx);
         const int jc = idx - gg * d.KY;
         const int ky = ky_of_jc(d, jc);
         const int n = jc <= d.K ? jc : ky + d.M;

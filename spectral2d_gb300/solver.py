@@ -354,6 +354,11 @@ class ClosureNet:
             self._L.s2d_cnn_destroy(self._c)
             self._c = None
 
+    def status(self) -> None:
+        """Raises if a tensor-core completion wait of the network's kernels
+        gave up since the last check (clears the flag)."""
+        L.check(self._L.s2d_cnn_status(self._c))
+
     def __enter__(self):
         return self
 
@@ -461,3 +466,11 @@ def les_set_closure(les: Spectral2D, net: ClosureNet | None) -> None:
 
 def les_integrate_steps(les: Spectral2D, n: int, dt: float) -> None:
     L.check(L.lib().s2d_les_integrate_steps(les._h, n, dt))
+
+
+def les_time_steps(les: Spectral2D, n: int, dt: float) -> float:
+    """Device time (ms, CUDA events on the handle's stream) of n closure-LES
+    steps of ``les_integrate_steps``."""
+    ms = C.c_double()
+    L.check(L.lib().s2d_les_time_steps(les._h, n, dt, C.byref(ms)))
+    return ms.value

@@ -126,3 +126,32 @@ def test_fortran_interfaces_match_the_header(built_lib):
         assert nargs == nparams, (cname, nargs, nparams)
         assert ("SUBROUTINE" in kind) == (ret == "void"), (cname, kind, ret)
         assert hasattr(lib, cname), cname
+
+
+def test_multiply_high_quotients_are_exact_over_the_kernels_index_ranges():
+    """The kernels split indices with q = floor(n m / 2^32), m = ceil(2^32 / d)
+    (FFT passes: j mod Ns; column gathers and stores: n / G, n / M, n / KY)
+    instead of an integer division.  The bound n (m d - 2^32) < 2^32 makes q
+    exact for n < 2^17, d < 2^14; checked here for every d of that range that
+    a plan can produce (G, Ns, M, KY: 1..4097 and the M = 3 * 2^a * 3^b up to
+    6144) and every n < 2^17."""
+    import numpy as np
+    n = np.arange(1 << 17, dtype=np.uint64)
+    ds = set(range(1, 4098))
+    ds |= {m for m in range(12, 6145, 12) if all(p in (2, 3) for p in _prime_factors(m))}
+    for d in sorted(ds):
+        m = np.uint64((0xFFFFFFFF // d + 1) & 0xFFFFFFFF if d > 1 else 0)
+        q = n if d == 1 else (n * m) >> np.uint64(32)
+        assert np.array_equal(q, n // np.uint64(d)), d
+
+
+def _prime_factors(m):
+    out, p = [], 2
+    while p * p <= m:
+        while m % p == 0:
+            out.append(p)
+            m //= p
+        p += 1
+    if m > 1:
+        out.append(m)
+    return out

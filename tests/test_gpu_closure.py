@@ -164,6 +164,31 @@ def test_les_with_closure_runs_and_changes_the_solution(S, precision):
     assert 1e-8 < d < 0.5
 
 
+def test_timed_closure_steps_match_untimed_ones(S):
+    """s2d_les_time_steps runs the same step graph as s2d_les_integrate_steps
+    (closure term on a second stream beside the first stage's transforms):
+    same bits after the same steps, and a positive device time."""
+    n, nu, steps = 16, 2e-3, 8
+    with S.ClosureNet(24, max_batch=8, seed=7) as net:
+        dt = _dataset(S, net, nsnap=8)
+        net.set_scales(net.dataset_stats())
+        w0 = O.random_state(O.get_grid_size(n, n), 21, decay=0.2)
+        out = []
+        for timed in (False, True):
+            with S.Spectral2D(n, nu=nu, precision="fp32") as a:
+                a.set_state(w0)
+                S.les_set_closure(a, net)
+                if timed:
+                    ms = S.les_time_steps(a, steps, dt)
+                    assert ms > 0.0
+                else:
+                    S.les_integrate_steps(a, steps, dt)
+                out.append(a.get_state()[0])
+                S.les_set_closure(a, None)
+        net.status()
+    assert np.array_equal(out[0], out[1])
+
+
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_batched_closure_les_matches_single_runs(S, precision):
     """A batch of LES runs with one closure network (one forward over all

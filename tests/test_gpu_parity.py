@@ -415,3 +415,25 @@ def test_handles_from_several_host_threads(S2D):
     assert not errs, errs
     for a, b in zip(out, serial):
         assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+@pytest.mark.parametrize("n", [96, 1024])
+def test_programmatic_launches_give_the_plain_order_bits(S2D, monkeypatch, precision, n):
+    """Every kernel of a step is launched as a programmatic dependent of the
+    one before it (it waits for its predecessor's completion before touching
+    memory): the state after 20 steps is bit-identical to plain stream order
+    (S2D_PDL=0, read when the handle is created).  FP64 handles take the split
+    K3 (column FFTs, then the stage kernel), FP32 the fused one."""
+    g = O.get_grid_size(n, n)
+    w0 = O.random_state(g, 60, decay=0.1)
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("S2D_PDL", mode)
+        with S2D(n, nu=1e-3, precision=precision) as s:
+            s.set_state(w0)
+            dt = s.compute_time_step(0.5)
+            s.integrate_steps(20, dt)
+            s.check_finite()
+            out[mode] = s.get_state()[0]
+    assert np.array_equal(out["0"], out["1"])
