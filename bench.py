@@ -180,11 +180,14 @@ def dist_env():
 
 
 # ---------------------------------------------------------------------------
-def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float, cores: int | None = None):
+def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float, cores: int | None = None,
+                  min_steps: int = 5):
     """Time the oracle (FP64 CPU restatement) on all host cores (or on
-    ``cores`` threads).  Returns (Mpt*steps/s, timed steps, cores, seconds per
-    step)."""
-    import numpy as np  # noqa: F401
+    ``cores`` threads): ``warmup`` untimed steps, then steps timed one by one
+    until ``steps`` or until ``budget_s`` seconds have passed after at least
+    ``min_steps``.  Returns (Mpt*steps/s from the median step time, timed
+    steps, cores, median seconds per step)."""
+    import numpy as np
     import oracle as O
     cores = cores or O.cpu_count()
     O.set_workers(cores)
@@ -193,14 +196,15 @@ def cpu_step_rate(n: int, steps: int, warmup: int, budget_s: float, cores: int |
     dt = O.cfl_dt(w, g, CFL)
     for _ in range(warmup):
         w, psi = O.integrate_one_step(w, psi, g, NU, dt)
-    done, t0 = 0, time.perf_counter()
-    while done < steps:
+    times, t0 = [], time.perf_counter()
+    while len(times) < steps:
+        t = time.perf_counter()
         w, psi = O.integrate_one_step(w, psi, g, NU, dt)
-        done += 1
-        if time.perf_counter() - t0 > budget_s:
+        times.append(time.perf_counter() - t)
+        if len(times) >= min(min_steps, steps) and time.perf_counter() - t0 > budget_s:
             break
-    el = time.perf_counter() - t0
-    return n * n * done / el / 1e6, done, cores, el / done
+    med = float(np.median(times))
+    return n * n / med / 1e6, len(times), cores, med
 
 
 def run_reference(args, rank, world):
@@ -216,7 +220,7 @@ def run_reference(args, rank, world):
         "data": "synthetic (seeded random-phase IC)",
         "config": workload_config(args.n),
         "cpu_baseline": {"value": rate, "unit": "Mpt*steps/s", "cores": cores, "kind": "port",
-                         "sample": f"{done} RK3 steps of the {args.n}^2 FP64 workload, "
+                         "sample": f"median of {done} timed RK3 steps of the {args.n}^2 FP64 workload, "
                                    f"numpy/scipy.fft restatement of the reference, {cores} threads"},
         "e2e": {"value": rate, "unit": "Mpt*steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -459,14 +463,15 @@ def main():
     # CPU baseline first (no GPU context yet in this process)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        # a bounded sample: one warm-up step, then steps until cpu_budget seconds
+        # a bounded sample: one warm-up step, then at least 5 timed steps and
+        # more until cpu_budget seconds; the rate is that of the median step
         rate, done, cores, sps = cpu_step_rate(args.n, 10000, 1, budget_s=args.cpu_budget)
         cpu = {"value": rate, "unit": "Mpt*steps/s", "cores": cores, "kind": "port",
-               "sample": f"{done} RK3 step(s) of the {args.n}^2 FP64 workload after 1 warm-up step, "
-                         f"numpy/scipy.fft restatement of the reference on {cores} threads "
+               "sample": f"median of {done} timed RK3 steps of the {args.n}^2 FP64 workload after 1 "
+                         f"warm-up step, numpy/scipy.fft restatement of the reference on {cores} threads "
                          f"({sps:.2f} s/step)"}
         if cores > 1:
-            r1, d1, _, s1 = cpu_step_rate(args.n, 10000, 0, budget_s=args.cpu_budget / 2, cores=1)
+            r1, d1, _, s1 = cpu_step_rate(args.n, 10000, 1, budget_s=args.cpu_budget / 2, cores=1)
             cpu["one_core"] = {"value": r1, "unit": "Mpt*steps/s", "cores": 1, "steps": d1, "s_per_step": s1}
 
     import numpy as np
