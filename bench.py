@@ -412,8 +412,8 @@ def run_les(args, rank, world):
             "ms_per_step_dns": ms_dns, "ms_per_step_les_no_closure": ms_bare,
             "speedup_no_closure": ms_dns / ms_bare,
             "speedup_at_10x_dns_dt": 10.0 * ms_dns / ms_les,
-            # per step: the RK3 kernels plus the closure's five transform and six convolution kernels
-            "gpu_launches": (les.kernels_per_step() + 11) * args.steps}), flush=True)
+            # per step: the RK3 kernels plus the closure's four transform and six convolution kernels
+            "gpu_launches": (les.kernels_per_step() + 10) * args.steps}), flush=True)
     les_set_closure(les, None)
     for h in (les, bare, dns):
         h.close()

@@ -223,7 +223,6 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
     __shared__ uint32_t tmem_base;
     __shared__ int s_ok;
 
-    pdl_enter();   // before the TMEM allocation: a waiting CTA holds no columns
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
     const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
@@ -258,6 +257,14 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     const uint32_t tmem = tmem_base;
+    // Launched as a programmatic dependent (the closure's inference chain
+    // only, where the weights do not change), the prologue above -- TMEM
+    // columns, barriers, the layer's weights -- overlaps the previous kernel;
+    // the input activations and the outputs are touched only after this.  A
+    // waiting CTA holds 32 TMEM columns: at most eight CTAs of 256 threads
+    // share an SM (2048 threads), 256 of its 512 columns, so no allocation
+    // waits on a CTA that waits in turn.
+    pdl_enter();
 
     // thread 0's bookkeeping: the parity to wait for on each barrier and what
     // is in flight
@@ -746,10 +753,8 @@ struct LesRun {
     typename Vec<T>::t* I0;
     typename Vec<T>::t* I1;
     typename Vec<T>::t* I2;
-    T* pw;          // physical w on the M x M collocation grid
-    T* pp;          // physical psi
     typename Vec<T>::t* src;   // -Pi^ (compact layout)
-    double* part;   // sums of w^2 per row tile of k_cl_xinv; part[nparts]: their mean per point
+    double* part;   // sums of |w^|^2 per column tile of k_cl_yinv; part[nparts]: their total
 };
 
 // Sum of the nparts partial sums by one warp in a fixed order (lane l adds
@@ -763,7 +768,11 @@ __device__ __forceinline__ double warp_ordered_sum(const double* __restrict__ pa
     return s;
 }
 
-// K1 of (w, psi): inverse y-pass of every run's state.
+// K1 of (w, psi): inverse y-pass of every run's state.  The CTAs of the w
+// field also sum |w^|^2 over their columns (kx > 0 twice: the other half of
+// the spectrum), which by Parseval is the mean of w^2 over the collocation
+// grid (the inverse transform is unnormalised); per thread, then a fixed
+// tree over the CTA, into part[column tile].
 template <typename T>
 __global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __restrict__ runs,
                                                   const double* __restrict__ rk2,
@@ -779,35 +788,20 @@ __global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __rest
     fs.out[0] = R.I0;
     fs.out[1] = R.I1;
     yinv_body<T>(d, R.S0, rk2, fs, tw, G, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
-}
-
-// Physical rows of w and psi (one inverse FFT of W + i PSI per row) and the
-// tile's sum of w^2 (fixed order: per thread, then warps in order).
-template <typename T>
-__global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
-                                                  const typename Vec<T>::t* __restrict__ tw, int G) {
-    using VT = typename Vec<T>::t;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_enter();
-    const LesRun<T>& R = runs[blockIdx.y];
-    VT* bufs = reinterpret_cast<VT*>(smem_raw);
-    const int g = threadIdx.x / d.Tg;
-    const int lane = threadIdx.x - g * d.Tg;
-    const int y = blockIdx.x * G + g;
-    const bool active = y < d.M;
-    const int yy = active ? y : 0;
-    VT* Z = bufs + (size_t)g * d.M;
-    build_pair(Z, R.I0 + (size_t)yy * d.ldI, R.I1 + (size_t)yy * d.ldI, d, lane, active);
-    fft_run<true>(Z, d, lane, tw);
+    const int ncg = (d.KX + G - 1) / G;
+    if ((int)blockIdx.x >= ncg) return;   // the psi field's CTAs (uniform per CTA)
+    const int kx0 = blockIdx.x * G;
+    const int gtot = min(G, d.KX - kx0);
+    const DivBy byKY(d.KY);
     double s = 0.0;
-    if (active)
-        for (int n = lane; n < d.M; n += d.Tg) {
-            const VT z = Z[n];
-            R.pw[(size_t)y * d.M + n] = z.x;
-            R.pp[(size_t)y * d.M + n] = z.y;
-            s += (double)z.x * (double)z.x;
-        }
-    // tree over the CTA in the (now free) FFT buffers: G*M*16 B >= 8 B per thread
+    for (int idx = threadIdx.x; idx < gtot * d.KY; idx += blockDim.x) {
+        const int gg = byKY(idx);
+        const int kx = kx0 + gg;
+        const VT v = __ldcg(&R.S0[(size_t)kx * d.ldS + (idx - gg * d.KY)]);
+        const double m = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        s += kx > 0 ? 2.0 * m : m;
+    }
+    // tree over the CTA in the (now free) FFT buffers: G*M*vsz >= 8 B per thread
     double* red = reinterpret_cast<double*>(smem_raw);
     __syncthreads();
     red[threadIdx.x] = s;
@@ -821,28 +815,45 @@ __global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __rest
     if (threadIdx.x == 0) R.part[blockIdx.x] = red[0];
 }
 
-// Network input of every run: (w / (a s0), psi / (a s1)), a = rms w of the
-// run; the mean of w^2 is kept in part[nparts] for k_cl_xfwd.  Only channels
-// 0 and 1 of x are written: channels 2..15 of the input buffer are zero from
-// its allocation on, and every writer of it keeps them so.
+// Physical rows of w and psi (one inverse FFT of W + i PSI per row), written
+// as the network input of every run: (w / (a s0), psi / (a s1)) in BF16, a =
+// rms w of the run from the nparts sums of k_cl_yinv (their total, the mean
+// of w^2, is kept in part[nparts] for k_cl_xfwd).  Only channels 0 and 1 of
+// x are written: channels 2..15 of the input buffer are zero from its
+// allocation on, and every writer of it keeps them so.
 template <typename T>
-__global__ void k_cl_pack(const LesRun<T>* __restrict__ runs, int nparts, long HW, float r0, float r1,
-                          __nv_bfloat16* x) {
+__global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
+                                                  const typename Vec<T>::t* __restrict__ tw, int G, int nparts,
+                                                  float r0, float r1, __nv_bfloat16* x) {
+    using VT = typename Vec<T>::t;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double s_ia;
     pdl_enter();
     const LesRun<T>& R = runs[blockIdx.y];
     if (threadIdx.x < 32) {
-        const double mean = warp_ordered_sum(R.part, nparts, threadIdx.x) / (double)HW;
+        const double mean = warp_ordered_sum(R.part, nparts, threadIdx.x);
         if (threadIdx.x == 0) {
             s_ia = 1.0 / sqrt(mean);
             if (blockIdx.x == 0) R.part[nparts] = mean;
         }
     }
-    __syncthreads();
+    VT* bufs = reinterpret_cast<VT*>(smem_raw);
+    const int g = threadIdx.x / d.Tg;
+    const int lane = threadIdx.x - g * d.Tg;
+    const int y = blockIdx.x * G + g;
+    const bool active = y < d.M;
+    const int yy = active ? y : 0;
+    VT* Z = bufs + (size_t)g * d.M;
+    build_pair(Z, R.I0 + (size_t)yy * d.ldI, R.I1 + (size_t)yy * d.ldI, d, lane, active);
+    fft_run<true>(Z, d, lane, tw);   // begins with a barrier: s_ia is visible after it
     const T a0 = (T)((double)r0 * s_ia), a1 = (T)((double)r1 * s_ia);
-    __nv_bfloat16* xb = x + (size_t)blockIdx.y * HW * 16;
-    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < HW; i += (long)gridDim.x * blockDim.x)
-        *reinterpret_cast<uint32_t*>(xb + i * 16) = pack_bf16((float)(R.pw[i] * a0), (float)(R.pp[i] * a1));
+    if (active) {
+        uint32_t* xr = reinterpret_cast<uint32_t*>(x + ((size_t)blockIdx.y * d.M + y) * (size_t)d.M * 16);
+        for (int n = lane; n < d.M; n += d.Tg) {
+            const VT z = Z[n];
+            xr[(size_t)n * 8] = pack_bf16((float)(z.x * a0), (float)(z.y * a1));
+        }
+    }
 }
 
 // Network output -> -Pi on the grid (scale a^2 y, scale = -s2), forward x-FFT
@@ -1162,15 +1173,15 @@ int ensure_les_buffers(s2d_handle* h) {
     return S2D_OK;
 }
 
-// LesRun table of n runs followed by n * nparts partial sums.
+// LesRun table of n runs followed by M + 1 doubles per run: the partial
+// sums of k_cl_yinv (one per column tile, at most M) and their total.
 int closure_table_impl(s2d_handle* const* runs, int n, void** tab) {
     const s2d_handle* h0 = runs[0];
-    const int nparts = (h0->d.M + h0->L_xrow.G - 1) / h0->L_xrow.G;
+    const size_t pstride = (size_t)h0->d.M + 1;
     const size_t head = (size_t)n * sizeof(LesRun<double>);
     void* t = nullptr;
-    C_CUDA(cudaMalloc(&t, head + (size_t)n * (nparts + 1) * sizeof(double)));
+    C_CUDA(cudaMalloc(&t, head + (size_t)n * pstride * sizeof(double)));
     std::vector<LesRun<double>> rows(n);
-    const long HW = (long)h0->d.M * h0->d.M;
     for (int i = 0; i < n; ++i) {
         s2d_handle* h = runs[i];
         LesRun<double>& R = rows[i];
@@ -1182,10 +1193,8 @@ int closure_table_impl(s2d_handle* const* runs, int n, void** tab) {
         R.I1 = (double2*)(ib ? ib + h->Ibytes : h->I[1]);
         R.I2 = (double2*)(ib ? ib + 2 * h->Ibytes : h->I[2]);
         // phys holds M*M 8-byte elements per field; FP32 runs use the front half
-        R.pw = (double*)h->phys;
-        R.pp = h->prec == S2D_FP64 ? R.pw + HW : (double*)((float*)h->phys + HW);
         R.src = (double2*)h->src;
-        R.part = (double*)((char*)t + head) + (size_t)i * (nparts + 1);
+        R.part = (double*)((char*)t + head) + (size_t)i * pstride;
     }
     const cudaError_t e = cudaMemcpy(t, rows.data(), head, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
@@ -1202,19 +1211,15 @@ int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab,
     const s2d_handle* h0 = runs[0];
     const Dims& d = h0->d;
     const LesRun<T>* R = (const LesRun<T>*)tab;
-    const long HW = (long)d.M * d.M;
     const Launch& Ly = h0->L_yinv;
     const Launch& Lx = h0->L_xrow;
     const Launch& Ls = h0->L_ystore;
-    const int nparts = (d.M + Lx.G - 1) / Lx.G;
+    const int nparts = (d.KX + Ly.G - 1) / Ly.G;   // k_cl_yinv's column tiles of the w field
     const VT* tw = (const VT*)h0->tw;
     const bool pdl = Ly.pdl;
-    C_CUDA(launch_k(k_cl_yinv<T>, dim3(2 * ((d.KX + Ly.G - 1) / Ly.G), n), Ly.threads, Ly.smem, st, pdl, d, R,
-                    h0->rk2, tw, Ly.G));
-    C_CUDA(launch_k(k_cl_xinv<T>, dim3(nparts, n), Lx.threads, Lx.smem, st, pdl, d, R, tw, Lx.G));
-    const int chunks = (int)std::min<long>((HW + 255) / 256, 64);
-    C_CUDA(launch_k(k_cl_pack<T>, dim3(chunks, n), 256, 0, st, pdl, R, nparts, HW, (float)(1.0 / c->scale[0]),
-                    (float)(1.0 / c->scale[1]), c->X0));
+    C_CUDA(launch_k(k_cl_yinv<T>, dim3(2 * nparts, n), Ly.threads, Ly.smem, st, pdl, d, R, h0->rk2, tw, Ly.G));
+    C_CUDA(launch_k(k_cl_xinv<T>, dim3((d.M + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st, pdl, d, R, tw, Lx.G,
+                    nparts, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]), c->X0));
     // the network runs on the caller's stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
     c->stream = st;
