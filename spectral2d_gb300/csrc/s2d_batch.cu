@@ -112,8 +112,7 @@ __global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict
                 fs.out[1] = R.I1;
                 yinv_body<T>(R.d, stage <= 1 ? R.S0 : R.S1, R.rk2, fs, R.tw, R.G12, blk, bufs);
             } else if (ph == 1) {
-                const T scale = (T)(0.5 / ((double)R.d.M * (double)R.d.M));
-                xpass_bas_body<T>(R.d, R.I0, R.I1, R.tw, R.G12, scale, blk, bufs);
+                xpass_bas_body<T>(R.d, R.I0, R.I1, R.tw, R.G12, (T)1, blk, bufs);
             } else {
                 bad |= yfwd_body<T>(R.d, R.I0, R.I1, R.S0, R.S1, nullptr, R.src, stage, R.dt, R.ph, R.tw, R.G3,
                                     blk, bufs);
@@ -224,7 +223,7 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
         R.I0 = (VT*)h->I[0];
         R.I1 = (VT*)h->I[1];
         R.src = b->cnn ? (const VT*)h->src : nullptr;
-        R.rk2 = h->rk2;
+        R.rk2 = h->rk2s;   // Basdevant runs: u, v prescaled (no scale in the x-pass)
         R.tw = (const VT*)h->tw;
         R.dt = b->dt[i];
         const int Tg = h->d.Tg;

@@ -193,9 +193,9 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
     fs.out[2] = h->I[2];
     const void* win = (stage <= 1) ? h->S0 : h->S1;
     if (ev) S2D_CUDA(cudaEventRecord(ev[0], h->stream));
-    S2D_CUDA(Kern<T>::yinv(d, win, h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    S2D_CUDA(Kern<T>::yinv(d, win, bas ? h->rk2s : h->rk2, fs, h->tw, h->stream, h->L_yinv));
     if (ev) S2D_CUDA(cudaEventRecord(ev[1], h->stream));
-    if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow));
+    if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow, true));
     else S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
     if (ev) S2D_CUDA(cudaEventRecord(ev[2], h->stream));
     if (h->Fv) {
@@ -586,6 +586,9 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     h->I[1] = (char*)h->Ibase + h->Ibytes;
     h->I[2] = (char*)h->Ibase + 2 * h->Ibytes;
     S2D_ALLOC(h->rk2, (size_t)d.KX * d.ldS * sizeof(double));
+    if (h->ph.form == S2D_NL_BASDEVANT) {
+        S2D_ALLOC(h->rk2s, (size_t)d.KX * d.ldS * sizeof(double));
+    }
     // complex twiddles (M entries) followed by the FMA-form blocks
     std::vector<TwEnt<double>> tabd;
     std::vector<TwEnt<float>> tabf;
@@ -618,7 +621,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         if (tab_size && cudaMemcpy((char*)h->tw + d.tab_bytes, src, tab_size, cudaMemcpyHostToDevice) != cudaSuccess)
             return bail(fail(S2D_ERR_CUDA, "twiddle table upload failed"));
     }
-    if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess)
+    if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess ||
+        (h->rk2s && Kern<double>::init_rk2(d, h->rk2s, h->stream, std::sqrt(0.5) / (double)d.M) != cudaSuccess))
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
     // launch shapes: about 256 threads per CTA so that at least two CTAs
@@ -672,7 +676,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
-    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->tw,  h->ref_stage,
+    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
                     h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);

@@ -144,8 +144,10 @@ struct Kern {
                             const void* tw, cudaStream_t st, const Launch& L);
     static cudaError_t xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw, const void* tw,
                                  cudaStream_t st, const Launch& L);
+    // prescaled: u and v came from the rk2s table (scaled by sqrt(0.5)/M), so
+    // their products carry the 1/(2 M^2) of the forward transform already
     static cudaError_t xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw, cudaStream_t st,
-                                 const Launch& L);
+                                 const Launch& L, bool prescaled = false);
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
                                 void* Sdw, const void* src, int stage, double dt, const Phys& ph,
                                 const void* tw, unsigned int* flags, cudaStream_t st, const Launch& L);
@@ -180,7 +182,8 @@ struct Kern {
                                  cudaStream_t st, const Launch& L);
     static cudaError_t yfwd_store(const Dims& d, const void* I, void* S, const void* tw,
                                   cudaStream_t st, const Launch& L);
-    static cudaError_t init_rk2(const Dims& d, double* rk2, cudaStream_t st);
+    // rk2[kx][jc] = factor / k^2 (0 at k = 0)
+    static cudaError_t init_rk2(const Dims& d, double* rk2, cudaStream_t st, double factor = 1.0);
     static size_t smem_limit_yinv();
 };
 
@@ -217,6 +220,11 @@ struct s2d_handle {
     void* I[3] = {nullptr, nullptr, nullptr};
     size_t Ibytes = 0;
     double* rk2 = nullptr;
+    // Basdevant form: rk2 times sqrt(0.5)/M.  The step's inverse y-pass takes
+    // u = i ky psi and v = -i kx psi through it, so that the products u v and
+    // v^2 - u^2 carry the normalisation 1/(2 M^2) of the forward transform and
+    // the x-pass does not multiply its 2 (K+1) outputs per row by it
+    double* rk2s = nullptr;
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array

@@ -556,14 +556,14 @@ __global__ void __launch_bounds__(512) k_yfwd_store(Dims d, const typename Vec<T
 }
 
 // 1/(kx^2+ky^2) per compact mode, 0 at the mean mode (FP64 in every variant).
-__global__ void k_init_rk2(Dims d, double* rk2) {
+__global__ void k_init_rk2(Dims d, double* rk2, double factor) {
     const int total = d.KX * d.KY;
     for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
         const int kx = idx / d.KY;
         const int jc = idx - kx * d.KY;
         const int ky = ky_of_jc(d, jc);
         const double k2 = (double)kx * kx + (double)ky * ky;
-        rk2[(size_t)kx * d.ldS + jc] = (k2 == 0.0) ? 0.0 : 1.0 / k2;
+        rk2[(size_t)kx * d.ldS + jc] = (k2 == 0.0) ? 0.0 : factor / k2;
     }
 }
 
@@ -620,9 +620,9 @@ cudaError_t Kern<T>::xpass_rhs(const Dims& d, void* Iu, void* Iv, const void* Iw
 
 template <typename T>
 cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw, cudaStream_t st,
-                               const Launch& L) {
+                               const Launch& L, bool prescaled) {
     using VT = typename Vec<T>::t;
-    const T scale = (T)(0.5 / ((double)d.M * (double)d.M));
+    const T scale = prescaled ? (T)1 : (T)(0.5 / ((double)d.M * (double)d.M));
     const int nb = (d.M + L.G - 1) / L.G;
     VT* u = (VT*)Iu;
     VT* v = (VT*)Iv;
@@ -780,8 +780,8 @@ cudaError_t Kern<T>::yfwd_store(const Dims& d, const void* I, void* S, const voi
 }
 
 template <typename T>
-cudaError_t Kern<T>::init_rk2(const Dims& d, double* rk2, cudaStream_t st) {
-    k_init_rk2<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2);
+cudaError_t Kern<T>::init_rk2(const Dims& d, double* rk2, cudaStream_t st, double factor) {
+    k_init_rk2<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2, factor);
     return cudaGetLastError();
 }
 

@@ -163,6 +163,15 @@ template <typename VT>
 __device__ __forceinline__ void extract_pair(const VT* buf, VT* A, VT* B, const Dims& d, int lane,
                                              bool active, decltype(buf[0].x) scale) {
     if (!active) return;
+    if (scale == (decltype(scale))1) {   // products of prescaled u, v: no multiply
+        for (int k = lane; k <= d.K; k += d.Tg) {
+            const VT p = buf[k];
+            const VT q = buf[k == 0 ? 0 : d.M - k];
+            A[k] = mk<VT>(p.x + q.x, p.y - q.y);
+            B[k] = mk<VT>(p.y + q.y, q.x - p.x);
+        }
+        return;
+    }
     for (int k = lane; k <= d.K; k += d.Tg) {
         const VT p = buf[k];
         const VT q = buf[k == 0 ? 0 : d.M - k];
