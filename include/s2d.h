@@ -145,8 +145,14 @@ S2D_API int s2d_integrate_steps(s2d_handle* h, int32_t n, double dt);
  * one) are read and written in place by the kernels where the device can
  * address them: page-locked memory, and ordinary pageable memory whose pages
  * are resident on systems whose GPU reads the host page tables (Grace,
- * cudaDevAttrPageableMemoryAccess); otherwise through staging copies.  The environment variable S2D_HOST_IO=copy,
- * read by s2d_create, forces the copies for that handle. */
+ * cudaDevAttrPageableMemoryAccess); otherwise through staging copies.  The
+ * environment variable S2D_HOST_IO=copy, read by s2d_create, forces the
+ * copies for that handle.
+ *
+ * Every kernel of a step is launched as a programmatic dependent of the one
+ * before it on the handle's stream (it waits for its predecessor to complete
+ * before touching memory, so results are the same bit for bit);
+ * S2D_PDL=0, read by s2d_create, gives plain stream order. */
 S2D_API int s2d_integrate_one_step_host(s2d_handle* h, double* wC, double* psiC,
                                         int32_t cISize, int32_t nyG, double dt);
 
