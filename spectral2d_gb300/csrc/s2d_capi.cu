@@ -185,9 +185,12 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
     const bool bas = h->ph.form == S2D_NL_BASDEVANT;
     FieldSet fs{};
     fs.nf = bas ? 2 : 3;
-    fs.op[0] = OP_U;
-    fs.op[1] = OP_V;
+    // Basdevant: the scaled factors of u and v from their tables
+    fs.op[0] = bas ? OP_TU : OP_U;
+    fs.op[1] = bas ? OP_TV : OP_V;
     fs.op[2] = OP_W;
+    fs.tab[0] = h->fu;
+    fs.tab[1] = h->fv;
     fs.out[0] = h->I[0];
     fs.out[1] = h->I[1];
     fs.out[2] = h->I[2];
@@ -588,6 +591,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     S2D_ALLOC(h->rk2, (size_t)d.KX * d.ldS * sizeof(double));
     if (h->ph.form == S2D_NL_BASDEVANT) {
         S2D_ALLOC(h->rk2s, (size_t)d.KX * d.ldS * sizeof(double));
+        S2D_ALLOC(h->fu, (size_t)d.KX * d.ldS * sizeof(double));
+        S2D_ALLOC(h->fv, (size_t)d.KX * d.ldS * sizeof(double));
     }
     // complex twiddles (M entries) followed by the FMA-form blocks
     std::vector<TwEnt<double>> tabd;
@@ -622,7 +627,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
             return bail(fail(S2D_ERR_CUDA, "twiddle table upload failed"));
     }
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess ||
-        (h->rk2s && Kern<double>::init_rk2(d, h->rk2s, h->stream, std::sqrt(0.5) / (double)d.M) != cudaSuccess))
+        (h->rk2s && Kern<double>::init_rk2(d, h->rk2s, h->stream, std::sqrt(0.5) / (double)d.M) != cudaSuccess) ||
+        (h->fu && Kern<double>::init_uv_factors(d, h->rk2s, h->fu, h->fv, h->stream) != cudaSuccess))
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
     // launch shapes: about 256 threads per CTA so that at least two CTAs
@@ -676,7 +682,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
-    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->tw,  h->ref_stage,
+    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
                     h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);

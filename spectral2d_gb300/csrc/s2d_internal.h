@@ -86,12 +86,17 @@ enum FieldOp : int {
     OP_WY = 5,   // i ky omega
     OP_UX = 6,   // i kx u
     OP_VY = 7,   // i ky v
+    OP_TU = 8,   // u with its factor ky/k^2 (scaled) read from the field's table
+    OP_TV = 9,   // v with its factor -kx/k^2 (scaled) read from the field's table
 };
 
+// tab[f]: per-mode factor table of field f (compact layout) for OP_TU /
+// OP_TV; the other operators read the 1/k^2 table the kernel is given.
 struct FieldSet {
     int nf;
     int op[4];
     void* out[4];
+    const double* tab[4];
 };
 
 // Launch shape for one kernel: G groups of Tg threads, dynamic smem bytes.
@@ -184,6 +189,9 @@ struct Kern {
                                   cudaStream_t st, const Launch& L);
     // rk2[kx][jc] = factor / k^2 (0 at k = 0)
     static cudaError_t init_rk2(const Dims& d, double* rk2, cudaStream_t st, double factor = 1.0);
+    // fu = ky * rk2, fv = -kx * rk2 per mode: the factors OP_U / OP_V form
+    // in the kernel, as tables (the same products, so the same bits)
+    static cudaError_t init_uv_factors(const Dims& d, const double* rk2, double* fu, double* fv, cudaStream_t st);
     static size_t smem_limit_yinv();
 };
 
@@ -225,6 +233,11 @@ struct s2d_handle {
     // v^2 - u^2 carry the normalisation 1/(2 M^2) of the forward transform and
     // the x-pass does not multiply its 2 (K+1) outputs per row by it
     double* rk2s = nullptr;
+    // ky * rk2s and -kx * rk2s per mode: the step's inverse y-pass reads the
+    // factor of u and of v instead of forming it (a conversion and a multiply
+    // on the FP64 pipe per mode saved)
+    double* fu = nullptr;
+    double* fv = nullptr;
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array

@@ -567,6 +567,19 @@ __global__ void k_init_rk2(Dims d, double* rk2, double factor) {
     }
 }
 
+__global__ void k_init_uv_factors(Dims d, const double* __restrict__ rk2, double* fu, double* fv) {
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const int ky = ky_of_jc(d, jc);
+        const size_t off = (size_t)kx * d.ldS + jc;
+        // the expressions of apply_op's OP_U and OP_V
+        fu[off] = (double)ky * rk2[off];
+        fv[off] = -(double)kx * rk2[off];
+    }
+}
+
 // FP64 throughput probe: 8 independent FMA chains per thread.
 __global__ void k_fp64_probe(double* sink, int iters) {
     double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
@@ -782,6 +795,12 @@ cudaError_t Kern<T>::yfwd_store(const Dims& d, const void* I, void* S, const voi
 template <typename T>
 cudaError_t Kern<T>::init_rk2(const Dims& d, double* rk2, cudaStream_t st, double factor) {
     k_init_rk2<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2, factor);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::init_uv_factors(const Dims& d, const double* rk2, double* fu, double* fv, cudaStream_t st) {
+    k_init_uv_factors<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2, fu, fv);
     return cudaGetLastError();
 }
 

@@ -59,6 +59,9 @@ __device__ __forceinline__ VT apply_op(int op, VT w, int kx, int ky, double rk2)
             return scale_by(w, -(double)kx * (double)ky * rk2, false);
         case OP_VY:  // i ky v = kx ky psi
             return scale_by(w, (double)kx * (double)ky * rk2, false);
+        case OP_TU:  // as OP_U / OP_V, rk2 being the factor itself
+        case OP_TV:
+            return scale_by(w, rk2, true);
         default:
             return w;
     }
@@ -85,12 +88,14 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
     // select without dynamic indexing of the parameter struct
     int op;
     void* outp;
+    const double* tab;
     switch (f) {
-        case 0: op = fs.op[0]; outp = fs.out[0]; break;
-        case 1: op = fs.op[1]; outp = fs.out[1]; break;
-        case 2: op = fs.op[2]; outp = fs.out[2]; break;
-        default: op = fs.op[3]; outp = fs.out[3]; break;
+        case 0: op = fs.op[0]; outp = fs.out[0]; tab = fs.tab[0]; break;
+        case 1: op = fs.op[1]; outp = fs.out[1]; tab = fs.tab[1]; break;
+        case 2: op = fs.op[2]; outp = fs.out[2]; tab = fs.tab[2]; break;
+        default: op = fs.op[3]; outp = fs.out[3]; tab = fs.tab[3]; break;
     }
+    if (op == OP_TU || op == OP_TV) rk2 = tab;   // the factor table takes the 1/k^2 table's place
     VT* buf = bufs + (size_t)g * d.M;
 
     const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
