@@ -209,7 +209,7 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
         // the epilogue after a cross-stream join is an ordinary launch
         if (join) S2D_CUDA(cudaStreamWaitEvent(h->stream, join, 0));
         S2D_CUDA(Kern<T>::stage(d, h->I[2], h->Fv, h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->flags,
-                                h->stream, h->L_ycol.pdl && !join));
+                                h->stream, h->L_ycol.pdl && !join, h->cc, h->vk));
     } else {
         Launch L = h->L_yfwd;
         if (join) {
@@ -583,6 +583,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     S2D_ALLOC(h->S1, state_bytes);
     if (h->prec == S2D_FP64 && h->ph.form == S2D_NL_BASDEVANT) {
         S2D_ALLOC(h->Fv, state_bytes);
+        S2D_ALLOC(h->cc, (size_t)d.KX * d.ldS * 2 * sizeof(double));
+        S2D_ALLOC(h->vk, (size_t)d.KX * d.ldS * sizeof(double));
     }
     S2D_ALLOC(h->Ibase, 3 * h->Ibytes);
     h->I[0] = h->Ibase;
@@ -628,7 +630,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     }
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess ||
         (h->rk2s && Kern<double>::init_rk2(d, h->rk2s, h->stream, std::sqrt(0.5) / (double)d.M) != cudaSuccess) ||
-        (h->fu && Kern<double>::init_uv_factors(d, h->rk2s, h->fu, h->fv, h->stream) != cudaSuccess))
+        (h->fu && Kern<double>::init_uv_factors(d, h->rk2s, h->fu, h->fv, h->stream) != cudaSuccess) ||
+        (h->cc && Kern<double>::init_stage_factors(d, h->ph.nu, h->cc, h->vk, h->stream) != cudaSuccess))
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
     // launch shapes: about 256 threads per CTA so that at least two CTAs
@@ -682,7 +685,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
-    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->tw,  h->ref_stage,
+    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->cc, h->vk, h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
                     h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);

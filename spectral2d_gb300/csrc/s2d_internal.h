@@ -162,7 +162,11 @@ struct Kern {
                                 const void* tw, cudaStream_t st, const Launch& L);
     static cudaError_t stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
                              const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
-                             cudaStream_t st, bool pdl = false);
+                             cudaStream_t st, bool pdl = false, const double* cc = nullptr,
+                             const double* vk = nullptr);
+    // cc (2 per mode) = (kx^2 - ky^2, kx ky), vk = nu k^2: the Basdevant stage
+    // factors as tables (stage() computes them when given none)
+    static cudaError_t init_stage_factors(const Dims& d, double nu, double* cc, double* vk, cudaStream_t st);
     static cudaError_t ref_to_compact(const Dims& d, const double* ref, int C, void* S,
                                       cudaStream_t st);
     static cudaError_t compact_to_ref(const Dims& d, const void* S, int C, double* refW,
@@ -246,6 +250,8 @@ struct s2d_handle {
     double* dscratch = nullptr;           // spectrum / partial sums
     size_t dscratch_n = 0;
     void* Fv = nullptr;   // FP64 Basdevant: second compact array of the split K3 (the first is I[2])
+    double* cc = nullptr;  // ... and its stage kernel's factors (kx^2 - ky^2, kx ky) per mode
+    double* vk = nullptr;  // ... and nu k^2 per mode
     // host-array calls: the truncated part of an output array (outside the
     // retained rectangle) is copied from this buffer of zeros on xstream,
     // concurrently with the step on stream

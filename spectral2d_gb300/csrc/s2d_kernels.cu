@@ -102,9 +102,10 @@ __global__ void __launch_bounds__(256) k_stage(Dims d, const typename Vec<T>::t*
                                                const typename Vec<T>::t* __restrict__ Fv, typename Vec<T>::t* S0,
                                                typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
                                                const typename Vec<T>::t* __restrict__ src, int stage, double dt,
-                                               Phys ph, unsigned int* flags) {
+                                               Phys ph, unsigned int* flags, const double2* __restrict__ cc,
+                                               const double* __restrict__ vk) {
     pdl_enter();
-    if (stage_body<T>(d, Fu, Fv, S0, S1, Sdw, src, stage, dt, ph)) atomicOr(flags, 1u);
+    if (stage_body<T>(d, Fu, Fv, S0, S1, Sdw, src, stage, dt, ph, cc, vk)) atomicOr(flags, 1u);
 }
 
 // ------------------------------------------------------------------------
@@ -580,6 +581,20 @@ __global__ void k_init_uv_factors(Dims d, const double* __restrict__ rk2, double
     }
 }
 
+// The Basdevant stage factors of every retained mode: cc = (kx^2 - ky^2,
+// kx ky), exact; vk = nu k^2, the product stage_point forms.
+__global__ void k_init_stage_factors(Dims d, double nu, double2* cc, double* vk) {
+    const int total = d.KX * d.KY;
+    for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+        const int kx = idx / d.KY;
+        const int jc = idx - kx * d.KY;
+        const int ky = ky_of_jc(d, jc);
+        const size_t off = (size_t)kx * d.ldS + jc;
+        cc[off] = make_double2((double)(kx * kx - ky * ky), (double)(kx * ky));
+        vk[off] = nu * (double)(kx * kx + ky * ky);
+    }
+}
+
 // FP64 throughput probe: 8 independent FMA chains per thread.
 __global__ void k_fp64_probe(double* sink, int iters) {
     double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
@@ -686,10 +701,11 @@ cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, voi
 template <typename T>
 cudaError_t Kern<T>::stage(const Dims& d, const void* Fu, const void* Fv, void* S0, void* S1, void* Sdw,
                            const void* src, int stage, double dt, const Phys& ph, unsigned int* flags,
-                           cudaStream_t st, bool pdl) {
+                           cudaStream_t st, bool pdl, const double* cc, const double* vk) {
     using VT = typename Vec<T>::t;
     return launch_k(k_stage<T>, dim3((d.KY + 255) / 256, d.KX), dim3(256), 0, st, pdl, d, (const VT*)Fu,
-                    (const VT*)Fv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, flags);
+                    (const VT*)Fv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, flags,
+                    (const double2*)cc, vk);
 }
 
 template <typename T>
@@ -801,6 +817,12 @@ cudaError_t Kern<T>::init_rk2(const Dims& d, double* rk2, cudaStream_t st, doubl
 template <typename T>
 cudaError_t Kern<T>::init_uv_factors(const Dims& d, const double* rk2, double* fu, double* fv, cudaStream_t st) {
     k_init_uv_factors<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, rk2, fu, fv);
+    return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t Kern<T>::init_stage_factors(const Dims& d, double nu, double* cc, double* vk, cudaStream_t st) {
+    k_init_stage_factors<<<grid_for((long)d.KX * d.KY, 256), 256, 0, st>>>(d, nu, (double2*)cc, vk);
     return cudaGetLastError();
 }
 

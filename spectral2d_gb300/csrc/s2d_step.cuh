@@ -213,6 +213,15 @@ __device__ __forceinline__ void xpass_bas_body(const Dims& d, typename Vec<T>::t
     extract_pair(Z, urow, vrow, d, lane, active, scale);
 }
 
+// a b + c with one rounding, and a b alone rounded (never fused into a
+// neighbouring add): the epilogue's arithmetic fixed operation by operation,
+// so that every kernel that inlines it -- the single-run stage kernels and
+// the batch -- rounds the same way whatever the compiler would contract.
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double mul_t(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float mul_t(float a, float b) { return __fmul_rn(a, b); }
+
 // One mode (kx, jc) of the K3 epilogue: dW from the two transformed products
 // nx, ny, then the stage update below, Truncate (|k|^2 > K^2 -> 0) and the
 // non-finite check.  Returns true for a non-finite result.
@@ -220,11 +229,14 @@ template <typename T>
 __device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx, typename Vec<T>::t ny, int kx,
                                             int jc, typename Vec<T>::t* S0, typename Vec<T>::t* S1,
                                             typename Vec<T>::t* Sdw, const typename Vec<T>::t* __restrict__ src,
-                                            int stage, double dt, const Phys& ph) {
+                                            int stage, double dt, const Phys& ph, const T* fac = nullptr) {
     using VT = typename Vec<T>::t;
     const T tdt = (T)dt;
     const T c34 = (T)0.75, c14 = (T)0.25, c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0);
-    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * 2.0 / 3.0);
+    // 2 dt / 3 as dt times the rounded 2/3, like the 1/3 above: a division
+    // here would be one FP64 division per mode in the one-mode-per-thread
+    // stage kernel (its stage-3 launch took 107 instead of 76 us at 2048^2)
+    const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * (2.0 / 3.0));
     const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
     const int ky = ky_of_jc(d, jc);
     const size_t off = (size_t)kx * d.ldS + jc;
@@ -237,21 +249,23 @@ __device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx
         const VT w0 = S0[off];
         const VT win = (stage <= 1) ? w0 : S1[off];
         const T fkx = (T)kx, fky = (T)ky;
-        const T visc = tnu * (T)kk;
+        // fac (Basdevant): kx^2 - ky^2, kx ky, nu k^2 of this mode from tables
+        // (the same values, exact or the same product)
+        const T visc = fac ? fac[2] : tnu * (T)kk;
         T dwx, dwy;
         if (ph.form == S2D_NL_BASDEVANT) {
             // dW = (kx^2-ky^2) F[uv] + kx ky F[v^2-u^2] - nu k^2 w
-            const T c1 = (T)(kx * kx - ky * ky), c2 = (T)(kx * ky);
-            dwx = c1 * nx.x + c2 * ny.x - visc * win.x;
-            dwy = c1 * nx.y + c2 * ny.y - visc * win.y;
+            const T c1 = fac ? fac[0] : (T)(kx * kx - ky * ky), c2 = fac ? fac[1] : (T)(kx * ky);
+            dwx = fma_t(c1, nx.x, fma_t(c2, ny.x, -mul_t(visc, win.x)));
+            dwy = fma_t(c1, nx.y, fma_t(c2, ny.y, -mul_t(visc, win.y)));
         } else {
             // dW = -i kx F[uw] - i ky F[vw] - nu k^2 w  (src/Spectral.F90:464-479)
-            dwx = fkx * nx.y + fky * ny.y - visc * win.x;
-            dwy = -(fkx * nx.x) - fky * ny.x - visc * win.y;
+            dwx = fma_t(fkx, nx.y, fma_t(fky, ny.y, -mul_t(visc, win.x)));
+            dwy = fma_t(-fkx, nx.x, fma_t(-fky, ny.x, -mul_t(visc, win.y)));
         }
         if (talpha != (T)0) {
-            dwx -= talpha * win.x;
-            dwy -= talpha * win.y;
+            dwx = fma_t(-talpha, win.x, dwx);
+            dwy = fma_t(-talpha, win.y, dwy);
         }
         if (ph.fk != 0 && kx == 0 && (ky == ph.fk || ky == -ph.fk)) {
             dwx += (T)ph.f_re;
@@ -265,11 +279,13 @@ __device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx
         if (stage == 0) {
             out = mk<VT>(dwx, dwy);
         } else if (stage == 1) {
-            out = mk<VT>(w0.x + tdt * dwx, w0.y + tdt * dwy);
+            out = mk<VT>(fma_t(tdt, dwx, w0.x), fma_t(tdt, dwy, w0.y));
         } else if (stage == 2) {
-            out = mk<VT>(c34 * w0.x + c14 * win.x + dt4 * dwx, c34 * w0.y + c14 * win.y + dt4 * dwy);
+            out = mk<VT>(fma_t(dt4, dwx, fma_t(c14, win.x, mul_t(c34, w0.x))),
+                         fma_t(dt4, dwy, fma_t(c14, win.y, mul_t(c34, w0.y))));
         } else {
-            out = mk<VT>(c13 * w0.x + c23 * win.x + dt23 * dwx, c13 * w0.y + c23 * win.y + dt23 * dwy);
+            out = mk<VT>(fma_t(dt23, dwx, fma_t(c23, win.x, mul_t(c13, w0.x))),
+                         fma_t(dt23, dwy, fma_t(c23, win.y, mul_t(c13, w0.y))));
         }
         bad = bits_nonfinite(out.x) | bits_nonfinite(out.y);
     }
@@ -356,11 +372,17 @@ __device__ __forceinline__ bool stage_body(const Dims& d, const typename Vec<T>:
                                            const typename Vec<T>::t* __restrict__ Fv, typename Vec<T>::t* S0,
                                            typename Vec<T>::t* S1, typename Vec<T>::t* Sdw,
                                            const typename Vec<T>::t* __restrict__ src, int stage, double dt,
-                                           const Phys& ph) {
+                                           const Phys& ph, const double2* __restrict__ cc,
+                                           const double* __restrict__ vk) {
     const int kx = blockIdx.y;
     const int jc = blockIdx.x * blockDim.x + threadIdx.x;
     if (kx >= d.KX || jc >= d.KY) return false;
     const size_t off = (size_t)kx * d.ldS + jc;
+    if (cc) {   // the mode's factors from tables: no integer-to-FP64 conversions or nu k^2 product
+        const double2 c = __ldg(&cc[off]);
+        const T fac[3] = {(T)c.x, (T)c.y, (T)__ldg(&vk[off])};
+        return stage_point<T>(d, __ldcg(&Fu[off]), __ldcg(&Fv[off]), kx, jc, S0, S1, Sdw, src, stage, dt, ph, fac);
+    }
     return stage_point<T>(d, __ldcg(&Fu[off]), __ldcg(&Fv[off]), kx, jc, S0, S1, Sdw, src, stage, dt, ph);
 }
 
