@@ -14,17 +14,27 @@ total energy 0.5).  Metric: Mpt*steps/s = N^2 * steps/s / 1e6.
   IntegrateOneStep with host arrays (s2d_integrate_one_step_host): every step
   moves wC's retained modes in from page-locked host memory and wC, psiC out
   over the host link (the kernels read and write the host arrays in place).
-* ``roofline``: the dominant kernel's algorithmic bytes per launch (byte model
-  below) over its CUDA-event launch time, against the measured HBM peak; the
-  FP64-ALU view of the same kernel is reported beside it.
+* ``roofline``: the dominant kernel against the roof that binds it, from its
+  CUDA-event launch time.  FP64: benchFFT flops per launch against the FP64
+  FMA rate measured on this GPU (``bound: "fp64"``), with the HBM view
+  (algorithmic bytes per launch over the measured copy bandwidth) nested as
+  ``hbm``; FP32: the HBM view (``bound: "hbm"``).
 * ``cpu_baseline``: the FP64 CPU restatement of the reference (scipy/pocketfft
   on all host cores, and on one core) timed on a bounded sample of the same
   workload.
 * ``--impl reference``: that CPU restatement as the reference arm (the
   reference itself, Fortran + FFTW-MPI, cannot be built on these machines).
 
-Multi-GPU: one independent replica per rank (a single run does not shard);
-``value`` is the sum over ranks, time is the max over ranks.
+Multi-GPU: one process per GPU.  Under torchrun (or any launcher that sets
+RANK / LOCAL_RANK / WORLD_SIZE / MASTER_ADDR / MASTER_PORT) each process is one
+rank; ``python bench.py --gpus N`` without a launcher starts the N local ranks
+itself with those variables set.  The headline DNS workload runs one
+independent replica per rank (a single run does not shard): ``value`` is the
+sum over ranks of the points x steps advanced over the slowest rank's time.
+``--workload ensemble`` and ``les-batch`` split their runs over the ranks by
+cost (replicas.shard_runs); ``value`` is all runs' work over the slowest
+rank's time.  ``--dry-cpu`` runs only this rank logic over gloo on CPU, with
+stand-in step times (tests/test_bench_cpu.py).
 """
 
 from __future__ import annotations
@@ -228,33 +238,78 @@ def run_reference(args, rank, world):
     return 0
 
 
-def run_ensemble(args, rank, world):
-    """The batched-ensemble workload (not the headline line): 96 runs,
-    32 x 128^2, 32 x 256^2, 32 x 512^2, nu ~ U[5e-4, 5e-3], per-run seeds and
-    CFL-0.5 dt, one persistent launch per RK3 stage from a CUDA graph."""
+def ensemble_runs():
+    """The batched-ensemble workload's runs in their global order: 32 x 128^2,
+    32 x 256^2, 32 x 512^2 with nu ~ U[5e-4, 5e-3] (seeded); run i's initial
+    condition uses seed i, whichever rank advances it."""
     import numpy as np
-    from spectral2d_gb300 import Ensemble
     rng = np.random.default_rng(0)
     nxs = [128] * 32 + [256] * 32 + [512] * 32
-    nus = list(rng.uniform(5e-4, 5e-3, 96))
-    ens = Ensemble(nxs, nus, precision=args.precision)
-    dts = []
-    for i, r in enumerate(ens.runs):
-        r.set_turbulent_velocity(seed=1000 * rank + i, spectrum="k4gauss", k0=10.0, tke=0.5)
-        dts.append(r.compute_time_step(CFL))
-    ens.set_dt(dts)
-    threads, cps, _ = ens.tune()
-    ens.integrate_steps(args.warmup)
-    ens.synchronize()
-    ms = ens.time_steps(args.steps)
-    ens.status()
-    pts = sum(n * n for n in nxs)
+    nus = [float(x) for x in rng.uniform(5e-4, 5e-3, 96)]
+    return nxs, nus
+
+
+def dry_ms(nxs, steps, rank):
+    """--dry-cpu: a stand-in for a rank's timed steps (no GPU): proportional
+    to the rank's summed run cost, plus a rank-dependent offset so that the
+    max over ranks is exercised."""
+    from spectral2d_gb300.replicas import run_cost
+    return steps * (1e-6 * sum(run_cost(n) for n in nxs) + 0.01 * (rank + 1))
+
+
+def group(args, local):
+    from spectral2d_gb300.replicas import ReplicaGroup
+    return ReplicaGroup(backend="gloo" if args.dry_cpu else None, device=None if args.dry_cpu else local)
+
+
+def run_ensemble(args, rank, world, local):
+    """The batched-ensemble workload (not the headline line): 96 runs,
+    32 x 128^2, 32 x 256^2, 32 x 512^2, nu ~ U[5e-4, 5e-3], per-run seeds and
+    CFL-0.5 dt, one persistent launch per RK3 stage from a CUDA graph.  With
+    N ranks the runs are split by cost (replicas.shard_runs, M^2 log2 M per
+    run): each rank advances its share as one batch, and value = all runs'
+    points x steps over the slowest rank's time (total work fixed: strong
+    scaling)."""
+    import numpy as np
+    from spectral2d_gb300.replicas import run_cost, shard_runs
+    nxs_all, nus_all = ensemble_runs()
+    shards = shard_runs([run_cost(n) for n in nxs_all], world)
+    mine = shards[rank]
+    nxs = [nxs_all[i] for i in mine]
+    nus = [nus_all[i] for i in mine]
+    D = group(args, local)
+    threads = cps = None
     check = None
-    if args.ens_check_steps > 0:
+    ens = None
+    if args.dry_cpu:
+        ms = dry_ms(nxs, args.steps, rank)
+    elif mine:
+        from spectral2d_gb300 import Ensemble
+        ens = Ensemble(nxs, nus, precision=args.precision, device=local)
+        dts = []
+        for i, r in zip(mine, ens.runs):
+            r.set_turbulent_velocity(seed=i, spectrum="k4gauss", k0=10.0, tke=0.5)
+            dts.append(r.compute_time_step(CFL))
+        ens.set_dt(dts)
+        threads, cps, _ = ens.tune()
+        ens.integrate_steps(args.warmup)
+        ens.synchronize()
+    D.barrier()
+    if ens is not None:
+        ms = ens.time_steps(args.steps)
+        ens.status()
+    elif not args.dry_cpu:
+        ms = 0.0
+    D.barrier()
+    ms_max = D.reduce(ms, "MAX")
+    ms_ranks = D.gather(ms)
+    shards_seen = D.gather(mine)
+    if ens is not None and args.ens_check_steps > 0:
         # every run advanced in both precisions from the same state; the FP64
         # batch equals single-run FP64 bit for bit (tests/test_gpu_ensemble.py)
+        from spectral2d_gb300 import Ensemble
         other = "fp64" if args.precision == "fp32" else "fp32"
-        ens2 = Ensemble(nxs, nus, precision=other)
+        ens2 = Ensemble(nxs, nus, precision=other, device=local)
         for i, r in enumerate(ens.runs):
             ens2.runs[i].set_state(r.get_state()[0])
         ens2.set_dt(dts)
@@ -268,96 +323,134 @@ def run_ensemble(args, rank, world):
         for i, n in enumerate(nxs):
             a, b = e32.runs[i].get_state()[0], e64.runs[i].get_state()[0]
             errs.setdefault(n, []).append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+        ens2.close()
+        merged = {}
+        for part in D.gather(errs):
+            for n, v in part.items():
+                merged.setdefault(n, []).extend(v)
         check = {"steps": args.ens_check_steps,
                  "fp32_vs_fp64_w_rel_l2": {str(n): {"max": max(v), "median": float(np.median(v))}
-                                           for n, v in errs.items()}}
-        ens2.close()
+                                           for n, v in sorted(merged.items())}}
+    pts = sum(n * n for n in nxs_all)
     if rank == 0:
-        print(json.dumps({
+        line = {
             "metric": "ensemble Mpt*steps/s (96 runs: 32x128^2, 32x256^2, 32x512^2)",
-            "value": pts * args.steps / (ms * 1e-3) / 1e6, "unit": "Mpt*steps/s",
+            "value": pts * args.steps / (ms_max * 1e-3) / 1e6, "unit": "Mpt*steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "strong" if world > 1 else "weak",
             "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
             "data": "synthetic (seeded random-phase ICs)",
             "config": {"workload": "batched ensemble, one persistent launch per RK3 stage",
+                       "parallelism": f"runs split by cost over {world} rank(s) (M^2 log2 M per run)",
                        "tile_threads": threads, "ctas_per_sm": cps},
-            "gpu_launches": 3 * args.steps, "precision_check": check}), flush=True)
-    ens.close()
+            "runs_per_rank": [len(x) for x in shards_seen], "ms_per_rank": ms_ranks,
+            "gpu_launches": 3 * args.steps if not args.dry_cpu else 0, "precision_check": check}
+        if args.dry_cpu:
+            line["dry_cpu"] = True
+            line["shards"] = shards_seen
+        print(json.dumps(line), flush=True)
+    if ens is not None:
+        ens.close()
+    D.close()
     return 0
 
 
-def run_les_batch(args, rank, world):
+def run_les_batch(args, rank, world, local):
     """Concurrent closure LES (not the headline line): args.les_runs runs of
     256^2 (384^2 collocation grid), decaying turbulence with per-run seeds,
     nu = 1e-4, CFL-0.5 dt; every step is one network forward over all runs
     (the trained 128^2 closure's weights when packaged, else a seeded random
     network) plus the batched transforms and three persistent stage launches,
     replayed from one CUDA graph.  Both precisions are timed; the FP32 runs'
-    energy spectra are compared with the FP64 runs' after the same steps."""
+    energy spectra are compared with the FP64 runs' after the same steps.
+    With N ranks the runs are split evenly (equal cost): each rank advances
+    its share as one batch with its own copy of the network, and value = all
+    runs' steps over the slowest rank's time."""
     import os
     import numpy as np
-    from spectral2d_gb300 import ClosureNet, Ensemble, closure
-    nr, n, nu = args.les_runs, 256, 1e-4
-    grid = 3 * n // 2
-    net = ClosureNet(grid, max_batch=nr, seed=0)
-    wpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "spectral2d_gb300", "data",
-                         "closure_les128.npz")
-    if os.path.exists(wpath):
-        closure.load_weights(net, wpath)
-        weights = "trained 128^2 closure (spectral2d_gb300/data/closure_les128.npz)"
+    from spectral2d_gb300.replicas import run_cost, shard_runs
+    nr_all, n, nu = args.les_runs, 256, 1e-4
+    shards = shard_runs([run_cost(n)] * nr_all, world)
+    mine = shards[rank]
+    nr = len(mine)
+    D = group(args, local)
+    res, errs, weights = {}, [], None
+    if args.dry_cpu:
+        res = {p: dry_ms([n] * nr, 1, rank) for p in ("fp64", "fp32")}
+        errs = [0.0] * nr
+    elif nr:
+        from spectral2d_gb300 import ClosureNet, Ensemble, closure
+        grid = 3 * n // 2
+        net = ClosureNet(grid, max_batch=nr, seed=0, device=local)
+        wpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "spectral2d_gb300", "data",
+                             "closure_les128.npz")
+        if os.path.exists(wpath):
+            closure.load_weights(net, wpath)
+            weights = "trained 128^2 closure (spectral2d_gb300/data/closure_les128.npz)"
+        else:
+            net.set_scales([1.0, 1.0, 1.0])
+            weights = "seeded random network"
+        ens = {p: Ensemble([n] * nr, [nu] * nr, precision=p, device=local) for p in ("fp64", "fp32")}
+        dts = []
+        for j, i in enumerate(mine):
+            r64 = ens["fp64"].runs[j]
+            r64.set_turbulent_velocity(seed=i, spectrum="k4gauss", k0=10.0, tke=0.5)
+            dts.append(r64.compute_time_step(CFL))
+            ens["fp32"].runs[j].set_state(r64.get_state()[0])
+        for p, e in ens.items():
+            e.set_dt(dts)
+            e.set_closure(net)
+            e.integrate_steps(args.warmup)
+            e.synchronize()
+            D.barrier()
+            ms = e.time_steps(args.steps)
+            e.status()
+            res[p] = ms / args.steps
+        # the network's buffers are shared: the two batches ran one after the other
+        for j in range(nr):
+            _, e64, _, _, _ = ens["fp64"].runs[j].compute_spectrum()
+            _, e32, _, _, _ = ens["fp32"].runs[j].compute_spectrum()
+            kk = slice(1, 41)
+            errs.append(float(np.max(np.abs(e32[kk] - e64[kk]) / e64[kk])))
+        for e in ens.values():
+            e.set_closure(None)
+            e.close()
+        net.close()
     else:
-        net.set_scales([1.0, 1.0, 1.0])
-        weights = "seeded random network"
-    ens = {p: Ensemble([n] * nr, [nu] * nr, precision=p) for p in ("fp64", "fp32")}
-    dts = []
-    for i in range(nr):
-        r64 = ens["fp64"].runs[i]
-        r64.set_turbulent_velocity(seed=1000 * rank + i, spectrum="k4gauss", k0=10.0, tke=0.5)
-        dts.append(r64.compute_time_step(CFL))
-        ens["fp32"].runs[i].set_state(r64.get_state()[0])
-    res = {}
-    for p, e in ens.items():
-        e.set_dt(dts)
-        e.set_closure(net)
-        e.integrate_steps(args.warmup)
-        e.synchronize()
-        ms = e.time_steps(args.steps)
-        e.status()
-        res[p] = ms / args.steps
-    # the network's buffers are shared: the two batches ran one after the other
-    errs = []
-    for i in range(nr):
-        _, e64, _, _, _ = ens["fp64"].runs[i].compute_spectrum()
-        _, e32, _, _, _ = ens["fp32"].runs[i].compute_spectrum()
-        kk = slice(1, 41)
-        errs.append(float(np.max(np.abs(e32[kk] - e64[kk]) / e64[kk])))
+        res = {"fp64": 0.0, "fp32": 0.0}
+    D.barrier()
+    res_max = {p: D.reduce(v, "MAX") for p, v in res.items()}
+    all_errs = [x for part in D.gather(errs) for x in part]
+    shards_seen = D.gather(mine)
     p = args.precision
     if rank == 0:
-        print(json.dumps({
-            "metric": f"closure-LES run-steps/s ({nr} concurrent 256^2 runs)",
-            "value": nr / (res[p] * 1e-3), "unit": "run-steps/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res[p],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        line = {
+            "metric": f"closure-LES run-steps/s ({nr_all} concurrent 256^2 runs)",
+            "value": nr_all / (res_max[p] * 1e-3), "unit": "run-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res_max[p],
+            "higher_is_better": True, "scaling": "strong" if world > 1 else "weak", "vs_baseline": None,
             "dtype": "f64" if p == "fp64" else "f32",
             "data": "synthetic (seeded random-phase ICs)",
             "config": {"workload": "batched closure LES, one network forward + three persistent stage "
                                    "launches per step in one CUDA graph",
-                       "runs": nr, "n": n, "nu": nu, "cfl": CFL, "network": weights},
-            "ms_per_step_fp64": res["fp64"], "ms_per_step_fp32": res["fp32"],
-            "mpt_steps_per_s": nr * n * n / (res[p] * 1e-3) / 1e6,
-            "fp32_vs_fp64_Ek_max_rel_err_k_le_40": {"max_over_runs": max(errs),
-                                                    "mean_over_runs": float(np.mean(errs)),
-                                                    "after_steps": args.warmup + args.steps}}),
-              flush=True)
-    for e in ens.values():
-        e.set_closure(None)
-        e.close()
-    net.close()
+                       "runs": nr_all, "n": n, "nu": nu, "cfl": CFL, "network": weights,
+                       "parallelism": f"runs split evenly over {world} rank(s)"},
+            "ms_per_step_fp64": res_max["fp64"], "ms_per_step_fp32": res_max["fp32"],
+            "mpt_steps_per_s": nr_all * n * n / (res_max[p] * 1e-3) / 1e6,
+            "runs_per_rank": [len(x) for x in shards_seen],
+            "fp32_vs_fp64_Ek_max_rel_err_k_le_40": {"max_over_runs": max(all_errs) if all_errs else None,
+                                                    "mean_over_runs": float(np.mean(all_errs)) if all_errs else None,
+                                                    "after_steps": args.warmup + args.steps}}
+        if args.dry_cpu:
+            line["dry_cpu"] = True
+            line["shards"] = shards_seen
+        print(json.dumps(line), flush=True)
+    D.close()
     return 0
 
 
-def run_les(args, rank, world):
+def run_les(args, rank, world, local):
     """Single-run closure LES against the DNS (not the headline line): the
     128^2 FP32 LES (192^2 collocation grid) with the trained closure
     (spectral2d_gb300/data/closure_les128.npz; a seeded random network of the
@@ -371,7 +464,7 @@ def run_les(args, rank, world):
     from spectral2d_gb300 import (ClosureNet, Spectral2D, closure, filter_state, les_integrate_steps,
                                   les_set_closure, les_time_steps)
     nd, nl, nu = 2048, 128, 1e-4
-    net = ClosureNet(3 * nl // 2, max_batch=1, seed=0)
+    net = ClosureNet(3 * nl // 2, max_batch=1, seed=0, device=local)
     wpath = os.path.join(os.path.dirname(os.path.abspath(__file__)), "spectral2d_gb300", "data",
                          "closure_les128.npz")
     if os.path.exists(wpath):
@@ -380,9 +473,9 @@ def run_les(args, rank, world):
     else:
         net.set_scales([1.0, 1.0, 1.0])
         weights = "seeded random network"
-    dns = Spectral2D(nd, nu=nu)
-    les = Spectral2D(nl, nu=nu, precision="fp32")
-    bare = Spectral2D(nl, nu=nu, precision="fp32")
+    dns = Spectral2D(nd, nu=nu, device=local)
+    les = Spectral2D(nl, nu=nu, precision="fp32", device=local)
+    bare = Spectral2D(nl, nu=nu, precision="fp32", device=local)
     dns.set_turbulent_velocity(seed=SEED + rank, spectrum="k4gauss", k0=10.0, tke=0.5)
     dt = dns.compute_time_step(CFL)
     filter_state(dns, les)
@@ -421,6 +514,66 @@ def run_les(args, rank, world):
     return 0
 
 
+def free_port() -> int:
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        return sk.getsockname()[1]
+
+
+def spawn_local_ranks(n: int) -> int:
+    """--gpus N without a launcher (WORLD_SIZE unset): start N ranks of this
+    script on this node with RANK, LOCAL_RANK, WORLD_SIZE, MASTER_ADDR
+    (127.0.0.1) and MASTER_PORT set, as torchrun would, one GPU per rank
+    (LOCAL_RANK).  Rank 0 prints the JSON line.  If a rank fails the others
+    are stopped; returns the first non-zero exit code (0 if all succeed)."""
+    port = free_port()
+    procs = []
+    for r in range(n):
+        env = dict(os.environ, RANK=str(r), LOCAL_RANK=str(r), WORLD_SIZE=str(n), LOCAL_WORLD_SIZE=str(n),
+                   MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+        procs.append(subprocess.Popen([sys.executable, os.path.abspath(__file__), *sys.argv[1:]], env=env))
+    rc = 0
+    live = list(procs)
+    while live:
+        for p in list(live):
+            code = p.poll()
+            if code is None:
+                continue
+            live.remove(p)
+            if code != 0 and rc == 0:
+                rc = code if code > 0 else 1
+                for q in live:
+                    q.terminate()
+        time.sleep(0.05)
+    return rc
+
+
+def run_dns_dry(args, rank, world, local):
+    """--dry-cpu of the headline workload: one replica per rank (a single run
+    does not shard), stand-in step times; value = the sum over ranks of the
+    points x steps each replica advanced, over the slowest rank's time."""
+    D = group(args, local)
+    n = args.n
+    D.barrier()
+    ms = dry_ms([n], args.steps, rank)
+    D.barrier()
+    ms_max = D.reduce(ms, "MAX")
+    value = D.reduce(n * n * args.steps / (ms_max * 1e-3) / 1e6, "SUM")
+    ms_ranks = D.gather(ms)
+    if rank == 0:
+        print(json.dumps({
+            "metric": f"Mpt*steps/s at {n}^2 {args.precision.upper()} (RK3 step of the "
+                      "vorticity-streamfunction RHS)",
+            "value": value, "unit": "Mpt*steps/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.precision == "fp64" else "f32",
+            "data": "none (dry run of the rank logic)", "config": workload_config(n, args.precision),
+            "ms_per_rank": ms_ranks, "dry_cpu": True, "gpu_launches": 0}), flush=True)
+    D.close()
+    return 0
+
+
 def workload_config(n, precision="fp64"):
     w = 16 if precision == "fp64" else 8
     ws = 2 * (n // 2 + 1) * (3 * n // 2) * w / 1e9   # the two half-spectral intermediates
@@ -448,17 +601,24 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=10.0)
     ap.add_argument("--ref-budget", type=float, default=150.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--dry-cpu", action="store_true",
+                    help="rank logic only, on CPU over gloo: sharding, max/sum over ranks and the JSON "
+                         "line, with stand-in step times and no GPU work (for tests)")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return spawn_local_ranks(args.gpus)
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
     if args.workload == "ensemble":
-        return run_ensemble(args, rank, world)
+        return run_ensemble(args, rank, world, local)
     if args.workload == "les-batch":
-        return run_les_batch(args, rank, world)
+        return run_les_batch(args, rank, world, local)
     if args.workload == "les":
-        return run_les(args, rank, world)
+        return run_les(args, rank, world, local)
+    if args.dry_cpu:
+        return run_dns_dry(args, rank, world, local)
 
     # CPU baseline first (no GPU context yet in this process)
     cpu = None
@@ -542,6 +702,22 @@ def main():
                        "(reference-layout wC in: its retained modes; wC, psiC out, their truncated "
                        "part written from a second stream during the step)"}
 
+    hbm_view = {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "peak_source": f"{hbm_src} HBM copy bandwidth (MEASURED_PEAKS.json)",
+                "algorithmic_bytes_per_launch": bm["per_kernel"][dom],
+                "step_frac": bm["step"] / (ms_per_step * 1e-3) / 1e9 / hbm,
+                "step_frac_reference_form_bytes": bm["step_reference_form"] / (ms_per_step * 1e-3) / 1e9 / hbm}
+    common = {"kernel": dom, "traffic": traffic, "launch_ms": avg[dom], "nonlinear_form": args.form,
+              "kernel_ms_per_step": {k: kms[i] / ksteps for i, k in enumerate(names)}}
+    if args.precision == "fp64" and fp64:
+        # FP64 on GB300: the FFT kernels keep the FP64 pipe ~90 % busy at a few
+        # percent of the HBM roof, so the binding roof is the FP64 rate
+        roofline = {"bound": "fp64", "achieved": alu, "peak": fp64, "unit": "TFLOP/s", "frac": alu / fp64,
+                    "peak_source": "measured FP64 FMA loop on this GPU (s2d_probe_fp64_peak)",
+                    "flops_per_launch": fm[dom], "flop_convention": "benchFFT 2.5 M log2 M per real 1-D FFT",
+                    "hbm": hbm_view, **common}
+    else:
+        roofline = {"bound": "hbm", **{k: v for k, v in hbm_view.items()}, "traffic": traffic, **common}
     if rank == 0:
         line = {
             "metric": f"Mpt*steps/s at {n}^2 {args.precision.upper()} (RK3 step of the "
@@ -552,21 +728,7 @@ def main():
             "dtype": "f64" if args.precision == "fp64" else "f32",
             "data": "synthetic (seeded random-phase IC)",
             "config": workload_config(n, args.precision),
-            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm,
-                         "unit": "GB/s", "frac": achieved / hbm,
-                         "peak_source": f"{hbm_src} HBM copy bandwidth",
-                         "traffic": traffic,
-                         "algorithmic_bytes_per_launch": bm["per_kernel"][dom],
-                         "launch_ms": avg[dom],
-                         "fp64_alu": ({"achieved_tflops": alu, "peak_tflops": fp64,
-                                       "frac": (alu / fp64) if fp64 else None,
-                                       "peak_source": "measured FP64 FMA loop on this GPU",
-                                       "flops_per_launch": fm[dom]}
-                                      if args.precision == "fp64" else None),
-                         "step_hbm_frac": bm["step"] / (ms_per_step * 1e-3) / 1e9 / hbm,
-                         "step_hbm_frac_reference_form_bytes": bm["step_reference_form"] / (ms_per_step * 1e-3) / 1e9 / hbm,
-                         "nonlinear_form": args.form,
-                         "kernel_ms_per_step": {k: kms[i] / ksteps for i, k in enumerate(names)}},
+            "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": s.kernels_per_step() * args.steps,

@@ -361,9 +361,16 @@ S2D_API int s2d_batch_set_closure(s2d_batch* b, s2d_cnn* c);
  * allocation.  nx must be a multiple of 8 and at most S2D_NOALLOC_MAX_NX,
  * else S2D_ERR_INVALID.  The first call on a device resolves the array's
  * device address (cudaGetSymbolAddress) and sets kernel attributes: make it
- * before any stream capture.  Every call shares the one array, so calls that
- * overlap on the GPU (other streams, other host threads) race; serialise
- * them.  Errors are reported by the return code only.
+ * before any stream capture.  The first call with a given nx on a device
+ * (and the first after a call with another nx) also queues the upload of
+ * that grid's twiddle and 1/k^2 tables into the array on the same stream;
+ * later calls with the same nx reuse them.  Every call shares the one
+ * array, so calls that overlap on the GPU (other streams, other host
+ * threads) race; serialise them.  The library remembers which tables the
+ * array holds, so do not use this entry point on a device after
+ * cudaDeviceReset (the array's contents are lost while that record stays).
+ * Errors are reported by the return code only; a NaN or Inf in wC gives a
+ * non-finite dW that is not detected or reported.
  */
 #define S2D_NOALLOC_MAX_NX          256
 #define S2D_NOALLOC_SCRATCH_BYTES   (3u << 20)

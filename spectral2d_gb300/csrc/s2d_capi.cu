@@ -10,6 +10,7 @@
 // conditions.  No framework types cross this boundary.
 #include "s2d.h"
 #include "s2d_internal.h"
+#include "s2d_plan.h"
 
 #include <cuda_runtime.h>
 #include <sys/mman.h>
@@ -56,89 +57,12 @@ int fail(int code, const char* fmt, ...) {
         if (r_ != S2D_OK) return r_;    \
     } while (0)
 
-// exp(-2 pi i r / M) correctly rounded in practice: octant reduction with
-// exact integer arithmetic, residual angle in [0, pi/4] in long double.
-void twiddle(long long r, long long M, double* c, double* s) {
-    const long double PI_4 = 0.785398163397448309615660845819875721L;
-    r %= M;
-    const long long n8 = 8 * r;
-    const int oct = (int)(n8 / M);
-    const long long rem = n8 - (long long)oct * M;
-    const long double x = ((oct & 1) ? (long double)(M - rem) : (long double)rem) / (long double)M * PI_4;
-    const long double cx = cosl(x), sx = sinl(x);
-    long double C = 0, S = 0;
-    switch (oct) {
-        case 0: C = cx; S = sx; break;
-        case 1: C = sx; S = cx; break;
-        case 2: C = -sx; S = cx; break;
-        case 3: C = -cx; S = sx; break;
-        case 4: C = -cx; S = -sx; break;
-        case 5: C = -sx; S = -cx; break;
-        case 6: C = sx; S = -cx; break;
-        default: C = cx; S = -sx; break;
-    }
-    *c = (double)C;
-    *s = -(double)S;  // forward sign
-}
-
-// exp(-2 pi i m / M) = i^q * c * (1 + i t) with |t| <= 1 (needs 4 | M):
-// q0 = nearest quarter turn of m, residual angle th in [-pi/4, pi/4].
-void twiddle_fma(long long m, long long M, int* q, long double* c, long double* t) {
-    const long double PI = 3.141592653589793238462643383279502884L;
-    m %= M;
-    if (m < 0) m += M;
-    const long long q0 = (4 * m + M / 2) / M;
-    const long long mr = m - q0 * (M / 4);
-    const long double th = 2.0L * PI * (long double)mr / (long double)M;
-    *q = (int)((4 - (q0 % 4)) % 4);   // (-i)^q0 = i^-q0
-    *c = cosl(th);
-    *t = -sinl(th) / cosl(th);
-}
-
-// TwEnt blocks of every pass after the first with radix 4 or 2.
+// FMA-form twiddle blocks of a plan (s2d_plan.h) in a vector.
 template <typename T>
 std::vector<TwEnt<T>> fma_tables(Dims* d) {
-    std::vector<TwEnt<T>> tab;
-    int Ns = 1;
-    for (int p = 0; p < d->npass; ++p) {
-        const int R = d->radix[p];
-        d->twoff[p] = -1;
-        if (p > 0 && (R == 4 || R == 2)) {
-            d->twoff[p] = (int)tab.size();
-            const long long step = d->M / (Ns * R);
-            for (int k = 0; k < Ns; ++k) {
-                TwEnt<T> e{};
-                int qs[4] = {0, 0, 0, 0};
-                long double cs[4] = {1, 1, 1, 1}, ts[4] = {0, 0, 0, 0};
-                for (int r = 1; r < R; ++r) twiddle_fma((long long)r * k * step, d->M, &qs[r], &cs[r], &ts[r]);
-                e.t1 = (T)ts[1];
-                e.t2 = (T)ts[2];
-                e.t3 = (T)ts[3];
-                e.c1 = (T)cs[1];
-                e.c2 = (T)cs[2];
-                e.r31 = (T)(cs[3] / cs[1]);
-                e.q = qs[1] | (qs[2] << 2) | (qs[3] << 4);
-                tab.push_back(e);
-            }
-        }
-        Ns *= R;
-    }
+    std::vector<TwEnt<T>> tab((size_t)fma_table_entries(*d));
+    fill_fma_tables<T>(d, tab.data(), (int)tab.size());
     return tab;
-}
-
-bool factor_plan(int M, Dims* d) {
-    int m = M, a = 0, b = 0;
-    while (m % 2 == 0) { m /= 2; ++a; }
-    while (m % 3 == 0) { m /= 3; ++b; }
-    if (m != 1 || M % kElemsPerThread != 0) return false;
-    int np = 0;
-    for (int i = 0; i < b; ++i) d->radix[np++] = 3;
-    if (a % 2) d->radix[np++] = 2;
-    for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
-    if (np > kMaxPasses) return false;
-    d->npass = np;
-    set_pass_constants(d);
-    return true;
 }
 
 int kIntMaxBins(int kxMG, int kyMG) {
@@ -615,7 +539,7 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     // twiddles exp(-2 pi i t / M)
     {
         std::vector<double> twd(2 * (size_t)d.M);
-        for (int t = 0; t < d.M; ++t) twiddle(t, d.M, &twd[2 * t], &twd[2 * t + 1]);
+        fill_twiddles(d.M, twd.data());
         if (h->prec == S2D_FP64) {
             if (cudaMemcpy(h->tw, twd.data(), twd.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
                 return bail(fail(S2D_ERR_CUDA, "twiddle upload failed"));

@@ -82,7 +82,7 @@ __global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>:
     pdl_enter();
     const bool bad = yfwd_body<T>(d, Iu, Iv, S0, S1, Sdw, src, stage, dt, ph, tw, G, blockIdx.x,
                                   reinterpret_cast<VT*>(smem_raw));
-    if (bad) atomicOr(flags, 1u);
+    if (bad && flags) atomicOr(flags, 1u);   // flags may be null: no non-finite report
 }
 
 // K3 split in two (FP64 single runs): forward y-FFT of one field's columns

@@ -7,15 +7,18 @@
 // buffers it is handed.  For them s2d_compute_rhs_noalloc evaluates the
 // right-hand side of src/Spectral.F90:396-482 on caller-provided device arrays
 // and keeps all of its own scratch (compact state, 1/k^2 table, twiddle
-// tables, the two half-spectral intermediates, dW and a status word) in one
-// file-scope __device__ array of S2D_NOALLOC_SCRATCH_BYTES.  Every GPU that
-// loads the library holds that array until the process exits.
+// tables, the two half-spectral intermediates and dW) in one file-scope
+// __device__ array of S2D_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the
+// library holds that array until the process exits.
 //
 // Nothing here calls cudaMalloc, cudaFree, malloc/new or any allocating
-// library routine: twiddle tables are built in static host buffers and
-// copied into the scratch array.
+// library routine: the plan and twiddle tables are built by the handle
+// path's own builders (s2d_plan.h) into static host buffers and copied into
+// the scratch array when nx changes on a device; calls with the nx whose
+// tables are resident reuse the cached plan and upload nothing.
 #include "s2d.h"
 #include "s2d_internal.h"
+#include "s2d_plan.h"
 
 #include <cuda_runtime.h>
 
@@ -34,7 +37,9 @@ constexpr int kMaxM = 3 * S2D_NOALLOC_MAX_NX / 2;
 struct DevState {
     bool ready;              // symbol address resolved for this device
     unsigned char* base;     // device address of g_s2d_noalloc_scratch
-    int tables_nx;           // nx whose twiddle and 1/k^2 tables are resident
+    int tables_nx;           // nx whose twiddle and 1/k^2 tables are resident (0: none)
+    int ntab;                // FMA-form twiddle entries of that plan
+    Dims plan;               // that plan (radices, pass constants, table offsets)
     int max_smem;
 };
 DevState g_dev[kMaxDevices];
@@ -49,7 +54,7 @@ int err(int code, const char*) { return code; }
 
 size_t up256(size_t x) { return (x + 255) / 256 * 256; }
 
-// Same plan, twiddles and FMA-form twiddle blocks as the handle path.
+// Geometry and radix plan of the handle path (s2d_plan.h), FP64.
 bool plan_noalloc(int nx, Dims* d) {
     std::memset(d, 0, sizeof(*d));
     d->K = nx / 2;
@@ -58,87 +63,15 @@ bool plan_noalloc(int nx, Dims* d) {
     d->M = 3 * nx / 2;
     d->ldS = d->KY + 1;
     d->ldI = (d->KX + 3) / 4 * 4;
-    int m = d->M, a = 0, b = 0;
-    while (m % 2 == 0) { m /= 2; ++a; }
-    while (m % 3 == 0) { m /= 3; ++b; }
-    if (m != 1 || d->M % kElemsPerThread != 0) return false;
-    int np = 0;
-    for (int i = 0; i < b; ++i) d->radix[np++] = 3;
-    if (a % 2) d->radix[np++] = 2;
-    for (int i = 0; i < a / 2; ++i) d->radix[np++] = 4;
-    d->npass = np;
-    set_pass_constants(d);
+    if (!factor_plan(d->M, d)) return false;
     d->Tg = d->M / kElemsPerThread;
+    d->tab_bytes = (long long)up256((size_t)d->M * sizeof(double2));
     return true;
 }
 
-void tw_plain(long long r, long long M, double* c, double* s) {
-    const long double PI_4 = 0.785398163397448309615660845819875721L;
-    r %= M;
-    const long long n8 = 8 * r;
-    const int oct = (int)(n8 / M);
-    const long long rem = n8 - (long long)oct * M;
-    const long double x = ((oct & 1) ? (long double)(M - rem) : (long double)rem) / (long double)M * PI_4;
-    const long double cx = cosl(x), sx = sinl(x);
-    long double C = 0, S = 0;
-    switch (oct) {
-        case 0: C = cx; S = sx; break;
-        case 1: C = sx; S = cx; break;
-        case 2: C = -sx; S = cx; break;
-        case 3: C = -cx; S = sx; break;
-        case 4: C = -cx; S = -sx; break;
-        case 5: C = -sx; S = -cx; break;
-        case 6: C = sx; S = -cx; break;
-        default: C = cx; S = -sx; break;
-    }
-    *c = (double)C;
-    *s = -(double)S;
-}
-
-void tw_fma(long long m, long long M, int* q, long double* c, long double* t) {
-    const long double PI = 3.141592653589793238462643383279502884L;
-    m %= M;
-    if (m < 0) m += M;
-    const long long q0 = (4 * m + M / 2) / M;
-    const long long mr = m - q0 * (M / 4);
-    const long double th = 2.0L * PI * (long double)mr / (long double)M;
-    *q = (int)((4 - (q0 % 4)) % 4);
-    *c = cosl(th);
-    *t = -sinl(th) / cosl(th);
-}
-
-int fill_tables(Dims* d) {
-    for (int t = 0; t < d->M; ++t) tw_plain(t, d->M, &g_host_tw[2 * t], &g_host_tw[2 * t + 1]);
-    int n = 0, Ns = 1;
-    for (int p = 0; p < d->npass; ++p) {
-        const int R = d->radix[p];
-        d->twoff[p] = -1;
-        if (p > 0 && (R == 4 || R == 2)) {
-            d->twoff[p] = n;
-            const long long step = d->M / (Ns * R);
-            for (int k = 0; k < Ns; ++k) {
-                TwEnt<double> e{};
-                int qs[4] = {0, 0, 0, 0};
-                long double cs[4] = {1, 1, 1, 1}, ts[4] = {0, 0, 0, 0};
-                for (int r = 1; r < R; ++r) tw_fma((long long)r * k * step, d->M, &qs[r], &cs[r], &ts[r]);
-                e.t1 = (double)ts[1];
-                e.t2 = (double)ts[2];
-                e.t3 = (double)ts[3];
-                e.c1 = (double)cs[1];
-                e.c2 = (double)cs[2];
-                e.r31 = (double)(cs[3] / cs[1]);
-                e.q = qs[1] | (qs[2] << 2) | (qs[3] << 4);
-                g_host_tab[n++] = e;
-            }
-        }
-        Ns *= R;
-    }
-    return n;
-}
-
-// Carve the scratch array: flags | twiddles (+ FMA blocks) | rk2 | S | Sdw | I0 | I1.
+// Carve the scratch array: twiddles (+ FMA blocks) | rk2 | S | Sdw | I0 | I1.
 struct Carve {
-    size_t flags, tw, rk2, S, Sdw, I0, I1, end;
+    size_t tw, rk2, S, Sdw, I0, I1, end;
 };
 
 Carve carve(const Dims& d, int ntab) {
@@ -146,8 +79,7 @@ Carve carve(const Dims& d, int ntab) {
     const size_t state = (size_t)d.KX * d.ldS * sizeof(double2);
     const size_t inter = (size_t)d.M * d.ldI * sizeof(double2);
     const size_t twb = up256((size_t)d.M * sizeof(double2)) + (size_t)ntab * sizeof(TwEnt<double>);
-    c.flags = 0;
-    c.tw = 256;
+    c.tw = 0;
     c.rk2 = c.tw + up256(twb);
     c.S = c.rk2 + up256((size_t)d.KX * d.ldS * sizeof(double));
     c.Sdw = c.S + up256(state);
@@ -198,24 +130,35 @@ S2D_API int s2d_compute_rhs_noalloc(int32_t nx, double nu, const double* wC_dev,
         ds.tables_nx = 0;
         ds.ready = true;
     }
-    Dims d;
-    if (!plan_noalloc(nx, &d)) return err(S2D_ERR_UNSUPPORTED, "padded grid is not 2^a 3^b");
-    // the table layout is needed for the carve even when the tables are resident
-    const int ntab = fill_tables(&d);
-    d.tab_bytes = (long long)up256((size_t)d.M * sizeof(double2));
-    const Carve c = carve(d, ntab);
-    if (c.end > S2D_NOALLOC_SCRATCH_BYTES) return err(S2D_ERR_INVALID, "grid does not fit the static scratch");
     unsigned char* B = ds.base;
-    if (ds.tables_nx != nx) {
-        if (cudaMemcpyAsync(B + c.tw, g_host_tw, (size_t)d.M * sizeof(double2), cudaMemcpyHostToDevice, st) !=
+    Dims d;
+    int ntab;
+    if (ds.tables_nx == nx) {   // tables of this nx resident: the cached plan, no upload
+        d = ds.plan;
+        ntab = ds.ntab;
+    } else {
+        if (!plan_noalloc(nx, &d)) return err(S2D_ERR_UNSUPPORTED, "padded grid is not 2^a 3^b");
+        ntab = fill_fma_tables<double>(&d, g_host_tab, kMaxM);
+        if (ntab < 0) return err(S2D_ERR_INVALID, "twiddle table exceeds its static buffer");
+        if (carve(d, ntab).end > S2D_NOALLOC_SCRATCH_BYTES)
+            return err(S2D_ERR_INVALID, "grid does not fit the static scratch");
+        fill_twiddles(d.M, g_host_tw);
+        const Carve c0 = carve(d, ntab);
+        ds.tables_nx = 0;   // until the new tables are queued
+        // the copies are queued on st before any kernel of this call that reads them
+        if (cudaMemcpyAsync(B + c0.tw, g_host_tw, (size_t)d.M * sizeof(double2), cudaMemcpyHostToDevice, st) !=
                 cudaSuccess ||
-            cudaMemcpyAsync(B + c.tw + d.tab_bytes, g_host_tab, (size_t)ntab * sizeof(TwEnt<double>),
-                            cudaMemcpyHostToDevice, st) != cudaSuccess)
+            (ntab > 0 && cudaMemcpyAsync(B + c0.tw + d.tab_bytes, g_host_tab, (size_t)ntab * sizeof(TwEnt<double>),
+                                         cudaMemcpyHostToDevice, st) != cudaSuccess))
             return err(S2D_ERR_CUDA, "twiddle upload failed");
-        if (Kern<double>::init_rk2(d, (double*)(B + c.rk2), st) != cudaSuccess)
+        // pageable source buffers: the copies have read them when cudaMemcpyAsync returns
+        if (Kern<double>::init_rk2(d, (double*)(B + c0.rk2), st) != cudaSuccess)
             return err(S2D_ERR_CUDA, "1/k^2 table kernel failed");
+        ds.plan = d;
+        ds.ntab = ntab;
         ds.tables_nx = nx;
     }
+    const Carve c = carve(d, ntab);
     Phys ph{};
     ph.nu = nu;
     ph.form = S2D_NL_BASDEVANT;
@@ -236,14 +179,13 @@ S2D_API int s2d_compute_rhs_noalloc(int32_t nx, double nu, const double* wC_dev,
     fs.out[0] = B + c.I0;
     fs.out[1] = B + c.I1;
     const int C = d.M / 2 + 1;
-    // the status word must start at zero; every other region is fully
-    // written before it is read
-    if (cudaMemsetAsync(B + c.flags, 0, 256, st) != cudaSuccess) return err(S2D_ERR_CUDA, "memset failed");
+    // every region of the scratch is fully written before it is read; the
+    // stage kernel gets no status word (a NaN/Inf in dW is not reported)
     if (Kern<double>::ref_to_compact(d, wC_dev, C, B + c.S, st) != cudaSuccess ||
         Kern<double>::yinv(d, B + c.S, (const double*)(B + c.rk2), fs, B + c.tw, st, Ly) != cudaSuccess ||
         Kern<double>::xpass_bas(d, B + c.I0, B + c.I1, B + c.tw, st, Lx) != cudaSuccess ||
         Kern<double>::yfwd_rk3(d, B + c.I0, B + c.I1, B + c.S, B + c.S, B + c.Sdw, nullptr, 0, 0.0, ph, B + c.tw,
-                               (unsigned int*)(B + c.flags), st, Lf) != cudaSuccess ||
+                               nullptr, st, Lf) != cudaSuccess ||
         Kern<double>::compact_to_ref(d, B + c.Sdw, C, dW_dev, nullptr, st) != cudaSuccess)
         return err(S2D_ERR_CUDA, "kernel launch failed");
     return S2D_OK;

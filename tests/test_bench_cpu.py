@@ -36,3 +36,50 @@ def test_reference_arm_prints_one_json_line_with_its_contract_keys():
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["value"] == line["value"]
     assert line["e2e"] == {"value": line["value"], "unit": "Mpt*steps/s", "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def _dry(*extra):
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--gpus", "2", "--dry-cpu",
+                          "--steps", "3", "--warmup", "3", *extra],
+                         capture_output=True, text=True, timeout=300, cwd=ROOT,
+                         env={k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")})
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, out.stdout[-2000:]   # rank 0 alone prints
+    return json.loads(lines[0])
+
+
+def test_gpus_2_shards_the_ensemble_by_cost_over_two_gloo_ranks():
+    """bench.py --gpus 2 without a launcher starts two ranks; the 96-run
+    ensemble is split by cost, every run exactly once, and value is all
+    runs' points x steps over the slowest rank's time."""
+    import bench
+    from spectral2d_gb300.replicas import run_cost
+    line = _dry("--workload", "ensemble")
+    assert line["n_gpus"] == 2 and line["dry_cpu"] and line["scaling"] == "strong"
+    shards = line["shards"]
+    assert len(shards) == 2 and sorted(shards[0] + shards[1]) == list(range(96))
+    nxs, _ = bench.ensemble_runs()
+    loads = [sum(run_cost(nxs[i]) for i in s) for s in shards]
+    assert abs(loads[0] - loads[1]) <= max(run_cost(n) for n in nxs)
+    ms = line["ms_per_rank"]
+    pts = sum(n * n for n in nxs)
+    assert abs(line["value"] - pts * 3 / (max(ms) * 1e-3) / 1e6) <= 1e-9 * line["value"]
+    assert line["runs_per_rank"] == [len(s) for s in shards]
+
+
+def test_gpus_2_splits_the_les_batch_evenly():
+    line = _dry("--workload", "les-batch", "--les-runs", "10")
+    assert line["n_gpus"] == 2 and line["runs_per_rank"] == [5, 5]
+    assert sorted(line["shards"][0] + line["shards"][1]) == list(range(10))
+
+
+def test_gpus_2_replicas_sum_their_rates():
+    """The headline DNS workload: one replica per rank; value is the sum of
+    the per-rank rates taken at the slowest rank's time."""
+    line = _dry("--n", "64")
+    assert line["n_gpus"] == 2 and line["scaling"] == "weak"
+    ms = line["ms_per_rank"]
+    assert len(ms) == 2
+    per_rank = 64 * 64 * 3 / (max(ms) * 1e-3) / 1e6
+    assert abs(line["value"] - 2 * per_rank) <= 1e-9 * line["value"]
