@@ -340,6 +340,53 @@ S2D_API int s2d_les_time_steps(s2d_handle* les, int32_t n, double dt, double* ms
  * persistent stage launches, all in the step's CUDA graph. */
 S2D_API int s2d_batch_set_closure(s2d_batch* b, s2d_cnn* c);
 
+/* ---- one run decomposed over several ranks (slabs) --------------------- *
+ * The reference runs one simulation on several MPI ranks in slabs, with an
+ * all-to-all transpose inside every FFTW-MPI transform (src/Alloc.F90:90-100,
+ * src/Spectral.F90:340-349, :760, :780).  A slab here is one rank's share of
+ * a run: the kx columns [kx0, kx0 + nkx) of the spectral state, for the
+ * inverse y-pass (K1) and the forward y-pass with the stage update (K3),
+ * and the physical rows [y0, y0 + ny) for the x-pass (K2).  Each stage of
+ * IntegrateOneStep is three phases with two all-to-alls between them, which
+ * the CALLER performs (MPI_Alltoallv, NCCL, or copies between slabs of one
+ * process) on the slab's device buffers:
+ *
+ *   for stage in 1..3:
+ *     s2d_slab_phase(s, stage, 0, dt)   K1 on my columns, pack exchange 0
+ *     synchronise; all-to-all of exchange 0 (s2d_slab_exchange)
+ *     s2d_slab_phase(s, stage, 1, dt)   unpack, K2 on my rows, pack exchange 1
+ *     synchronise; all-to-all of exchange 1
+ *     s2d_slab_phase(s, stage, 2, dt)   unpack, K3 and the stage update
+ *
+ * Segment q of a send buffer goes to rank q; segment q of a receive buffer
+ * comes from rank q; segments follow one another in rank order with the
+ * byte counts s2d_slab_exchange gives.  Phases run asynchronously on the
+ * slab handle's stream (s2d_synchronize).  Every rank's handle holds
+ * full-size arrays: set the same initial state on every rank (s2d_set_state,
+ * s2d_set_turbulent, ... on s2d_slab_handle); after steps only the rank's
+ * own columns of its state are current, and s2d_slab_get_columns writes them
+ * (and psi) into reference-layout host arrays, leaving the other columns
+ * untouched.  The kernels are the single-run kernels on a column view or a
+ * row range, so a decomposed run equals the single run bit for bit.
+ * Basdevant form only. */
+#define S2D_SLAB_MAX_RANKS 16
+typedef struct s2d_slab s2d_slab;
+/* part = {kx0, nkx, y0, ny} of rank `rank` of nranks for an nx grid */
+S2D_API int s2d_slab_partition(int32_t nx, int32_t nranks, int32_t rank, int32_t part[4]);
+S2D_API int s2d_slab_create(const s2d_config* cfg, int32_t rank, int32_t nranks, s2d_slab** out);
+S2D_API void s2d_slab_destroy(s2d_slab* s);
+/* the slab's handle: initial conditions, set_state, CFL, s2d_synchronize */
+S2D_API int s2d_slab_handle(s2d_slab* s, s2d_handle** h);
+/* device send / receive buffers of exchange 0 or 1 (the same two buffers
+ * serve both) and the bytes per peer (arrays of nranks; either may be NULL) */
+S2D_API int s2d_slab_exchange(s2d_slab* s, int32_t exchange, void** send, void** recv, int64_t* send_bytes,
+                              int64_t* recv_bytes);
+/* phase 0, 1 or 2 of RK3 stage 1..3 (asynchronous on the slab's stream) */
+S2D_API int s2d_slab_phase(s2d_slab* s, int32_t stage, int32_t phase, double dt);
+/* the rank's columns of wC and psiC (either may be NULL, not both), reference
+ * layout; synchronises */
+S2D_API int s2d_slab_get_columns(s2d_slab* s, double* wC, double* psiC, int32_t cISize, int32_t nyG);
+
 /* ---- allocation-free right-hand side ----------------------------------- *
  * No counterpart in the reference.  For callers that must not allocate
  * device memory -- host codes whose device memory belongs to another

@@ -88,6 +88,14 @@ SIGNATURES = {
     "s2d_host_free": (C.c_int, [C.c_void_p]),
     "s2d_probe_fp64_peak": (C.c_int, [C.c_int32, _dp]),
     "s2d_compute_rhs_noalloc": (C.c_int, [C.c_int32, C.c_double, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "s2d_slab_partition": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int32)]),
+    "s2d_slab_create": (C.c_int, [C.POINTER(S2DConfig), C.c_int32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "s2d_slab_destroy": (None, [C.c_void_p]),
+    "s2d_slab_handle": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "s2d_slab_exchange": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                    C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "s2d_slab_phase": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_double]),
+    "s2d_slab_get_columns": (C.c_int, [C.c_void_p, _dp, _dp, C.c_int32, C.c_int32]),
     "s2d_batch_create": (C.c_int, [C.c_int32, C.POINTER(S2DConfig), C.POINTER(C.c_void_p)]),
     "s2d_batch_destroy": (None, [C.c_void_p]),
     "s2d_batch_size": (C.c_int, [C.c_void_p]),

@@ -22,8 +22,8 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libspectral2d_gb300.so")
 DRIVER = os.path.join(PKG, "spectral2d_run")
 
-SOURCES = ["s2d_kernels.cu", "s2d_capi.cu", "s2d_ic.cpp", "s2d_noalloc.cu", "s2d_batch.cu",
-           "s2d_closure.cu", "s2d_io.cu"]
+SOURCES = ["s2d_kernels.cu", "s2d_capi.cu", "s2d_ic.cpp", "s2d_ic_dev.cu", "s2d_noalloc.cu", "s2d_batch.cu",
+           "s2d_closure.cu", "s2d_io.cu", "s2d_slab.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
           "-Xcompiler", "-fvisibility=hidden", "-I", os.path.join(ROOT, "include"),

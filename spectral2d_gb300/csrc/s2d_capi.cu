@@ -441,6 +441,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         return fail(S2D_ERR_UNSUPPORTED, "padded grid %d is not 2^a 3^b with 12 | M", M);
     }
     d.Tg = d.M / kElemsPerThread;
+    d.rows = d.M;
+    d.kx0 = 0;
     h->ph.nu = cfg->nu;
     h->ph.alpha = cfg->alpha;
     h->ph.form = cfg->nonlinear_form;

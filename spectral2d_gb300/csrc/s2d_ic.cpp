@@ -9,6 +9,9 @@
 // hash of (seed, kx, ky) instead of the compiler RNG seeded from /dev/urandom
 // (src/Random.F90:59-69); the kx = 0 column is made Hermitian; omega is scaled
 // so that ComputeSpectrum's TKE equals the requested value.
+// s2d_set_turbulent computes the same initial condition on the device
+// (s2d_ic_dev.cu); this host generator serves callers without a GPU and
+// checks the device one.
 #include "s2d.h"
 #include "s2d_internal.h"
 
@@ -146,17 +149,6 @@ S2D_API int s2d_turbulent_ic_host(int32_t nx, uint64_t seed, int32_t spectrum, d
     }
     std::memcpy(wC, w.data(), sizeof(double) * 2 * n);
     return S2D_OK;
-}
-
-S2D_API int s2d_set_turbulent(s2d_handle* h, uint64_t seed, int32_t spectrum, double k0, double urms, double tke) {
-    if (!h) return S2D_ERR_INVALID;
-    s2d_grid g;
-    const int nx = s2d::handle_nx(h);
-    if (s2d_get_grid_size(nx, nx, S2D_DEALIAS_3_2_RULE, &g) != S2D_OK) return S2D_ERR_INVALID;
-    std::vector<double> wC((size_t)2 * g.cISize * g.nyG);
-    int r = s2d_turbulent_ic_host(nx, seed, spectrum, k0, urms, tke, wC.data());
-    if (r != S2D_OK) return r;
-    return s2d_set_state(h, wC.data(), g.cISize, g.nyG);
 }
 
 }  // extern "C"

@@ -55,6 +55,13 @@ struct Dims {
     // (0 for Ns = 1), for j mod Ns by a multiply-high, and M / (Ns R)
     unsigned mg[kMaxPasses];
     int tstep[kMaxPasses];
+    // slabs of a decomposed run (s2d_slab.cu); a whole run has rows = M and
+    // kx0 = 0.  rows: physical rows the x-pass processes.  kx0: true kx of
+    // column 0 of the arrays a kernel is handed (a slab's column view: KX
+    // columns from kx0 on), used where the wavenumber enters the arithmetic
+    // (truncation, 1/k^2, stage factors, forcing)
+    int rows;
+    int kx0;
 };
 
 // mg[] and tstep[] of a plan whose M, npass and radix[] are set.
@@ -298,6 +305,10 @@ int launch_step_sourced(s2d_handle* h, double dt, cudaEvent_t src_ready);
 // the network's grid and batch capacity
 int cnn_grid(const struct s2d_cnn* c);
 int cnn_max_batch(const struct s2d_cnn* c);
+
+// The turbulent initial condition (s2d_set_turbulent) computed on the
+// device into h->S0; synchronises the handle's stream (s2d_ic_dev.cu).
+int set_turbulent_device(s2d_handle* h, uint64_t seed, int spectrum, double k0, double urms, double tke);
 
 // Record msg as this thread's last error (s2d_last_error) and return code.
 int set_error(int code, const char* msg);

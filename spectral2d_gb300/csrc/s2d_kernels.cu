@@ -221,8 +221,8 @@ __global__ void __launch_bounds__(256) k_rect_to_compact(Dims d, const double2* 
         const int jc = jc0 + i, kx = kx0 + tx;
         double2 v = make_double2(0.0, 0.0);
         if (jc < d.KY && kx < d.KX) {
-            const int ky = ky_of_jc(d, jc);
-            if (kx * kx + ky * ky <= d.K * d.K) v = ref[(size_t)(ky >= 0 ? ky : ky + d.M) * C + kx];
+            const int ky = ky_of_jc(d, jc), kxt = kx + d.kx0;
+            if (kxt * kxt + ky * ky <= d.K * d.K) v = ref[(size_t)(ky >= 0 ? ky : ky + d.M) * C + kx];
         }
         tile[i][tx] = v;
     }
@@ -262,7 +262,8 @@ __global__ void __launch_bounds__(256) k_compact_to_rect(Dims d, const typename 
             const double2 w = tile[tx][i];
             if (refW) refW[o] = w;
             if (refPsi) {
-                const double k2 = (double)kx * kx + (double)ky * ky;
+                const double kxt = (double)(kx + d.kx0);
+                const double k2 = kxt * kxt + (double)ky * ky;
                 refPsi[o] = (k2 == 0.0) ? make_double2(0.0, 0.0) : make_double2(w.x / k2, w.y / k2);
             }
         }
@@ -651,7 +652,7 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
                                const Launch& L, bool prescaled) {
     using VT = typename Vec<T>::t;
     const T scale = prescaled ? (T)1 : (T)(0.5 / ((double)d.M * (double)d.M));
-    const int nb = (d.M + L.G - 1) / L.G;
+    const int nb = (d.rows + L.G - 1) / L.G;
     VT* u = (VT*)Iu;
     VT* v = (VT*)Iv;
     const VT* t = (const VT*)tw;

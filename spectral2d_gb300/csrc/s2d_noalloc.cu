@@ -65,6 +65,7 @@ bool plan_noalloc(int nx, Dims* d) {
     d->ldI = (d->KX + 3) / 4 * 4;
     if (!factor_plan(d->M, d)) return false;
     d->Tg = d->M / kElemsPerThread;
+    d->rows = d->M;
     d->tab_bytes = (long long)up256((size_t)d->M * sizeof(double2));
     return true;
 }

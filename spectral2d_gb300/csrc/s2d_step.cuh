@@ -199,7 +199,7 @@ __device__ __forceinline__ void xpass_bas_body(const Dims& d, typename Vec<T>::t
     const int g = threadIdx.x / d.Tg;
     const int lane = threadIdx.x - g * d.Tg;
     const int y = blk * G + g;
-    const bool active = y < d.M && g < G;
+    const bool active = y < d.rows && g < G;
     VT* Z = bufs + (size_t)g * d.M;
     VT* urow = Iu + (size_t)(active ? y : 0) * d.ldI;
     VT* vrow = Iv + (size_t)(active ? y : 0) * d.ldI;
@@ -224,9 +224,10 @@ __device__ __forceinline__ float mul_t(float a, float b) { return __fmul_rn(a, b
 
 // One mode (kx, jc) of the K3 epilogue: dW from the two transformed products
 // nx, ny, then the stage update below, Truncate (|k|^2 > K^2 -> 0) and the
-// non-finite check.  Returns true for a non-finite result.
+// non-finite check.  Returns true for a non-finite result.  kxl is the
+// mode's column in the arrays given (kx = kxl + d.kx0).
 template <typename T>
-__device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx, typename Vec<T>::t ny, int kx,
+__device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx, typename Vec<T>::t ny, int kxl,
                                             int jc, typename Vec<T>::t* S0, typename Vec<T>::t* S1,
                                             typename Vec<T>::t* Sdw, const typename Vec<T>::t* __restrict__ src,
                                             int stage, double dt, const Phys& ph, const T* fac = nullptr) {
@@ -238,8 +239,9 @@ __device__ __forceinline__ bool stage_point(const Dims& d, typename Vec<T>::t nx
     // stage kernel (its stage-3 launch took 107 instead of 76 us at 2048^2)
     const T dt4 = (T)(0.25 * dt), dt23 = (T)(dt * (2.0 / 3.0));
     const T tnu = (T)ph.nu, talpha = (T)ph.alpha;
+    const int kx = kxl + d.kx0;
     const int ky = ky_of_jc(d, jc);
-    const size_t off = (size_t)kx * d.ldS + jc;
+    const size_t off = (size_t)kxl * d.ldS + jc;
     const int kk = kx * kx + ky * ky;
     bool bad = false;
     VT out;

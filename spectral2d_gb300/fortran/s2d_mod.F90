@@ -189,5 +189,56 @@ MODULE s2d_m
          INTEGER(C_INT64_T), INTENT(OUT) :: nadv
          REAL(C_DOUBLE), INTENT(OUT) :: time
       END FUNCTION s2d_checkpoint_read
+
+      ! One run over several MPI ranks (the reference's slab decomposition,
+      ! src/Alloc.F90:90-100): per RK3 stage, phases 0, 1, 2 with an
+      ! MPI_Alltoallv of the slab's device buffers after phases 0 and 1
+      ! (CUDA-aware MPI), byte counts from s2d_slab_exchange.
+      INTEGER(C_INT) FUNCTION s2d_slab_partition(nx, nranks, rank, part) BIND(C, NAME='s2d_slab_partition')
+         IMPORT :: C_INT, C_INT32_T
+         INTEGER(C_INT32_T), VALUE :: nx, nranks, rank
+         INTEGER(C_INT32_T), DIMENSION(4), INTENT(OUT) :: part   ! kx0, nkx, y0, ny
+      END FUNCTION s2d_slab_partition
+
+      INTEGER(C_INT) FUNCTION s2d_slab_create(cfg, rank, nranks, s) BIND(C, NAME='s2d_slab_create')
+         IMPORT :: C_INT, C_INT32_T, C_PTR, s2d_config_t
+         TYPE(s2d_config_t), INTENT(IN) :: cfg
+         INTEGER(C_INT32_T), VALUE :: rank, nranks
+         TYPE(C_PTR), INTENT(OUT) :: s
+      END FUNCTION s2d_slab_create
+
+      SUBROUTINE s2d_slab_destroy(s) BIND(C, NAME='s2d_slab_destroy')
+         IMPORT :: C_PTR
+         TYPE(C_PTR), VALUE :: s
+      END SUBROUTINE s2d_slab_destroy
+
+      INTEGER(C_INT) FUNCTION s2d_slab_handle(s, h) BIND(C, NAME='s2d_slab_handle')
+         IMPORT :: C_INT, C_PTR
+         TYPE(C_PTR), VALUE :: s
+         TYPE(C_PTR), INTENT(OUT) :: h
+      END FUNCTION s2d_slab_handle
+
+      INTEGER(C_INT) FUNCTION s2d_slab_exchange(s, xchg, sendbuf, recvbuf, sendBytes, recvBytes) &
+            BIND(C, NAME='s2d_slab_exchange')
+         IMPORT :: C_INT, C_INT32_T, C_INT64_T, C_PTR
+         TYPE(C_PTR), VALUE :: s
+         INTEGER(C_INT32_T), VALUE :: xchg
+         TYPE(C_PTR), INTENT(OUT) :: sendbuf, recvbuf
+         INTEGER(C_INT64_T), DIMENSION(*), INTENT(OUT) :: sendBytes, recvBytes
+      END FUNCTION s2d_slab_exchange
+
+      INTEGER(C_INT) FUNCTION s2d_slab_phase(s, stage, phase, dt) BIND(C, NAME='s2d_slab_phase')
+         IMPORT :: C_INT, C_INT32_T, C_PTR, C_DOUBLE
+         TYPE(C_PTR), VALUE :: s
+         INTEGER(C_INT32_T), VALUE :: stage, phase
+         REAL(C_DOUBLE), VALUE :: dt
+      END FUNCTION s2d_slab_phase
+
+      INTEGER(C_INT) FUNCTION s2d_slab_get_columns(s, wC, psiC, cISize, nyG) BIND(C, NAME='s2d_slab_get_columns')
+         IMPORT :: C_INT, C_INT32_T, C_PTR, C_DOUBLE_COMPLEX
+         TYPE(C_PTR), VALUE :: s
+         INTEGER(C_INT32_T), VALUE :: cISize, nyG
+         COMPLEX(C_DOUBLE_COMPLEX), DIMENSION(cISize, nyG), INTENT(INOUT) :: wC, psiC
+      END FUNCTION s2d_slab_get_columns
    END INTERFACE
 END MODULE s2d_m
