@@ -215,6 +215,23 @@ S2D_API int s2d_synchronize(s2d_handle* h);
 S2D_API int s2d_time_steps(s2d_handle* h, int32_t n, double dt, double* ms,
                            double* kernel_ms);
 
+/* Radix order of the handle's FFTs (M = 2^a 3^b): plan 0 (the default) runs
+ * the radix-3 passes first -- the first one pruned for the truncated
+ * spectra of the inverse transforms -- then a radix-2 pass when a is odd,
+ * then radix-4 passes; plan 1 puts the radix-2 pass last; plan 2 runs the
+ * radix-2 and radix-4 passes first and the radix-3 passes last (no pruned
+ * pass).  Plans round differently (results agree to round-off, not bit for
+ * bit).  s2d_set_fft_plan rebuilds the twiddle tables (synchronises; not
+ * with a closure attached); s2d_tune_fft_plan times every plan on this
+ * handle's step with time step dt (its state is restored), keeps the
+ * fastest, and writes it and, when ms is not NULL, each plan's ms per step
+ * (S2D_FFT_PLANS entries) -- the autotuner of the radix schedule, the part
+ * of FFTW_MEASURE planning (src/Spectral.F90:340-349) that applies here. */
+#define S2D_FFT_PLANS 3
+S2D_API int s2d_set_fft_plan(s2d_handle* h, int32_t plan);
+S2D_API int s2d_get_fft_plan(const s2d_handle* h, int32_t* plan);
+S2D_API int s2d_tune_fft_plan(s2d_handle* h, double dt, int32_t* plan, double* ms);
+
 /* Kernels launched per RK3 step (for launch accounting). */
 S2D_API int s2d_kernels_per_step(const s2d_handle* h);
 
@@ -263,9 +280,12 @@ S2D_API int s2d_batch_time_steps(s2d_batch* b, int32_t n, double* ms);
  * S2D_ERR_NONFINITE if a run produced NaN/Inf; clears the flags. */
 S2D_API int s2d_batch_status(s2d_batch* b);
 S2D_API int s2d_batch_synchronize(s2d_batch* b);
-/* Autotuner: times the candidate tile schedules (128/256/512 threads per CTA,
- * i.e. transforms per tile, and 1-4 CTAs per SM) on this ensemble, keeps the
- * fastest and restores every run's state.  Any output may be NULL. */
+/* Autotuner: first the FFT radix plan of each run size (every plan of
+ * s2d_set_fft_plan, one size at a time; skipped with a closure attached),
+ * then the tile schedule (128/256/512 threads per CTA, i.e. transforms per
+ * tile, and 1-4 CTAs per SM), each timed on this ensemble; keeps the fastest
+ * and restores every run's state.  The chosen plans are read with
+ * s2d_get_fft_plan on the run handles.  Any output may be NULL. */
 S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads, int32_t* ctas_per_sm, double* ms_per_step);
 /* Fault injection for tests, made on the host: the x-pass tiles of run
  * `run` wait for an inverse y-pass tile that does not exist, so every step
@@ -304,6 +324,16 @@ S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t batch, floa
  * (same layout as the parameters) */
 S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, int32_t batch, float* grads,
                               double* loss);
+/* Introspection for tests and debugging.  With keep != 0 the gradient calls
+ * that follow keep dL/dz of every hidden layer in buffers of their own (five
+ * more activation-sized buffers; keep = 0 frees them).  s2d_cnn_get_tensor
+ * copies, as float, a BF16 tensor of the last forward/gradient call for the
+ * first `batch` images, layout [batch][grid][grid][channels padded to 16 or
+ * 32]: kind 0 = the input activations of `layer` (layer 0: the normalised
+ * network input), 1 = its pre-activation z (layers 0-4, after a gradient
+ * call), 2 = dL/dz of its output (layer 5 always; layers 0-4 when kept). */
+S2D_API int s2d_cnn_keep_layer_grads(s2d_cnn* c, int32_t keep);
+S2D_API int s2d_cnn_get_tensor(s2d_cnn* c, int32_t kind, int32_t layer, int32_t batch, float* out);
 /* device-resident training set of (w, psi, Pi) snapshots */
 S2D_API int s2d_cnn_dataset_reserve(s2d_cnn* c, int32_t capacity);
 S2D_API int s2d_cnn_dataset_size(const s2d_cnn* c);

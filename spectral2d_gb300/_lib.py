@@ -31,6 +31,7 @@ S2D_SPECTRUM_SCHUMANN = 0
 S2D_SPECTRUM_K4_GAUSS = 1
 S2D_NL_BASDEVANT = 0
 S2D_NL_CONSERVATIVE = 1
+S2D_FFT_PLANS = 3
 
 
 class S2DGrid(C.Structure):
@@ -84,6 +85,9 @@ SIGNATURES = {
     "s2d_synchronize": (C.c_int, [_h]),
     "s2d_time_steps": (C.c_int, [_h, C.c_int32, C.c_double, _dp, _dp]),
     "s2d_kernels_per_step": (C.c_int, [_h]),
+    "s2d_set_fft_plan": (C.c_int, [_h, C.c_int32]),
+    "s2d_get_fft_plan": (C.c_int, [_h, C.POINTER(C.c_int32)]),
+    "s2d_tune_fft_plan": (C.c_int, [_h, C.c_double, C.POINTER(C.c_int32), _dp]),
     "s2d_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "s2d_host_free": (C.c_int, [C.c_void_p]),
     "s2d_probe_fp64_peak": (C.c_int, [C.c_int32, _dp]),
@@ -118,6 +122,8 @@ SIGNATURES = {
     "s2d_cnn_get_band": (C.c_int, [C.c_void_p, _dp]),
     "s2d_cnn_forward_host": (C.c_int, [C.c_void_p, _fp, C.c_int32, _fp]),
     "s2d_cnn_grad_host": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int32, _fp, _dp]),
+    "s2d_cnn_keep_layer_grads": (C.c_int, [C.c_void_p, C.c_int32]),
+    "s2d_cnn_get_tensor": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _fp]),
     "s2d_cnn_dataset_reserve": (C.c_int, [C.c_void_p, C.c_int32]),
     "s2d_cnn_dataset_size": (C.c_int, [C.c_void_p]),
     "s2d_cnn_dataset_add": (C.c_int, [C.c_void_p, C.c_void_p]),

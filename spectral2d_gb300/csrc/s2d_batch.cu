@@ -112,7 +112,18 @@ __global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict
                 fs.out[1] = R.I1;
                 yinv_body<T>(R.d, stage <= 1 ? R.S0 : R.S1, R.rk2, fs, R.tw, R.G12, blk, bufs);
             } else if (ph == 1) {
-                xpass_bas_body<T>(R.d, R.I0, R.I1, R.tw, R.G12, (T)1, blk, bufs);
+                bool done32 = false;
+                if constexpr (sizeof(T) == 4) {
+                    // FP32 rows of M = 3072: the register radix-12/16 x-pass of
+                    // the single run (k_xpass32), one row per 256 threads
+                    if (R.d.M == kX32M && !R.d.xgen) {
+                        const int g = threadIdx.x / 256, y = blk * R.G12 + g;
+                        xpass32_m3072_row(R.d, R.I0, R.I1, R.tw, y, y < R.d.rows && g < R.G12,
+                                          threadIdx.x - g * 256, bufs + (size_t)g * kX32Buf);
+                        done32 = true;
+                    }
+                }
+                if (!done32) xpass_bas_body<T>(R.d, R.I0, R.I1, R.tw, R.G12, (T)1, blk, bufs);
             } else {
                 bad |= yfwd_body<T>(R.d, R.I0, R.I1, R.S0, R.S1, nullptr, R.src, stage, R.dt, R.ph, R.tw, R.G3,
                                     blk, bufs);
@@ -234,6 +245,8 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
         R.ntask[1] = (h->d.M + R.G12 - 1) / R.G12;
         R.ntask[2] = (h->d.KX + R.G3 - 1) / R.G3;
         smem = std::max(smem, (size_t)R.G12 * h->d.M * sizeof(VT));
+        if (sizeof(T) == 4 && h->d.M == kX32M)   // the register radix-12/16 x-pass (s2d_xpass32.cuh)
+            smem = std::max(smem, (size_t)R.G12 * kX32Buf * sizeof(VT));
         smem = std::max(smem, (size_t)2 * R.G3 * h->d.M * sizeof(VT));
         for (int p = 0; p < 3; ++p)
             for (int k = 0; k < R.ntask[p]; ++k) tasks[p].push_back(make_int4(i, p, k, 0));
@@ -494,6 +507,34 @@ S2D_API int s2d_batch_tune(s2d_batch* b, int32_t* threads_out, int32_t* ctas_per
     }
     int maxTg = 1;
     for (auto* h : b->runs) maxTg = std::max(maxTg, h->d.Tg);
+    // radix plan of each run size (not with a closure attached: its tables
+    // hold the runs' plans): every plan of one size at a time, the others
+    // fixed, on the current tile schedule
+    if (!b->cnn) {
+        std::vector<int> sizes;
+        for (auto* h : b->runs)
+            if (std::find(sizes.begin(), sizes.end(), h->d.M) == sizes.end()) sizes.push_back(h->d.M);
+        for (int M : sizes) {
+            double bms = 1e300;
+            int bp = -1;
+            for (int p = 0; p < S2D_FFT_PLANS; ++p) {
+                bool ok = true;
+                for (auto* h : b->runs)
+                    if (h->d.M == M && s2d_set_fft_plan(h, p) != S2D_OK) ok = false;
+                if (!ok || configure_any(b, b->threads, b->ctas_per_sm) != S2D_OK) continue;
+                double ms = 0.0;
+                if (s2d_batch_integrate_steps(b, 1) != S2D_OK) continue;
+                if (s2d_batch_time_steps(b, 2, &ms) != S2D_OK) continue;
+                if (ms < bms) {
+                    bms = ms;
+                    bp = p;
+                }
+            }
+            if (bp < 0) bp = 0;
+            for (auto* h : b->runs)
+                if (h->d.M == M) s2d_set_fft_plan(h, bp);
+        }
+    }
     double best = 1e300;
     int bt = 0, bc = 0;
     for (int threads : {128, 256, 512}) {

@@ -443,6 +443,10 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     d.Tg = d.M / kElemsPerThread;
     d.rows = d.M;
     d.kx0 = 0;
+    {
+        const char* xg = std::getenv("S2D_XPASS_GENERIC");
+        d.xgen = (xg && xg[0] == '1') ? 1 : 0;
+    }
     h->ph.nu = cfg->nu;
     h->ph.alpha = cfg->alpha;
     h->ph.form = cfg->nonlinear_form;
@@ -530,7 +534,18 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     d.tab_bytes = (long long)(((size_t)d.M * h->vsz + 63) / 64 * 64);
     const size_t tab_size = h->prec == S2D_FP64 ? tabd.size() * sizeof(TwEnt<double>)
                                                 : tabf.size() * sizeof(TwEnt<float>);
-    S2D_ALLOC(h->tw, (size_t)d.tab_bytes + tab_size + 64);
+    {
+        // room for the FMA-form blocks of every radix plan (s2d_set_fft_plan)
+        size_t cap = tab_size;
+        for (int p = 0; p < kNumPlans; ++p) {
+            Dims dp = d;
+            if (factor_plan(d.M, &dp, p))
+                cap = std::max(cap, (size_t)fma_table_entries(dp) *
+                                        (h->prec == S2D_FP64 ? sizeof(TwEnt<double>) : sizeof(TwEnt<float>)));
+        }
+        h->tab_cap = cap;
+    }
+    S2D_ALLOC(h->tw, (size_t)d.tab_bytes + h->tab_cap + 64);
     S2D_ALLOC(h->flags, 64);
     S2D_ALLOC(h->red64, 8 * sizeof(unsigned long long));
     h->dscratch_n = std::max<size_t>(d.K + 1, 4096);
@@ -624,6 +639,79 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     if (h->ev_join) cudaEventDestroy(h->ev_join);
     if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
     delete h;
+}
+
+static_assert(kNumPlans == S2D_FFT_PLANS, "plan count of the header");
+
+S2D_API int s2d_set_fft_plan(s2d_handle* h, int32_t plan) {
+    if (!h) return fail(S2D_ERR_INVALID, "null handle");
+    if (plan < 0 || plan >= kNumPlans) return fail(S2D_ERR_INVALID, "plan %d outside [0, %d)", plan, kNumPlans);
+    if (plan == h->plan) return S2D_OK;
+    if (h->cnn) return fail(S2D_ERR_INVALID, "detach the closure before changing the radix plan");
+    S2D_CUDA(cudaSetDevice(h->device));
+    Dims d = h->d;
+    if (!factor_plan(d.M, &d, plan)) return fail(S2D_ERR_UNSUPPORTED, "radix plan %d does not apply", plan);
+    S2D_CUDA(cudaStreamSynchronize(h->stream));
+    if (h->prec == S2D_FP64) {
+        const std::vector<TwEnt<double>> t = fma_tables<double>(&d);
+        if (t.size() * sizeof(TwEnt<double>) > h->tab_cap) return fail(S2D_ERR_UNSUPPORTED, "twiddle table too big");
+        if (!t.empty())
+            S2D_CUDA(cudaMemcpy((char*)h->tw + d.tab_bytes, t.data(), t.size() * sizeof(TwEnt<double>),
+                                cudaMemcpyHostToDevice));
+    } else {
+        const std::vector<TwEnt<float>> t = fma_tables<float>(&d);
+        if (t.size() * sizeof(TwEnt<float>) > h->tab_cap) return fail(S2D_ERR_UNSUPPORTED, "twiddle table too big");
+        if (!t.empty())
+            S2D_CUDA(cudaMemcpy((char*)h->tw + d.tab_bytes, t.data(), t.size() * sizeof(TwEnt<float>),
+                                cudaMemcpyHostToDevice));
+    }
+    h->d = d;
+    h->plan = plan;
+    drop_graph(h);   // the step's graph holds the old plan's Dims
+    return S2D_OK;
+}
+
+S2D_API int s2d_get_fft_plan(const s2d_handle* h, int32_t* plan) {
+    if (!h || !plan) return fail(S2D_ERR_INVALID, "null argument");
+    *plan = h->plan;
+    return S2D_OK;
+}
+
+S2D_API int s2d_tune_fft_plan(s2d_handle* h, double dt, int32_t* plan, double* ms) {
+    if (!h || !std::isfinite(dt)) return fail(S2D_ERR_INVALID, "null handle or bad dt");
+    S2D_CUDA(cudaSetDevice(h->device));
+    const size_t bytes = (size_t)h->d.KX * h->d.ldS * h->vsz;
+    void* save = nullptr;
+    S2D_CUDA(cudaMalloc(&save, bytes));
+    S2D_CUDA(cudaMemcpyAsync(save, h->S0, bytes, cudaMemcpyDeviceToDevice, h->stream));
+    const int start = h->plan;
+    double best = 1e300;
+    int bp = start;
+    int r = S2D_OK;
+    // about 0.1 s of steps per candidate, at least 3
+    const int n = std::max(3, std::min(200, (int)(4.0e8 / ((double)h->d.M * h->d.M + 1.0))));
+    for (int p = 0; p < kNumPlans && r == S2D_OK; ++p) {
+        if (s2d_set_fft_plan(h, p) != S2D_OK) continue;
+        double t = 0.0;
+        r = s2d_integrate_steps(h, 1, dt);   // warm-up (graph build)
+        if (r == S2D_OK) r = s2d_time_steps(h, n, dt, &t, nullptr);
+        if (r != S2D_OK) break;
+        if (ms) ms[p] = t / n;
+        if (t < best) {
+            best = t;
+            bp = p;
+        }
+    }
+    cudaMemcpyAsync(h->S0, save, bytes, cudaMemcpyDeviceToDevice, h->stream);
+    cudaStreamSynchronize(h->stream);
+    cudaFree(save);
+    if (r != S2D_OK) {
+        s2d_set_fft_plan(h, start);
+        return r;
+    }
+    S2D_TRY(s2d_set_fft_plan(h, bp));
+    if (plan) *plan = bp;
+    return S2D_OK;
 }
 
 S2D_API int s2d_set_state(s2d_handle* h, const double* wC, int32_t cISize, int32_t nyG) {

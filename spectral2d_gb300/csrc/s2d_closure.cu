@@ -960,6 +960,10 @@ struct s2d_cnn {
     __nv_bfloat16* X0 = nullptr;
     __nv_bfloat16 *Z[kLayers - 1] = {}, *A[kLayers - 1] = {};
     __nv_bfloat16 *dZ6 = nullptr, *dZa = nullptr, *dZb = nullptr;
+    // s2d_cnn_keep_layer_grads: dL/dz of every hidden layer kept (else the
+    // backward pass reuses two buffers)
+    __nv_bfloat16* dZk[kLayers - 1] = {};
+    bool keep = false;
     float *Y = nullptr, *tgt = nullptr;
     float* part = nullptr;
     long part_n = 0;
@@ -1040,7 +1044,7 @@ int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
             k_reduce_rows<<<nblocks(n, 256), 256, 0, c->stream>>>(c->part, c->wg_blocks, n, c->grad + c->poff[l]);
             C_CUDA(cudaGetLastError());
             if (l > 0) {
-                __nv_bfloat16* out = bufs[l & 1];
+                __nv_bfloat16* out = c->keep ? c->dZk[l - 1] : bufs[l & 1];
                 if (CO == 16)
                     C_CUDA((launch_conv<16, 32, -1, 2>(dz, c->WTb[l], nullptr, c->Z[l - 1], out, nullptr, nullptr,
                                                        B, c->H, c->Wd, c->cflags, c->sms, c->stream)));
@@ -1426,6 +1430,7 @@ S2D_API void s2d_cnn_destroy(s2d_cnn* c) {
     for (int l = 0; l < kLayers - 1; ++l) {
         if (c->Z[l]) cudaFree(c->Z[l]);
         if (c->A[l]) cudaFree(c->A[l]);
+        if (c->dZk[l]) cudaFree(c->dZk[l]);
     }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1512,6 +1517,60 @@ S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, i
         padded_to_logical(pad, grads, c->poff);
     }
     return s2d_cnn_status(c);
+}
+
+S2D_API int s2d_cnn_keep_layer_grads(s2d_cnn* c, int32_t keep) {
+    if (!c) return cerr(S2D_ERR_INVALID, "null network");
+    C_CUDA(cudaSetDevice(c->device));
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    const size_t n = (size_t)c->maxB * c->H * c->Wd * 32 * sizeof(__nv_bfloat16);
+    for (int l = 0; l < kLayers - 1; ++l) {
+        if (keep && !c->dZk[l] && cudaMalloc(&c->dZk[l], n) != cudaSuccess) {
+            for (int j = 0; j < kLayers - 1; ++j) {
+                cudaFree(c->dZk[j]);
+                c->dZk[j] = nullptr;
+            }
+            c->keep = false;
+            return cerr(S2D_ERR_NOMEM, "cudaMalloc of the layer-gradient buffers failed");
+        }
+        if (!keep && c->dZk[l]) {
+            cudaFree(c->dZk[l]);
+            c->dZk[l] = nullptr;
+        }
+    }
+    c->keep = keep != 0;
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_get_tensor(s2d_cnn* c, int32_t kind, int32_t layer, int32_t batch, float* out) {
+    if (!c || !out || layer < 0 || layer >= kLayers || batch < 1 || batch > c->maxB)
+        return cerr(S2D_ERR_INVALID, "bad tensor request");
+    const __nv_bfloat16* src = nullptr;
+    int ch = 32;
+    if (kind == 0) {                 // the layer's input activations
+        src = layer == 0 ? c->X0 : c->A[layer - 1];
+        ch = kCinP[layer];
+    } else if (kind == 1) {          // its pre-activation z (hidden layers)
+        if (layer == kLayers - 1) return cerr(S2D_ERR_INVALID, "the output layer keeps no pre-activation");
+        src = c->Z[layer];
+    } else if (kind == 2) {          // dL/dz of its output
+        if (layer == kLayers - 1) {
+            src = c->dZ6;
+            ch = kCoutP[layer];
+        } else {
+            if (!c->keep) return cerr(S2D_ERR_INVALID, "layer gradients are kept only after s2d_cnn_keep_layer_grads");
+            src = c->dZk[layer];
+        }
+    } else {
+        return cerr(S2D_ERR_INVALID, "kind must be 0, 1 or 2");
+    }
+    C_CUDA(cudaSetDevice(c->device));
+    const size_t n = (size_t)batch * c->H * c->Wd * ch;
+    std::vector<__nv_bfloat16> h(n);
+    C_CUDA(cudaMemcpyAsync(h.data(), src, n * sizeof(__nv_bfloat16), cudaMemcpyDeviceToHost, c->stream));
+    C_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < n; ++i) out[i] = __bfloat162float(h[i]);
+    return S2D_OK;
 }
 
 S2D_API int s2d_cnn_dataset_reserve(s2d_cnn* c, int32_t capacity) {

@@ -22,6 +22,10 @@ namespace s2d {
 
 constexpr int kMaxPasses = 16;
 constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
+// the FP32 x-pass with register radix-12/16 passes (s2d_xpass32.cuh): row
+// length and its padded shared-memory buffer (elements)
+constexpr int kX32M = 3072;
+constexpr int kX32Buf = kX32M + kX32M / 32;
 
 // Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
 // w_r = i^q_r * c_r * (1 + i t_r) with |t_r| <= 1, so that x*w_r costs two
@@ -62,6 +66,10 @@ struct Dims {
     // (truncation, 1/k^2, stage factors, forcing)
     int rows;
     int kx0;
+    // 1: the FP32 x-pass of M = 3072 runs the generic engine instead of the
+    // register radix-12/16 passes (s2d_xpass32.cuh); S2D_XPASS_GENERIC=1
+    // (read by s2d_create) sets it, for comparisons
+    int xgen;
 };
 
 // mg[] and tstep[] of a plan whose M, npass and radix[] are set.
@@ -273,6 +281,8 @@ struct s2d_handle {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t gexec = nullptr;
     double graph_dt = 0.0;
+    int plan = 0;          // radix order of the FFTs (s2d_plan.h, s2d_set_fft_plan)
+    size_t tab_cap = 0;    // bytes reserved for the FMA-form twiddle blocks (the largest plan's)
     int max_smem = 0;
     int sms = 152;
 };

@@ -39,6 +39,9 @@ namespace s2d {
 //   B = 2: FP32 CTAs of at most 512 threads (M = 6144), two per SM (64
 //          registers);
 //   B = 0: one CTA of up to 512 threads per SM.
+// (Wider FP32 column tiles -- 2 or 4 columns per CTA of 512 or 1024 threads,
+// so that the half-spectral rows are written and gathered a sector at a
+// time -- measured slower at 2048^2: 0.81 / 0.82 against 0.774 ms per step.)
 // ------------------------------------------------------------------------
 template <int B>
 constexpr int kMaxThreads = B == 1 ? 256 : 512;
@@ -69,8 +72,18 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_xpass_ba
     xpass_bas_body<T>(d, Iu, Iv, tw, G, scale, blockIdx.x, reinterpret_cast<VT*>(smem_raw));
 }
 
-template <typename T>
-__global__ void __launch_bounds__(512) k_yfwd_rk3(Dims d, const typename Vec<T>::t* __restrict__ Iu,
+// The FP32 x-pass of M = 3072 rows (s2d_xpass32.cuh): one row per 256-thread
+// CTA, three CTAs per SM (the radix-16 passes hold 16 complex values per
+// thread; inlined into k_xpass_bas at its four-per-SM budget of 64 registers
+// they spilled).
+__global__ void __launch_bounds__(256, 3) k_xpass32(Dims d, float2* Iu, float2* Iv, const float2* __restrict__ tw) {
+    __shared__ float2 sb[kX32Buf];
+    pdl_enter();
+    xpass32_m3072_row(d, Iu, Iv, tw, blockIdx.x, (int)blockIdx.x < d.rows, threadIdx.x, sb);
+}
+
+template <typename T, int B>
+__global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_yfwd_rk3(Dims d, const typename Vec<T>::t* __restrict__ Iu,
                                                    const typename Vec<T>::t* __restrict__ Iv,
                                                    typename Vec<T>::t* S0, typename Vec<T>::t* S1,
                                                    typename Vec<T>::t* Sdw,
@@ -656,6 +669,9 @@ cudaError_t Kern<T>::xpass_bas(const Dims& d, void* Iu, void* Iv, const void* tw
     VT* u = (VT*)Iu;
     VT* v = (VT*)Iv;
     const VT* t = (const VT*)tw;
+    if constexpr (sizeof(T) == 4)
+        if (d.M == kX32M && prescaled && !d.xgen)
+            return launch_k(k_xpass32, d.rows, 256, 0, st, L.pdl, d, (float2*)Iu, (float2*)Iv, (const float2*)tw);
     switch (budget<T>(L.threads)) {
         case 1: return launch_k(k_xpass_bas<T, 1>, nb, L.threads, L.smem, st, L.pdl, d, u, v, t, L.G, scale);
         case 2:
@@ -671,9 +687,15 @@ cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, voi
                               const void* src, int stage, double dt, const Phys& ph, const void* tw,
                               unsigned int* flags, cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
-    return launch_k(k_yfwd_rk3<T>, (d.KX + L.G - 1) / L.G, L.threads, L.smem, st, L.pdl, d, (const VT*)Iu,
-                    (const VT*)Iv, (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G,
-                    flags);
+    const int nb = (d.KX + L.G - 1) / L.G;
+    // FP32 CTAs of up to 256 threads at 64 registers, four per SM (at 80
+    // registers, three per SM: 0.244 against 0.219 ms of K3 per 2048^2 step)
+    if constexpr (sizeof(T) == 4)
+        if (L.threads <= 256)
+            return launch_k(k_yfwd_rk3<T, 1>, nb, L.threads, L.smem, st, L.pdl, d, (const VT*)Iu, (const VT*)Iv,
+                            (VT*)S0, (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G, flags);
+    return launch_k(k_yfwd_rk3<T, 0>, nb, L.threads, L.smem, st, L.pdl, d, (const VT*)Iu, (const VT*)Iv, (VT*)S0,
+                    (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G, flags);
 }
 
 template <typename T>
@@ -864,8 +886,9 @@ cudaError_t configure_kernels(int max_smem_optin) {
     S2D_SET((k_yfwd_col<float, 1>));
     S2D_SET((k_yfwd_col<float, 2>));
     S2D_SET((k_yfwd_col<float, 0>));
-    S2D_SET(k_yfwd_rk3<double>);
-    S2D_SET(k_yfwd_rk3<float>);
+    S2D_SET((k_yfwd_rk3<double, 0>));
+    S2D_SET((k_yfwd_rk3<float, 0>));
+    S2D_SET((k_yfwd_rk3<float, 1>));
     S2D_SET(k_xinv_cfl<double>);
     S2D_SET(k_xinv_moments<double>);
     S2D_SET(k_xinv_moments<float>);

@@ -50,22 +50,40 @@ inline void twiddle_fma(long long m, long long M, int* q, long double* c, long d
     *t = -sinl(th) / cosl(th);
 }
 
-// Radix sequence of a length-M transform (M = 2^a 3^b, 12 | M): the radix-3
-// passes first (the first one is the pruned pass of the inverse transforms),
-// then one radix-2 pass when a is odd, then radix-4 passes; sets npass,
-// radix[] and the per-pass constants.  False if M has another factor or the
-// plan needs more than kMaxPasses passes.
-inline bool factor_plan(int M, Dims* d) {
+// Radix sequences of a length-M transform (M = 2^a 3^b, 12 | M):
+//   plan 0: the radix-3 passes first (the first one is the pruned pass of
+//           the inverse transforms), one radix-2 pass when a is odd, then
+//           radix-4 passes;
+//   plan 1: radix-3 passes first, radix-4 passes, the radix-2 pass last;
+//   plan 2: the radix-2 pass first, radix-4 passes, radix-3 passes last
+//           (no pruned first pass).
+// Sets npass, radix[] and the per-pass constants.  False if M has another
+// factor, the plan is unknown or needs more than kMaxPasses passes.
+constexpr int kNumPlans = 3;
+inline bool factor_plan(int M, Dims* d, int plan = 0) {
     int m = M, a = 0, b = 0;
     while (m % 2 == 0) { m /= 2; ++a; }
     while (m % 3 == 0) { m /= 3; ++b; }
-    if (m != 1 || M % kElemsPerThread != 0) return false;
+    if (m != 1 || M % kElemsPerThread != 0 || plan < 0 || plan >= kNumPlans) return false;
     const int np = b + (a % 2) + a / 2;
     if (np > kMaxPasses) return false;
     int p = 0;
-    for (int i = 0; i < b; ++i) d->radix[p++] = 3;
-    if (a % 2) d->radix[p++] = 2;
-    for (int i = 0; i < a / 2; ++i) d->radix[p++] = 4;
+    auto put = [&](int r, int n) {
+        for (int i = 0; i < n; ++i) d->radix[p++] = r;
+    };
+    if (plan == 0) {
+        put(3, b);
+        put(2, a % 2);
+        put(4, a / 2);
+    } else if (plan == 1) {
+        put(3, b);
+        put(4, a / 2);
+        put(2, a % 2);
+    } else {
+        put(2, a % 2);
+        put(4, a / 2);
+        put(3, b);
+    }
     d->npass = np;
     set_pass_constants(d);
     return true;

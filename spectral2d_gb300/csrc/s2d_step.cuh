@@ -9,6 +9,7 @@
 
 #include "s2d_fft.cuh"
 #include "s2d_internal.h"
+#include "s2d_xpass32.cuh"
 
 namespace s2d {
 

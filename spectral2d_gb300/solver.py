@@ -245,6 +245,25 @@ class Spectral2D:
         L.check(self._L.s2d_time_steps(self._h, n, dt, C.byref(ms), None))
         return ms.value
 
+    @property
+    def fft_plan(self) -> int:
+        """Radix order of the FFTs (0, 1 or 2; see s2d_set_fft_plan)."""
+        p = C.c_int32()
+        L.check(self._L.s2d_get_fft_plan(self._h, C.byref(p)))
+        return p.value
+
+    @fft_plan.setter
+    def fft_plan(self, plan: int) -> None:
+        L.check(self._L.s2d_set_fft_plan(self._h, int(plan)))
+
+    def tune_fft_plan(self, dt: float):
+        """Time every radix plan on this run's step, keep the fastest (state
+        restored); returns (plan, ms per step of each plan)."""
+        p = C.c_int32()
+        ms = np.zeros(L.S2D_FFT_PLANS)
+        L.check(self._L.s2d_tune_fft_plan(self._h, dt, C.byref(p), _dptr(ms)))
+        return p.value, ms
+
     def kernels_per_step(self) -> int:
         return L.check(self._L.s2d_kernels_per_step(self._h))
 
@@ -420,6 +439,21 @@ class ClosureNet:
         loss = C.c_double()
         L.check(self._L.s2d_cnn_grad_host(self._c, _fptr(x), _fptr(t), x.shape[0], _fptr(g), C.byref(loss)))
         return loss.value, g
+
+    def keep_layer_grads(self, keep: bool = True) -> None:
+        """Keep dL/dz of every hidden layer in the following gradient calls."""
+        L.check(self._L.s2d_cnn_keep_layer_grads(self._c, int(bool(keep))))
+
+    _TENSOR_CH = {0: (16, 32, 32, 32, 32, 32), 1: (32,) * 5, 2: (32, 32, 32, 32, 32, 16)}
+
+    def tensor(self, kind: int, layer: int, batch: int) -> np.ndarray:
+        """A BF16 tensor of the last forward / gradient call as float32
+        (batch, grid, grid, padded channels): kind 0 = the layer's input,
+        1 = its pre-activation, 2 = dL/dz of its output."""
+        ch = self._TENSOR_CH[kind][layer]
+        out = np.zeros((batch, self.grid, self.grid, ch), dtype=np.float32)
+        L.check(self._L.s2d_cnn_get_tensor(self._c, kind, layer, batch, _fptr(out)))
+        return out
 
     def reserve(self, capacity: int) -> None:
         L.check(self._L.s2d_cnn_dataset_reserve(self._c, capacity))

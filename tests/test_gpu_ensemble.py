@@ -74,13 +74,16 @@ def test_tuner_keeps_state_and_results(mods):
         before = [r.get_state()[0] for r in ens.runs]
         threads, cps, ms = ens.tune()
         assert threads in (128, 256, 512) and cps >= 1 and ms > 0
+        plans = [r.fft_plan for r in ens.runs]
+        assert all(0 <= p < 3 for p in plans)
         after = [r.get_state()[0] for r in ens.runs]
         for a, b in zip(before, after):
             assert np.array_equal(a, b)
         ens.integrate_steps(5)
         wb = [r.get_state()[0] for r in ens.runs]
     for i, n in enumerate(nxs):
-        with Spectral2D(n, nu=nus[i]) as s:
+        with Spectral2D(n, nu=nus[i]) as s:   # the single run on the plan the tuner chose
+            s.fft_plan = plans[i]
             s.set_state(before[i])
             s.integrate_steps(5, dts[i])
             assert O.rel_l2(wb[i], s.get_state()[0]) <= 1e-15

@@ -437,3 +437,77 @@ def test_programmatic_launches_give_the_plain_order_bits(S2D, monkeypatch, preci
             s.check_finite()
             out[mode] = s.get_state()[0]
     assert np.array_equal(out["0"], out["1"])
+
+
+@pytest.mark.parametrize("n", [64, 96, 256])
+@pytest.mark.parametrize("plan", [0, 1, 2])
+def test_every_radix_plan_vs_oracle(S2D, n, plan):
+    """Each radix order of the FFTs (s2d_set_fft_plan) gives the oracle's RHS
+    and step to round-off; the plans differ in rounding only."""
+    g = O.get_grid_size(n, n)
+    w = O.random_state(g, 500 + n, decay=0.05)
+    nu, dt = 0.005, 1e-3
+    with S2D(n, nu=nu) as s:
+        s.fft_plan = plan
+        assert s.fft_plan == plan
+        s.set_state(w)
+        dW = s.compute_rhs()
+        s.integrate_steps(2, dt)
+        wg, _ = s.get_state()
+    wo, po = _oracle_state(w, g)
+    ref, _ = O.compute_rhs(wo, po, g, nu, round_trip=False)
+    assert O.rel_l2(dW, O.truncate(ref, g)) < 1e-13
+    for _ in range(2):
+        wo, po = O.integrate_one_step(wo, po, g, nu, dt, round_trip=False)
+    assert O.rel_l2(wg, wo) < 1e-12
+
+
+def test_fft_plan_tuner_keeps_the_state(S2D):
+    n, nu, dt = 256, 1e-3, 1e-3
+    g = O.get_grid_size(n, n)
+    w = O.truncate(O.random_state(g, 77, decay=0.05), g)
+    with S2D(n, nu=nu) as s:
+        s.set_state(w)
+        plan, ms = s.tune_fft_plan(dt)
+        assert 0 <= plan < 3 and s.fft_plan == plan and np.all(ms > 0)
+        print(f"N={n}: ms per step by plan {ms}, chosen {plan}")
+        w_after, _ = s.get_state()
+        assert np.array_equal(w_after, w)
+
+
+def test_fp32_xpass_2048_register_radix_vs_generic_and_oracle(S2D, monkeypatch):
+    """FP32 at 2048^2 runs its x-pass with register radix-12/16 passes
+    (k_xpass32); the generic engine (S2D_XPASS_GENERIC=1) computes the same
+    RHS up to FP32 round-off, and both stay within the FP32 error of the FP64
+    oracle; an FP32 2048^2 run in a batch equals the single run bit for bit."""
+    from spectral2d_gb300 import Ensemble
+    n, nu, dt = 2048, 1e-4, 2e-4
+    g = O.get_grid_size(n, n)
+    w = O.truncate(O.random_state(g, 2048, decay=0.02), g)
+    out = {}
+    for mode in ("register", "generic"):
+        if mode == "generic":
+            monkeypatch.setenv("S2D_XPASS_GENERIC", "1")
+        with S2D(n, nu=nu, precision="fp32") as s:
+            s.set_state(w)
+            out[mode] = s.compute_rhs()
+            if mode == "register":
+                s.integrate_steps(2, dt)
+                out["steps"] = s.get_state()[0]
+        monkeypatch.delenv("S2D_XPASS_GENERIC", raising=False)
+    wo, po = _oracle_state(w, g)
+    ref = O.truncate(O.compute_rhs(wo, po, g, nu, round_trip=False)[0], g)
+    e_reg, e_gen = O.rel_l2(out["register"], ref), O.rel_l2(out["generic"], ref)
+    print(f"FP32 2048^2 RHS vs FP64 oracle: register radix {e_reg:.2e}, generic {e_gen:.2e}, "
+          f"between them {O.rel_l2(out['register'], out['generic']):.2e}")
+    # the FP32 RHS error grows with N (the k^2 weights of the derivative
+    # terms): 8.2e-5 for both x-passes at 2048^2 on GB300
+    assert e_reg < 2e-4 and e_gen < 2e-4
+    assert e_reg < 1.25 * e_gen
+    with Ensemble([n], [nu], precision="fp32") as ens:
+        ens.runs[0].set_state(w)
+        ens.set_dt([dt])
+        ens.integrate_steps(2)
+        ens.status()
+        wb = ens.runs[0].get_state()[0]
+    assert np.array_equal(wb, out["steps"])
