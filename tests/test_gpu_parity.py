@@ -511,3 +511,23 @@ def test_fp32_xpass_2048_register_radix_vs_generic_and_oracle(S2D, monkeypatch):
         ens.status()
         wb = ens.runs[0].get_state()[0]
     assert np.array_equal(wb, out["steps"])
+
+
+@pytest.mark.parametrize("n,precision", [(512, "fp64"), (2048, "fp64"), (2048, "fp32")])
+def test_host_array_step_at_workload_sizes_equals_device_step(S2D, n, precision):
+    """The host-array step on the caller's page-locked arrays (read and
+    written in place by the conversion kernels) at the workload sizes, FP64
+    and FP32 (the register radix x-pass): the device-resident step's bits."""
+    from spectral2d_gb300.solver import pinned_array
+    g = O.get_grid_size(n, n)
+    w = O.truncate(O.random_state(g, 9, decay=0.02), g)
+    with S2D(n, nu=1e-4, precision=precision) as s:
+        s.set_state(w)
+        s.integrate_one_step(1e-4)
+        w_ref, p_ref = s.get_state()
+    with S2D(n, nu=1e-4, precision=precision) as s:
+        wh, ph = pinned_array(w.shape), pinned_array(w.shape)
+        wh[...] = w
+        ph[...] = np.nan
+        s.integrate_one_step_host(wh, 1e-4, ph, inplace=True)
+    assert np.array_equal(wh, w_ref) and np.array_equal(ph, p_ref)
