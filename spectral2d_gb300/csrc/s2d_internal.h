@@ -25,7 +25,7 @@ constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
 // the FP32 x-pass with register radix-12/16 passes (s2d_xpass32.cuh): row
 // length and its padded shared-memory buffer (elements)
 constexpr int kX32M = 3072;
-constexpr int kX32Buf = kX32M + kX32M / 32;
+constexpr int kX32Buf = kX32M + kX32M / 16;
 
 // Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
 // w_r = i^q_r * c_r * (1 + i t_r) with |t_r| <= 1, so that x*w_r costs two

@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_xpass_ba
 // CTA, three CTAs per SM (the radix-16 passes hold 16 complex values per
 // thread; inlined into k_xpass_bas at its four-per-SM budget of 64 registers
 // they spilled).
-__global__ void __launch_bounds__(256, 3) k_xpass32(Dims d, float2* Iu, float2* Iv, const float2* __restrict__ tw) {
+__global__ void __launch_bounds__(256, 4) k_xpass32(Dims d, float2* Iu, float2* Iv, const float2* __restrict__ tw) {
     __shared__ float2 sb[kX32Buf];
     pdl_enter();
     xpass32_m3072_row(d, Iu, Iv, tw, blockIdx.x, (int)blockIdx.x < d.rows, threadIdx.x, sb);

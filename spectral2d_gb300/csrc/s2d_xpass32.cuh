@@ -23,10 +23,8 @@
 //     one small exchange of the upper registers provides.
 //
 // Per element and row that is about 10 shared-memory accesses against
-// about 29 for the generic engine.  The buffer index is padded by one
-// element per 32 (i + i/32), which keeps every access pattern of the passes
-// within 1.1x of the conflict-free wavefront count (counted on the host for
-// all eleven patterns).  Twiddles between passes come from the handle's
+// about 29 for the generic engine, each exchange with a buffer index free
+// of bank conflicts (x32_i1, x32_i2).  Twiddles between passes come from the handle's
 // complex table tw[e] = exp(-2 pi i e / M) (conjugated for the inverse).
 #pragma once
 
@@ -34,7 +32,15 @@
 
 namespace s2d {
 
-__device__ __forceinline__ int x32_pad(int i) { return i + (i >> 5); }
+// Buffer index of element i in each of the five exchanges of a row, chosen
+// so that both the stores and the loads of that exchange are free of bank
+// conflicts in the half-warp phases of 8-byte accesses (counted on the host
+// for every access pattern; one padding per 32 elements for all five left
+// the stores 1.7x over the conflict-free wavefront count, as ncu showed):
+//   X1 inverse 1 -> 2, X2 inverse 2 -> 3, X3 forward 1 -> 2,
+//   X4 forward 2 -> 3, X5 the split's partners.
+__device__ __forceinline__ int x32_i1(int i) { return i ^ ((i >> 4) & 3); }
+__device__ __forceinline__ int x32_i2(int i) { return i + (i >> 4); }
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 __device__ __forceinline__ float2 f2add(float2 a, float2 b) { return f2(a.x + b.x, a.y + b.y); }
@@ -178,14 +184,14 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
     }
     x32_dft12<+1>(x);
 #pragma unroll
-    for (int q = 0; q < 12; ++q) sb[x32_pad(12 * t + q)] = x[3 * (q % 4) + q / 4];
+    for (int q = 0; q < 12; ++q) sb[x32_i1(12 * t + q)] = x[3 * (q % 4) + q / 4];
     __syncthreads();
     // ---- inverse pass 2: radix 16, Ns = 12 (threads < 192)
     const bool r16 = t < 192;
     const int k12 = t % 12;
     if (r16) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) x[r] = sb[x32_pad(t + 192 * r)];
+        for (int r = 0; r < 16; ++r) x[r] = sb[x32_i1(t + 192 * r)];
 #pragma unroll
         for (int r = 1; r < 16; ++r) x[r] = f2tw<+1>(x[r], __ldg(&tw[16 * r * k12]));
         x32_dft16<+1>(x);
@@ -193,14 +199,14 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
     __syncthreads();
     if (r16) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) sb[x32_pad((t - k12) * 16 + k12 + 12 * q)] = x[4 * (q % 4) + q / 4];
+        for (int q = 0; q < 16; ++q) sb[x32_i2((t - k12) * 16 + k12 + 12 * q)] = x[4 * (q % 4) + q / 4];
     }
     __syncthreads();
     // ---- inverse pass 3: radix 16, Ns = 192 -> z[t + 192 q]; products;
     //      forward pass 1: radix 16, Ns = 1 on p[t + 192 r] in registers
     if (r16) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) x[r] = sb[x32_pad(t + 192 * r)];
+        for (int r = 0; r < 16; ++r) x[r] = sb[x32_i2(t + 192 * r)];
 #pragma unroll
         for (int r = 1; r < 16; ++r) x[r] = f2tw<+1>(x[r], __ldg(&tw[r * t]));
         x32_dft16<+1>(x);   // z[t + 192 q] in slot 4 (q % 4) + q / 4
@@ -214,14 +220,14 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
     __syncthreads();
     if (r16) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) sb[x32_pad(16 * t + q)] = x[q];
+        for (int q = 0; q < 16; ++q) sb[x32_i2(16 * t + q)] = x[q];
     }
     __syncthreads();
     // ---- forward pass 2: radix 16, Ns = 16
     const int k16 = t % 16;
     if (r16) {
 #pragma unroll
-        for (int r = 0; r < 16; ++r) x[r] = sb[x32_pad(t + 192 * r)];
+        for (int r = 0; r < 16; ++r) x[r] = sb[x32_i2(t + 192 * r)];
 #pragma unroll
         for (int r = 1; r < 16; ++r) x[r] = f2tw<-1>(x[r], __ldg(&tw[12 * r * k16]));
         x32_dft16<-1>(x);
@@ -229,12 +235,12 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
     __syncthreads();
     if (r16) {
 #pragma unroll
-        for (int q = 0; q < 16; ++q) sb[x32_pad((t - k16) * 16 + k16 + 16 * q)] = x[4 * (q % 4) + q / 4];
+        for (int q = 0; q < 16; ++q) sb[x32_i2((t - k16) * 16 + k16 + 16 * q)] = x[4 * (q % 4) + q / 4];
     }
     __syncthreads();
     // ---- forward pass 3: radix 12, Ns = 256 -> P[t + 256 q]
 #pragma unroll
-    for (int r = 0; r < 12; ++r) x[r] = sb[x32_pad(t + 256 * r)];
+    for (int r = 0; r < 12; ++r) x[r] = sb[x32_i2(t + 256 * r)];
 #pragma unroll
     for (int r = 1; r < 12; ++r) x[r] = f2tw<-1>(x[r], __ldg(&tw[r * t]));
     x32_dft12<-1>(x);
@@ -242,7 +248,7 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
     // P[2048 .. 3071] (q = 8..11) through shared memory for the partners
     // P[M - k] of the outputs k in [1, K]
 #pragma unroll
-    for (int q = 8; q < 12; ++q) sb[x32_pad(t + 256 * q)] = x[3 * (q % 4) + q / 4];
+    for (int q = 8; q < 12; ++q) sb[t + 256 * q] = x[3 * (q % 4) + q / 4];
     __syncthreads();
     if (active) {
 #pragma unroll
@@ -250,7 +256,7 @@ __device__ __forceinline__ void xpass32_m3072_row(const Dims& d, float2* Iu, flo
             const int k = t + 256 * r;
             if (k <= K) {
                 const float2 p = x[3 * (r % 4) + r / 4];
-                const float2 q = k == 0 ? p : sb[x32_pad(M - k)];
+                const float2 q = k == 0 ? p : sb[M - k];
                 urow[k] = f2(p.x + q.x, p.y - q.y);
                 vrow[k] = f2(p.y + q.y, q.x - p.x);
             }
