@@ -320,6 +320,12 @@ S2D_API int s2d_cnn_set_band(s2d_cnn* c, double k_min);
 S2D_API int s2d_cnn_get_band(const s2d_cnn* c, double* k_min);
 /* x: batch x grid x grid x 2 (w, psi); y: batch x grid x grid (Pi) */
 S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t batch, float* y);
+/* Forward passes without a gradient (s2d_cnn_forward_host, s2d_cnn_eval, the
+ * LES closure term): on != 0 (the default) runs all six layers in one
+ * persistent cooperative launch with the activations in two images carrying
+ * a circular one-pixel frame; 0 runs one launch per layer, the kernels of the
+ * gradient path.  Both give the same bits. */
+S2D_API int s2d_cnn_set_fused(s2d_cnn* c, int32_t on);
 /* MSE loss of the normalised output against target/rms_Pi and its gradient
  * (same layout as the parameters) */
 S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, int32_t batch, float* grads,

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -492,6 +493,353 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
                     bias, zprev, z, a, yout, B, H, Wd, err);
 }
 
+// ---- the fused inference forward -----------------------------------------
+// All six layers of the network in one persistent launch, for the forward
+// passes that keep no pre-activations (the LES closure term, inference).
+//
+// Images carry a one-pixel circular frame: [B][H + 2][Wd + 2][KC], pixel
+// (y, x) at (y + 1, x + 1), frame row 0 = image row H - 1, frame row H + 1 =
+// image row 0, likewise the columns and the corners.  A layer's epilogue
+// writes each border pixel into the frame as well (up to four copies), so
+// the next layer's TMA boxes read the circular neighbourhood as it is, with
+// no fix-up pass.  Activations ping-pong between two framed images; between
+// layers the CTAs meet at a grid barrier (the launch is cooperative, so all
+// of them are resident; two CTAs of 288 threads and 110 KB per SM).
+//
+// Per CTA a three-stage pipeline over its 128-pixel tiles (8 x 16, as in
+// k_conv_tc): warp 8 issues the TMA loads of the halo boxes (three slots, the
+// next two tiles in flight) and the 9 * KC / 16 MMAs of a tile into one of
+// two tensor-memory accumulators; warps 0-7 read an accumulator, release it
+// (mbarrier), apply bias and GELU and store, while the MMAs of the next tile
+// run.  Every wait is bounded: a wait that runs out sets bit 4 of *err and
+// the abort flag, the CTA skips the rest (after bounded waits for its copies
+// and MMAs in flight) and frees its tensor memory.
+constexpr int kNetEpiWarps = 8;
+constexpr int kNetThreads = 32 * (kNetEpiWarps + 1);
+constexpr int kNetSlots = 3;
+constexpr int kNetSlotBytes = ConvTile<32, 32>::SLOT;
+constexpr int kNetWBytes = ConvTile<32, 32>::WBYTES;
+constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
+
+struct NetArgs {
+    const __nv_bfloat16* W[kLayers];   // BF16 working weights W[n][t][k]
+    const float* bias[kLayers];
+    __nv_bfloat16* act[2];             // framed 32-channel images
+    float* y;                          // output channel 0, [B][H][Wd]
+    unsigned int* bar;                 // grid barrier: arrivals of this launch
+    unsigned int* err;
+    int B, H, Wd;
+};
+
+struct NetShared {
+    uint64_t full[kNetSlots];   // the boxes of a slot have landed
+    uint64_t mmad[2];           // the MMAs into an accumulator are complete
+    uint64_t accfree[2];        // every epilogue warp has read an accumulator
+    uint32_t tmem;
+    int abort;
+    float bias[32];
+};
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+// Bounded wait that also gives up once another role of the CTA has aborted.
+__device__ __forceinline__ bool net_wait(uint32_t bar, uint32_t parity, const volatile int* abort) {
+    for (int it = 0; it < kMbarSpinLimit; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 255) == 255 && *abort) return false;
+    }
+    return false;
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+    return t;
+}
+
+// Grid barrier of one thread per CTA (the CTA synchronised before and
+// after): *bar counts the arrivals of the launch (zeroed before it), the
+// j-th barrier opens at j * gridDim.x.  Bounded: false after a second.
+__device__ __forceinline__ bool net_grid_sync(unsigned int* bar, unsigned int target) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    const unsigned long long t0 = globaltimer_ns();
+    while (ld_acquire_u32(bar) < target) {
+        if (globaltimer_ns() - t0 > 1000000000ull) return false;
+        __nanosleep(64);
+    }
+    return true;
+}
+
+// One layer over this CTA's tiles (tile blockIdx.x + k gridDim.x); irun is
+// the CTA's running tile count over all layers, which fixes every slot,
+// accumulator and barrier phase.
+template <int KC, int NC, bool LAST>
+__device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfloat16* __restrict__ W,
+                                          const float* __restrict__ bias, __nv_bfloat16* out, float* yout,
+                                          const NetArgs& a, NetShared& sh, unsigned char* gbase, uint32_t sbase,
+                                          int& irun) {
+    using TL = ConvTile<KC, NC>;
+    constexpr int KG = TL::KG;
+    constexpr int ROWB = TL::ROWB;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int H = a.H, Wd = a.Wd;
+    const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
+    const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
+    const int ntiles = tiles_img * a.B;
+    const int nk = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+    const uint32_t bw = sbase + kNetSlots * kNetSlotBytes;
+    volatile int* abort = &sh.abort;
+
+    // the layer's weights (the previous layer's MMAs are all complete) and bias
+    for (int i = tid; i < 9 * NC * KG; i += blockDim.x) {
+        const int nl = i % 8;
+        const int kg = (i / 8) % KG;
+        const int n = ((i / (8 * KG)) % (NC / 8)) * 8 + nl;
+        const int t = i / (KG * NC);
+        const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
+        const int off = ((t * (NC / 8) + n / 8) * KG + kg) * TL::CORE + (n % 8) * 16;
+        *reinterpret_cast<uint4*>(gbase + kNetSlots * kNetSlotBytes + off) = v;
+    }
+    if (tid < NC) sh.bias[tid] = bias[tid];
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    auto tile_xy = [&](int k, int& b, int& tx0, int& ty0) {
+        const int tile = (int)blockIdx.x + k * (int)gridDim.x;
+        b = tile / tiles_img;
+        const int tl = tile - b * tiles_img;
+        tx0 = (tl % tiles_x) * kConvTX;
+        ty0 = (tl / tiles_x) * kConvTY;
+    };
+    const int i0 = irun;
+
+    if (warp == kNetEpiWarps) {
+        // ---- control: TMA producer and MMA issuer (one thread)
+        if (lane == 0 && !*abort) {
+            auto load = [&](int k) {
+                const int i = i0 + k, s = i % kNetSlots;
+                int b, tx0, ty0;
+                tile_xy(k, b, tx0, ty0);
+                const uint32_t bar = smem_u32(&sh.full[s]);
+                mbar_expect_tx(bar, (uint32_t)TL::SLOT);
+#pragma unroll
+                for (int d = 0; d < 3; ++d)
+                    tma_load_4d(sbase + s * kNetSlotBytes + d * TL::BOX, tin, 0, tx0 + d, ty0, b, bar);
+            };
+            // what is in flight, for the abort path: loads of tiles [i0 + kw, i0 + kl), MMAs of tile i0 + km
+            int kl = 0, kw = 0, km = -1;
+            asm volatile("fence.proxy.async.global;\n" ::: "memory");
+            for (; kl < nk && kl < kNetSlots; ++kl) load(kl);
+            bool ok = true;
+            for (int k = 0; k < nk && ok; ++k) {
+                const int i = i0 + k, s = i % kNetSlots, acc = i & 1;
+                ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort);
+                if (!ok) break;
+                kw = k + 1;
+                if (i >= 2) ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)((i - 2) >> 1) & 1u, abort);
+                if (!ok) break;
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
+                const uint32_t a0 = sbase + s * kNetSlotBytes;
+                const uint32_t dacc = sh.tmem + (uint32_t)(acc * 32);
+#pragma unroll 1
+                for (int t = 0; t < 9; ++t) {
+                    const int dy = t / 3 - 1, dx = t % 3 - 1;
+                    const uint32_t abase = a0 + (dx + 1) * TL::BOX + (1 + dy) * kConvTX * ROWB;
+                    const uint32_t bbase = bw + t * (NC / 8) * TL::WGROUP;
+#pragma unroll
+                    for (int j = 0; j < KC / 16; ++j) {
+                        const uint64_t ad = umma_desc_sw<ROWB>(abase + j * 32);
+                        const uint64_t bd = umma_desc(bbase + j * 2 * TL::CORE, TL::CORE, TL::WGROUP);
+                        const uint32_t accum = (t | j) ? 1u : 0u;
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                            : "memory");
+                    }
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                        smem_u32(&sh.mmad[acc]))
+                    : "memory");
+                km = k;
+                // refill the slot of the previous tile, whose MMAs have had
+                // this tile's issue time to finish
+                if (k >= 1 && kl < nk) {
+                    const int ip = i - 1;
+                    ok = net_wait(smem_u32(&sh.mmad[ip & 1]), (uint32_t)(ip >> 1) & 1u, abort);
+                    if (!ok) break;
+                    load(kl++);
+                }
+            }
+            if (!ok) {
+                *abort = 1;
+                atomicOr(a.err, 4u);
+                for (int k = kw; k < kl; ++k) {
+                    const int i = i0 + k;
+                    mbar_wait_bounded(smem_u32(&sh.full[i % kNetSlots]), (uint32_t)(i / kNetSlots) & 1u);
+                }
+                if (km >= 0) {
+                    const int i = i0 + km;
+                    mbar_wait_bounded(smem_u32(&sh.mmad[i & 1]), (uint32_t)(i >> 1) & 1u);
+                }
+            }
+        }
+    } else {
+        // ---- epilogue warps: warp w reads accumulator lanes 32 (w % 4) .. + 31
+        // (tile pixels m at (m / 16, m % 16)) and columns 16 (w / 4) .. + 15
+        const int quarter = warp & 3, half = warp >> 2;
+        const bool cols = half * 16 < NC;   // warp-uniform
+        const long fw = Wd + 2;
+        for (int k = 0; k < nk; ++k) {
+            const int i = i0 + k, acc = i & 1;
+            if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i >> 1) & 1u, abort)) {
+                *abort = 1;
+                atomicOr(a.err, 4u);
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            uint32_t r[16];
+            if (cols) {
+                const uint32_t taddr = sh.tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * 32 + half * 16);
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                    "%15}, [%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                      "=r"(r[14]), "=r"(r[15])
+                    : "r"(taddr));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            }
+            asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(smem_u32(&sh.accfree[acc]));
+
+            int b, tx0, ty0;
+            tile_xy(k, b, tx0, ty0);
+            const int m = quarter * 32 + lane;
+            const int y = ty0 + m / kConvTX, x = tx0 + m % kConvTX;
+            if (!cols || y >= H || x >= Wd) continue;
+            if (LAST) {
+                if (half == 0) yout[((long)b * H + y) * Wd + x] = __uint_as_float(r[0]) + sh.bias[0];
+            } else {
+                uint32_t v[8];
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int n = half * 16 + 2 * e;
+                    v[e] = pack_bf16(gelu_f(__uint_as_float(r[2 * e]) + sh.bias[n]),
+                                     gelu_f(__uint_as_float(r[2 * e + 1]) + sh.bias[n + 1]));
+                }
+                const uint4 lo = make_uint4(v[0], v[1], v[2], v[3]), hi = make_uint4(v[4], v[5], v[6], v[7]);
+                // the pixel and its copies in the frame
+                const long img = (long)b * (H + 2) * fw;
+                const int wy = y == 0 ? H + 1 : (y == H - 1 ? 0 : -1);
+                const int wx = x == 0 ? Wd + 1 : (x == Wd - 1 ? 0 : -1);
+                auto put = [&](int fy, int fx) {
+                    uint4* p = reinterpret_cast<uint4*>(out + (img + fy * fw + fx) * 32 + half * 16);
+                    p[0] = lo;
+                    p[1] = hi;
+                };
+                put(y + 1, x + 1);
+                if (wy >= 0) put(wy, x + 1);
+                if (wx >= 0) put(y + 1, wx);
+                if (wy >= 0 && wx >= 0) put(wy, wx);
+            }
+        }
+        // this layer's stores are read by the next layer's TMA (async proxy)
+        asm volatile("fence.proxy.async.global;\n" ::: "memory");
+    }
+    irun = i0 + nk;
+}
+
+__global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
+                                                          const __grid_constant__ CUtensorMap m_a0,
+                                                          const __grid_constant__ CUtensorMap m_a1, NetArgs a) {
+    extern __shared__ __align__(1024) unsigned char net_smem[];
+    __shared__ NetShared sh;
+    const uint32_t sraw = smem_u32(net_smem);
+    const uint32_t sbase = (sraw + 1023u) & ~1023u;
+    unsigned char* gbase = net_smem + (sbase - sraw);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    if (warp == kNetEpiWarps) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&sh.tmem)),
+                     "r"(64)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    if (tid == 0) {
+        for (int s = 0; s < kNetSlots; ++s)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
+        for (int s = 0; s < 2; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&sh.accfree[s])),
+                         "r"(kNetEpiWarps)
+                         : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        sh.abort = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    int irun = 0, nbar = 0;
+    auto barrier = [&]() {
+        __syncthreads();
+        ++nbar;
+        if (tid == 0 && !sh.abort && !net_grid_sync(a.bar, (unsigned int)nbar * gridDim.x)) {
+            sh.abort = 1;
+            atomicOr(a.err, 4u);
+        }
+        __syncthreads();
+    };
+    net_layer<16, 32, false>(&m_in, a.W[0], a.bias[0], a.act[0], nullptr, a, sh, gbase, sbase, irun);
+    barrier();
+    net_layer<32, 32, false>(&m_a0, a.W[1], a.bias[1], a.act[1], nullptr, a, sh, gbase, sbase, irun);
+    barrier();
+    net_layer<32, 32, false>(&m_a1, a.W[2], a.bias[2], a.act[0], nullptr, a, sh, gbase, sbase, irun);
+    barrier();
+    net_layer<32, 32, false>(&m_a0, a.W[3], a.bias[3], a.act[1], nullptr, a, sh, gbase, sbase, irun);
+    barrier();
+    net_layer<32, 32, false>(&m_a1, a.W[4], a.bias[4], a.act[0], nullptr, a, sh, gbase, sbase, irun);
+    barrier();
+    net_layer<32, 16, true>(&m_a0, a.W[5], a.bias[5], nullptr, a.y, a, sh, gbase, sbase, irun);
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == kNetEpiWarps)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(sh.tmem), "r"(64) : "memory");
+}
+
+// Framed copy of B images [B][H][Wd][16] (the layer-1 input written
+// unframed): one thread per framed pixel and 16-byte half.
+__global__ void k_frame16(const __nv_bfloat16* __restrict__ x, int B, int H, int Wd, __nv_bfloat16* xf) {
+    const long fw = Wd + 2, fh = H + 2;
+    const long n = (long)B * fh * fw * 2;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int q = (int)(i & 1);
+        long p = i >> 1;
+        const int fx = (int)(p % fw);
+        p /= fw;
+        const int fy = (int)(p % fh);
+        const long b = p / fh;
+        const int yy = fy == 0 ? H - 1 : (fy == H + 1 ? 0 : fy - 1);
+        const int xx = fx == 0 ? Wd - 1 : (fx == Wd + 1 ? 0 : fx - 1);
+        reinterpret_cast<uint4*>(xf)[i] =
+            reinterpret_cast<const uint4*>(x)[((b * H + yy) * Wd + xx) * 2 + q];
+    }
+}
+
 // Weight and bias gradient of one layer on the FP32 pipes:
 //   dW[co, t, ci] = sum_p dz[p, co] in[p + off_t, ci],   db[co] = sum_p dz[p, co].
 // A CTA walks image rows, staging dz of the row and in of rows y-1, y, y+1 in
@@ -820,11 +1168,14 @@ __global__ void __launch_bounds__(512) k_cl_yinv(Dims d, const LesRun<T>* __rest
 // rms w of the run from the nparts sums of k_cl_yinv (their total, the mean
 // of w^2, is kept in part[nparts] for k_cl_xfwd).  Only channels 0 and 1 of
 // x are written: channels 2..15 of the input buffer are zero from its
-// allocation on, and every writer of it keeps them so.
+// allocation on, and every writer of it keeps them so.  framed: x holds
+// images with the one-pixel circular frame of the fused forward ([M + 2]^2
+// pixels, pixel (y, n) at (y + 1, n + 1)), the border pixels written into the
+// frame as well.
 template <typename T>
 __global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __restrict__ runs,
                                                   const typename Vec<T>::t* __restrict__ tw, int G, int nparts,
-                                                  float r0, float r1, __nv_bfloat16* x) {
+                                                  float r0, float r1, __nv_bfloat16* x, int framed) {
     using VT = typename Vec<T>::t;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double s_ia;
@@ -847,11 +1198,27 @@ __global__ void __launch_bounds__(512) k_cl_xinv(Dims d, const LesRun<T>* __rest
     build_pair(Z, R.I0 + (size_t)yy * d.ldI, R.I1 + (size_t)yy * d.ldI, d, lane, active);
     fft_run<true>(Z, d, lane, tw);   // begins with a barrier: s_ia is visible after it
     const T a0 = (T)((double)r0 * s_ia), a1 = (T)((double)r1 * s_ia);
-    if (active) {
+    if (active && !framed) {
         uint32_t* xr = reinterpret_cast<uint32_t*>(x + ((size_t)blockIdx.y * d.M + y) * (size_t)d.M * 16);
         for (int n = lane; n < d.M; n += d.Tg) {
             const VT z = Z[n];
             xr[(size_t)n * 8] = pack_bf16((float)(z.x * a0), (float)(z.y * a1));
+        }
+    } else if (active) {
+        const size_t fw = (size_t)d.M + 2;
+        const int wy = y == 0 ? d.M + 1 : (y == d.M - 1 ? 0 : -1);
+        uint32_t* xr = reinterpret_cast<uint32_t*>(x + ((size_t)blockIdx.y * fw + y + 1) * fw * 16);
+        uint32_t* xw = reinterpret_cast<uint32_t*>(x + ((size_t)blockIdx.y * fw + (wy < 0 ? 0 : wy)) * fw * 16);
+        for (int n = lane; n < d.M; n += d.Tg) {
+            const VT z = Z[n];
+            const uint32_t v = pack_bf16((float)(z.x * a0), (float)(z.y * a1));
+            const int wx = n == 0 ? d.M + 1 : (n == d.M - 1 ? 0 : -1);
+            xr[(size_t)(n + 1) * 8] = v;
+            if (wx >= 0) xr[(size_t)wx * 8] = v;
+            if (wy >= 0) {
+                xw[(size_t)(n + 1) * 8] = v;
+                if (wx >= 0) xw[(size_t)wx * 8] = v;
+            }
         }
     }
 }
@@ -979,6 +1346,13 @@ struct s2d_cnn {
     double scale[3] = {1.0, 1.0, 1.0};
     double k_min = 0.0;         // the closure term is applied only where |k| >= k_min
     long step = 0;
+    // the fused inference forward (k_net_fwd): framed layer-1 input and the
+    // two framed activation images, the grid barrier's arrival count
+    bool fused = true;
+    int net_grid = 0;           // resident CTAs of k_net_fwd (cooperative launch)
+    __nv_bfloat16* X0f = nullptr;
+    __nv_bfloat16* F[2] = {};
+    unsigned int* netbar = nullptr;
 };
 
 namespace {
@@ -1003,9 +1377,80 @@ int refresh_all(s2d_cnn* c) {
     return S2D_OK;
 }
 
+int ensure_net_buffers(s2d_cnn* c) {
+    if (c->netbar) return S2D_OK;
+    const size_t fp = (size_t)c->maxB * (c->H + 2) * (c->Wd + 2);
+    C_CUDA(cudaFuncSetAttribute(k_net_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem));
+    int occ = 0;
+    C_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fwd, kNetThreads, kNetSmem));
+    if (occ < 1) return cerr(S2D_ERR_UNSUPPORTED, "the fused network kernel does not fit on an SM");
+    c->net_grid = occ * c->sms;
+    bool ok = cudaMalloc(&c->X0f, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMemset(c->X0f, 0, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->F[0], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->F[1], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&c->netbar, 64) == cudaSuccess;
+    if (!ok) {
+        cudaFree(c->X0f);
+        cudaFree(c->F[0]);
+        cudaFree(c->F[1]);
+        cudaFree(c->netbar);
+        c->X0f = c->F[0] = c->F[1] = nullptr;
+        c->netbar = nullptr;
+        return cerr(S2D_ERR_NOMEM, "cudaMalloc failed (fused network buffers)");
+    }
+    return S2D_OK;
+}
+
+// Inference forward of B images in one launch (k_net_fwd); the layer-1 input
+// is in X0f already framed (k_cl_xinv writes it so) or framed here from X0.
+int forward_fused(s2d_cnn* c, int B, bool input_framed) {
+    int r = ensure_net_buffers(c);
+    if (r != S2D_OK) return r;
+    const int H = c->H, Wd = c->Wd;
+    if (!input_framed) {
+        k_frame16<<<nblocks((long)B * (H + 2) * (Wd + 2) * 2, 256), 256, 0, c->stream>>>(c->X0, B, H, Wd, c->X0f);
+        C_CUDA(cudaGetLastError());
+    }
+    CUtensorMap m_in, m_a0, m_a1;
+    C_CUDA(conv_tensor_map<16>(&m_in, c->X0f, B, H + 2, Wd + 2));
+    C_CUDA(conv_tensor_map<32>(&m_a0, c->F[0], B, H + 2, Wd + 2));
+    C_CUDA(conv_tensor_map<32>(&m_a1, c->F[1], B, H + 2, Wd + 2));
+    NetArgs a{};
+    for (int l = 0; l < kLayers; ++l) {
+        a.W[l] = c->Wb[l];
+        a.bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
+    }
+    a.act[0] = c->F[0];
+    a.act[1] = c->F[1];
+    a.y = c->Y;
+    a.bar = c->netbar;
+    a.err = c->cflags;
+    a.B = B;
+    a.H = H;
+    a.Wd = Wd;
+    const long ntiles = (long)((Wd + kConvTX - 1) / kConvTX) * ((H + kConvTY - 1) / kConvTY) * B;
+    const int grid = (int)std::min<long>(ntiles, c->net_grid);
+    C_CUDA(cudaMemsetAsync(c->netbar, 0, sizeof(unsigned int), c->stream));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(kNetThreads);
+    cfg.dynamicSmemBytes = kNetSmem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    C_CUDA(cudaLaunchKernelEx(&cfg, k_net_fwd, m_in, m_a0, m_a1, a));
+    return S2D_OK;
+}
+
 // forward of the batch in X0 (B images); the pre-activations z are kept only
-// when a backward pass follows
+// when a backward pass follows.  Without them the fused kernel runs (unless
+// switched off by s2d_cnn_set_fused).
 int forward(s2d_cnn* c, int B, bool keep_z, bool pdl = false) {
+    if (!keep_z && c->fused) return forward_fused(c, B, false);
     const float* bias[kLayers];
     for (int l = 0; l < kLayers; ++l) bias[l] = c->master + c->poff[l] + (long)kCoutP[l] * 9 * kCinP[l];
     C_CUDA((launch_conv<16, 32, 1, 0>(c->X0, c->Wb[0], bias[0], nullptr, keep_z ? c->Z[0] : nullptr, c->A[0],
@@ -1222,12 +1667,14 @@ int closure_terms_t(s2d_cnn* c, s2d_handle* const* runs, int n, const void* tab,
     const VT* tw = (const VT*)h0->tw;
     const bool pdl = Ly.pdl;
     C_CUDA(launch_k(k_cl_yinv<T>, dim3(2 * nparts, n), Ly.threads, Ly.smem, st, pdl, d, R, h0->rk2, tw, Ly.G));
+    const bool fused = c->fused;
     C_CUDA(launch_k(k_cl_xinv<T>, dim3((d.M + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st, pdl, d, R, tw, Lx.G,
-                    nparts, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]), c->X0));
+                    nparts, (float)(1.0 / c->scale[0]), (float)(1.0 / c->scale[1]), fused ? c->X0f : c->X0,
+                    (int)fused));
     // the network runs on the caller's stream: borrow it for the forward pass
     cudaStream_t saved = c->stream;
     c->stream = st;
-    const int r = forward(c, n, false, pdl);
+    const int r = fused ? forward_fused(c, n, true) : forward(c, n, false, pdl);
     c->stream = saved;
     if (r != S2D_OK) return r;
     C_CUDA(launch_k(k_cl_xfwd<T>, dim3((d.M / 2 + Lx.G - 1) / Lx.G, n), Lx.threads, Lx.smem, st, pdl, d, R,
@@ -1328,6 +1775,9 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
     c->device = device;
     c->H = c->Wd = grid;
     c->maxB = max_batch;
+    // S2D_CNN_LAYERWISE=1: gradient-free forward passes one launch per layer
+    // (for comparisons; s2d_cnn_set_fused switches it per network)
+    if (const char* e = std::getenv("S2D_CNN_LAYERWISE")) c->fused = e[0] == '\0' || e[0] == '0';
     auto bail = [&](int code) {
         s2d_cnn_destroy(c);
         return code;
@@ -1386,6 +1836,8 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
         ok = cudaMalloc(&c->Z[l], P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
              cudaMalloc(&c->A[l], P * 32 * sizeof(__nv_bfloat16)) == cudaSuccess;
     if (!ok) return bail(cerr(S2D_ERR_NOMEM, "cudaMalloc failed"));
+    // allocated here, not at first use: the first use may be inside a graph capture
+    if (ensure_net_buffers(c) != S2D_OK) return bail(S2D_ERR_NOMEM);
     {
         const int smax = 3 * grid * 32 * 2 + grid * 32 * 2;
         cudaFuncSetAttribute(k_conv_wgrad<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
@@ -1420,7 +1872,7 @@ S2D_API void s2d_cnn_destroy(s2d_cnn* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* ptrs[] = {c->master, c->grad, c->m, c->v, c->X0, c->dZ6, c->dZa, c->dZb, c->Y, c->tgt, c->part,
-                    c->lpart, c->idx, c->data, c->amp, c->sumsq, c->cflags};
+                    c->lpart, c->idx, c->data, c->amp, c->sumsq, c->cflags, c->X0f, c->F[0], c->F[1], c->netbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int l = 0; l < kLayers; ++l) {
@@ -1669,6 +2121,12 @@ S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_
     }
     if (mean_loss) *mean_loss = tot / nb;
     return s2d_cnn_status(c);
+}
+
+S2D_API int s2d_cnn_set_fused(s2d_cnn* c, int32_t on) {
+    if (!c) return cerr(S2D_ERR_INVALID, "null network");
+    c->fused = on != 0;
+    return S2D_OK;
 }
 
 S2D_API int s2d_cnn_status(s2d_cnn* c) {

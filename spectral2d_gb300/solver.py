@@ -440,6 +440,11 @@ class ClosureNet:
         L.check(self._L.s2d_cnn_grad_host(self._c, _fptr(x), _fptr(t), x.shape[0], _fptr(g), C.byref(loss)))
         return loss.value, g
 
+    def set_fused(self, on: bool = True) -> None:
+        """Gradient-free forward passes in one fused launch (default) or one
+        launch per layer; the results are the same bits."""
+        L.check(self._L.s2d_cnn_set_fused(self._c, int(bool(on))))
+
     def keep_layer_grads(self, keep: bool = True) -> None:
         """Keep dL/dz of every hidden layer in the following gradient calls."""
         L.check(self._L.s2d_cnn_keep_layer_grads(self._c, int(bool(keep))))

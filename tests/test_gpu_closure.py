@@ -142,6 +142,30 @@ def test_cnn_forward_edge_tiles_vs_oracle(S, grid, B):
         assert _rel(gp[l][0], go[l][0]) < 5e-2 and _rel(gp[l][1], go[l][1]) < 5e-2
 
 
+@pytest.mark.parametrize("grid, B", [(8, 3), (20, 2), (40, 1), (192, 1), (192, 9)])
+def test_fused_forward_equals_the_layerwise_forward(S, grid, B):
+    """The fused inference forward (all six layers in one persistent launch,
+    activations in framed images, grid barriers between layers) against one
+    launch per layer: the same MMAs in the same order and the same epilogue,
+    so the same bits -- at ragged and doubly wrapped tiles (8, 20, 40) and at
+    the 128^2 LES grid (192^2 pixels), one image (one tile per CTA) and nine
+    (several tiles per CTA, every slot and accumulator phase reused across
+    layers)."""
+    rng = np.random.default_rng(100 + grid + B)
+    with S.ClosureNet(grid, max_batch=B, seed=11) as net:
+        net.set_scales([1.0, 1.0, 1.0])
+        x = rng.standard_normal((B, grid, grid, 2)).astype(np.float32)
+        net.set_fused(True)
+        yf = net.forward(x)
+        yf2 = net.forward(x)
+        net.set_fused(False)
+        yl = net.forward(x)
+        net.status()
+    assert np.all(np.isfinite(yf))
+    assert np.array_equal(yf, yf2)
+    assert np.array_equal(yf, yl), _rel(yf, yl)
+
+
 def test_subgrid_flux_vs_oracle(S):
     nd, nl, nu = 64, 16, 2e-3
     gd, gl = O.get_grid_size(nd, nd), O.get_grid_size(nl, nl)
@@ -275,6 +299,42 @@ def test_batched_closure_les_matches_single_runs(S, precision):
                 wa, _ = a.get_state()
                 S.les_set_closure(a, None)
             assert np.array_equal(wa, wb[i]), O.rel_l2(wb[i], wa)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_les_closure_fused_network_matches_layerwise(S, precision):
+    """The LES step's closure term with the fused network (the layer-1 input
+    written framed by the transform kernel) against the per-layer launches:
+    the same state bits after the same steps, single run and batch."""
+    n, nu, steps = 128, 1e-3, 6
+    with S.ClosureNet(192, max_batch=2, seed=13) as net:
+        net.set_scales([1.0, 1.0, 0.05])
+        w0 = [O.random_state(O.get_grid_size(n, n), 40 + i, decay=0.2) for i in range(2)]
+        dt = 2e-3
+        out = {}
+        for fused in (True, False):
+            net.set_fused(fused)
+            with S.Spectral2D(n, nu=nu, precision=precision) as a:
+                a.set_state(w0[0])
+                S.les_set_closure(a, net)
+                S.les_integrate_steps(a, steps, dt)
+                out[("single", fused)] = a.get_state()[0]
+                S.les_set_closure(a, None)
+            with S.Ensemble([n] * 2, [nu] * 2, precision=precision) as ens:
+                for i in range(2):
+                    ens.runs[i].set_state(w0[i])
+                ens.set_dt([dt] * 2)
+                ens.set_closure(net)
+                ens.integrate_steps(steps)
+                ens.status()
+                out[("batch", fused)] = [r.get_state()[0] for r in ens.runs]
+                ens.set_closure(None)
+        net.status()
+    assert np.all(np.isfinite(out[("single", True)]))
+    assert np.array_equal(out[("single", True)], out[("single", False)])
+    for i in range(2):
+        assert np.array_equal(out[("batch", True)][i], out[("batch", False)][i])
+    assert np.array_equal(out[("single", True)], out[("batch", True)][0])
 
 
 def test_trained_closure_beats_the_closure_free_les(S):
