@@ -504,18 +504,22 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
 // the next layer's TMA boxes read the circular neighbourhood as it is, with
 // no fix-up pass.  Activations ping-pong between two framed images; between
 // layers the CTAs meet at a grid barrier (the launch is cooperative, so all
-// of them are resident; two CTAs of 288 threads and 110 KB per SM).
+// of them are resident; two CTAs of 320 threads and 110 KB per SM).
 //
-// Per CTA a three-stage pipeline over its 128-pixel tiles (8 x 16, as in
-// k_conv_tc): warp 8 issues the TMA loads of the halo boxes (three slots, the
-// next two tiles in flight) and the 9 * KC / 16 MMAs of a tile into one of
-// two tensor-memory accumulators; warps 0-7 read an accumulator, release it
-// (mbarrier), apply bias and GELU and store, while the MMAs of the next tile
-// run.  Every wait is bounded: a wait that runs out sets bit 4 of *err and
+// Per CTA a pipeline over its 128-pixel tiles (8 x 16, as in k_conv_tc):
+// warp 9 issues the TMA loads of the halo boxes into three slots, warp 8 the
+// 9 * KC / 16 MMAs of a tile into one of two tensor-memory accumulators
+// (descriptors precomputed per slot: a tap is an offset of the start
+// address), and warps 0-7 read an accumulator, release it (mbarrier), apply
+// bias and GELU and store while the MMAs of the next tile run.  The roles
+// meet only at mbarriers: full (slot landed), slotfree (its MMAs done),
+// mmad (accumulator ready), accfree (accumulator read).  Every wait is bounded: a wait that runs out sets bit 4 of *err and
 // the abort flag, the CTA skips the rest (after bounded waits for its copies
 // and MMAs in flight) and frees its tensor memory.
-constexpr int kNetEpiWarps = 8;
-constexpr int kNetThreads = 32 * (kNetEpiWarps + 1);
+constexpr int kNetEpiWarps = 8;                  // warps 0-7
+constexpr int kNetMmaWarp = kNetEpiWarps;        // warp 8
+constexpr int kNetProdWarp = kNetEpiWarps + 1;   // warp 9
+constexpr int kNetThreads = 32 * (kNetEpiWarps + 2);
 constexpr int kNetSlots = 3;
 constexpr int kNetSlotBytes = ConvTile<32, 32>::SLOT;
 constexpr int kNetWBytes = ConvTile<32, 32>::WBYTES;
@@ -533,6 +537,7 @@ struct NetArgs {
 
 struct NetShared {
     uint64_t full[kNetSlots];   // the boxes of a slot have landed
+    uint64_t slotfree[kNetSlots];   // the MMAs that read a slot are complete
     uint64_t mmad[2];           // the MMAs into an accumulator are complete
     uint64_t accfree[2];        // every epilogue warp has read an accumulator
     uint32_t tmem;
@@ -622,50 +627,71 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         ty0 = (tl / tiles_x) * kConvTY;
     };
     const int i0 = irun;
+    auto fail = [&]() {
+        *abort = 1;
+        atomicOr(a.err, 4u);
+    };
 
-    if (warp == kNetEpiWarps) {
-        // ---- control: TMA producer and MMA issuer (one thread)
+    if (warp == kNetProdWarp) {
+        // ---- TMA producer (one thread): the three halo boxes of each tile
+        // into slot i % kNetSlots once the MMAs of tile i - kNetSlots have
+        // read it
         if (lane == 0 && !*abort) {
-            auto load = [&](int k) {
-                const int i = i0 + k, s = i % kNetSlots;
+            asm volatile("fence.proxy.async.global;\n" ::: "memory");
+            int kl = 0;
+            bool ok = true;
+            for (; kl < nk; ++kl) {
+                const int i = i0 + kl, s = i % kNetSlots;
+                if (i >= kNetSlots &&
+                    !(ok = net_wait(smem_u32(&sh.slotfree[s]), (uint32_t)(i / kNetSlots - 1) & 1u, abort)))
+                    break;
                 int b, tx0, ty0;
-                tile_xy(k, b, tx0, ty0);
+                tile_xy(kl, b, tx0, ty0);
                 const uint32_t bar = smem_u32(&sh.full[s]);
                 mbar_expect_tx(bar, (uint32_t)TL::SLOT);
 #pragma unroll
                 for (int d = 0; d < 3; ++d)
                     tma_load_4d(sbase + s * kNetSlotBytes + d * TL::BOX, tin, 0, tx0 + d, ty0, b, bar);
-            };
-            // what is in flight, for the abort path: loads of tiles [i0 + kw, i0 + kl), MMAs of tile i0 + km
-            int kl = 0, kw = 0, km = -1;
-            asm volatile("fence.proxy.async.global;\n" ::: "memory");
-            for (; kl < nk && kl < kNetSlots; ++kl) load(kl);
+            }
+            if (!ok) {
+                fail();
+                // the loads that may still be in flight land before the memory goes
+                for (int k = kl - kNetSlots < 0 ? 0 : kl - kNetSlots; k < kl; ++k) {
+                    const int i = i0 + k;
+                    mbar_wait_bounded(smem_u32(&sh.full[i % kNetSlots]), (uint32_t)(i / kNetSlots) & 1u);
+                }
+            }
+        }
+    } else if (warp == kNetMmaWarp) {
+        // ---- MMA issuer (one thread): 9 * KC / 16 MMAs per tile into
+        // accumulator i & 1, committed to mmad (epilogue) and slotfree (producer)
+        if (lane == 0 && !*abort) {
+            const uint64_t bd0 = umma_desc(bw, TL::CORE, TL::WGROUP);
+            constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
+            int km = -1;
             bool ok = true;
-            for (int k = 0; k < nk && ok; ++k) {
+            for (int k = 0; k < nk; ++k) {
                 const int i = i0 + k, s = i % kNetSlots, acc = i & 1;
-                ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort);
-                if (!ok) break;
-                kw = k + 1;
-                if (i >= 2) ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)((i - 2) >> 1) & 1u, abort);
-                if (!ok) break;
+                if (!(ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort))) break;
+                if (i >= 2 && !(ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)((i - 2) >> 1) & 1u, abort)))
+                    break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
-                const uint32_t a0 = sbase + s * kNetSlotBytes;
+                const uint64_t ad0 = umma_desc_sw<ROWB>(sbase + s * kNetSlotBytes);
                 const uint32_t dacc = sh.tmem + (uint32_t)(acc * 32);
-#pragma unroll 1
+#pragma unroll
                 for (int t = 0; t < 9; ++t) {
                     const int dy = t / 3 - 1, dx = t % 3 - 1;
-                    const uint32_t abase = a0 + (dx + 1) * TL::BOX + (1 + dy) * kConvTX * ROWB;
-                    const uint32_t bbase = bw + t * (NC / 8) * TL::WGROUP;
 #pragma unroll
                     for (int j = 0; j < KC / 16; ++j) {
-                        const uint64_t ad = umma_desc_sw<ROWB>(abase + j * 32);
-                        const uint64_t bd = umma_desc(bbase + j * 2 * TL::CORE, TL::CORE, TL::WGROUP);
-                        const uint32_t accum = (t | j) ? 1u : 0u;
+                        // start addresses advance in 16-byte units in the low field
+                        const uint64_t ad =
+                            ad0 + (uint64_t)(((dx + 1) * TL::BOX + (1 + dy) * kConvTX * ROWB + j * 32) >> 4);
+                        const uint64_t bd =
+                            bd0 + (uint64_t)((t * (NC / 8) * TL::WGROUP + j * 2 * TL::CORE) >> 4);
                         asm volatile(
                             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
-                            "l"(ad), "l"(bd), "r"(idesc), "r"(accum)
+                            "l"(ad), "l"(bd), "r"(idesc), "r"((t | j) ? 1u : 0u)
                             : "memory");
                     }
                 }
@@ -673,23 +699,14 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                         smem_u32(&sh.mmad[acc]))
                     : "memory");
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                        smem_u32(&sh.slotfree[s]))
+                    : "memory");
                 km = k;
-                // refill the slot of the previous tile, whose MMAs have had
-                // this tile's issue time to finish
-                if (k >= 1 && kl < nk) {
-                    const int ip = i - 1;
-                    ok = net_wait(smem_u32(&sh.mmad[ip & 1]), (uint32_t)(ip >> 1) & 1u, abort);
-                    if (!ok) break;
-                    load(kl++);
-                }
             }
             if (!ok) {
-                *abort = 1;
-                atomicOr(a.err, 4u);
-                for (int k = kw; k < kl; ++k) {
-                    const int i = i0 + k;
-                    mbar_wait_bounded(smem_u32(&sh.full[i % kNetSlots]), (uint32_t)(i / kNetSlots) & 1u);
-                }
+                fail();
                 if (km >= 0) {
                     const int i = i0 + km;
                     mbar_wait_bounded(smem_u32(&sh.mmad[i & 1]), (uint32_t)(i >> 1) & 1u);
@@ -705,8 +722,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         for (int k = 0; k < nk; ++k) {
             const int i = i0 + k, acc = i & 1;
             if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i >> 1) & 1u, abort)) {
-                *abort = 1;
-                atomicOr(a.err, 4u);
+                fail();
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -772,15 +788,17 @@ __global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constan
     const uint32_t sbase = (sraw + 1023u) & ~1023u;
     unsigned char* gbase = net_smem + (sbase - sraw);
     const int tid = threadIdx.x, warp = tid >> 5;
-    if (warp == kNetEpiWarps) {
+    if (warp == kNetMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&sh.tmem)),
                      "r"(64)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
     if (tid == 0) {
-        for (int s = 0; s < kNetSlots; ++s)
+        for (int s = 0; s < kNetSlots; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.slotfree[s])) : "memory");
+        }
         for (int s = 0; s < 2; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&sh.accfree[s])),
@@ -817,7 +835,7 @@ __global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constan
     net_layer<32, 16, true>(&m_a0, a.W[5], a.bias[5], nullptr, a.y, a, sh, gbase, sbase, irun);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
-    if (warp == kNetEpiWarps)
+    if (warp == kNetMmaWarp)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(sh.tmem), "r"(64) : "memory");
 }
 
@@ -1381,6 +1399,8 @@ int ensure_net_buffers(s2d_cnn* c) {
     if (c->netbar) return S2D_OK;
     const size_t fp = (size_t)c->maxB * (c->H + 2) * (c->Wd + 2);
     C_CUDA(cudaFuncSetAttribute(k_net_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem));
+    // the largest carveout, so that two CTAs share an SM
+    C_CUDA(cudaFuncSetAttribute(k_net_fwd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int occ = 0;
     C_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fwd, kNetThreads, kNetSmem));
     if (occ < 1) return cerr(S2D_ERR_UNSUPPORTED, "the fused network kernel does not fit on an SM");
