@@ -504,23 +504,27 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
 // the next layer's TMA boxes read the circular neighbourhood as it is, with
 // no fix-up pass.  Activations ping-pong between two framed images; between
 // layers the CTAs meet at a grid barrier (the launch is cooperative, so all
-// of them are resident; two CTAs of 320 threads and 110 KB per SM).
+// of them are resident).
 //
-// Per CTA a pipeline over its 128-pixel tiles (8 x 16, as in k_conv_tc):
-// warp 9 issues the TMA loads of the halo boxes into three slots, warp 8 the
-// 9 * KC / 16 MMAs of a tile into one of two tensor-memory accumulators
-// (descriptors precomputed per slot: a tap is an offset of the start
-// address), and warps 0-7 read an accumulator, release it (mbarrier), apply
-// bias and GELU and store while the MMAs of the next tile run.  The roles
+// One CTA per SM (the cooperative limit), a pipeline over its 128-pixel
+// tiles (8 x 16, as in k_conv_tc): warp 17 issues the TMA loads of the halo
+// boxes into six slots, warp 16 the 9 * KC / 16 MMAs of a tile into one of
+// four tensor-memory accumulators (descriptors precomputed per slot: a tap
+// is an offset of the start address), and two groups of eight warps take
+// alternate tiles: read the accumulator, release it (mbarrier), apply bias
+// and GELU and store, while the MMAs of the following tiles run.  The roles
 // meet only at mbarriers: full (slot landed), slotfree (its MMAs done),
 // mmad (accumulator ready), accfree (accumulator read).  Every wait is bounded: a wait that runs out sets bit 4 of *err and
 // the abort flag, the CTA skips the rest (after bounded waits for its copies
 // and MMAs in flight) and frees its tensor memory.
-constexpr int kNetEpiWarps = 8;                  // warps 0-7
-constexpr int kNetMmaWarp = kNetEpiWarps;        // warp 8
-constexpr int kNetProdWarp = kNetEpiWarps + 1;   // warp 9
+constexpr int kNetGroups = 2;                    // epilogue groups of 8 warps
+constexpr int kNetAcc = 4;                       // accumulators (tile i: i % 4, group i % 2)
+constexpr int kNetEpiWarps = 8 * kNetGroups;     // warps 0-15
+constexpr int kNetMmaWarp = kNetEpiWarps;        // warp 16
+constexpr int kNetProdWarp = kNetEpiWarps + 1;   // warp 17
 constexpr int kNetThreads = 32 * (kNetEpiWarps + 2);
-constexpr int kNetSlots = 3;
+constexpr int kNetTmemCols = 32 * kNetAcc;
+constexpr int kNetSlots = 6;
 constexpr int kNetSlotBytes = ConvTile<32, 32>::SLOT;
 constexpr int kNetWBytes = ConvTile<32, 32>::WBYTES;
 constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
@@ -538,8 +542,8 @@ struct NetArgs {
 struct NetShared {
     uint64_t full[kNetSlots];   // the boxes of a slot have landed
     uint64_t slotfree[kNetSlots];   // the MMAs that read a slot are complete
-    uint64_t mmad[2];           // the MMAs into an accumulator are complete
-    uint64_t accfree[2];        // every epilogue warp has read an accumulator
+    uint64_t mmad[kNetAcc];     // the MMAs into an accumulator are complete
+    uint64_t accfree[kNetAcc];  // the 8 warps of its epilogue group have read an accumulator
     uint32_t tmem;
     int abort;
     float bias[32];
@@ -664,16 +668,17 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         }
     } else if (warp == kNetMmaWarp) {
         // ---- MMA issuer (one thread): 9 * KC / 16 MMAs per tile into
-        // accumulator i & 1, committed to mmad (epilogue) and slotfree (producer)
+        // accumulator i % 4, committed to mmad (epilogue) and slotfree (producer)
         if (lane == 0 && !*abort) {
             const uint64_t bd0 = umma_desc(bw, TL::CORE, TL::WGROUP);
             constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
             int km = -1;
             bool ok = true;
             for (int k = 0; k < nk; ++k) {
-                const int i = i0 + k, s = i % kNetSlots, acc = i & 1;
+                const int i = i0 + k, s = i % kNetSlots, acc = i % kNetAcc;
                 if (!(ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort))) break;
-                if (i >= 2 && !(ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)((i - 2) >> 1) & 1u, abort)))
+                if (i >= kNetAcc &&
+                    !(ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)(i / kNetAcc - 1) & 1u, abort)))
                     break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint64_t ad0 = umma_desc_sw<ROWB>(sbase + s * kNetSlotBytes);
@@ -709,19 +714,20 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                 fail();
                 if (km >= 0) {
                     const int i = i0 + km;
-                    mbar_wait_bounded(smem_u32(&sh.mmad[i & 1]), (uint32_t)(i >> 1) & 1u);
+                    mbar_wait_bounded(smem_u32(&sh.mmad[i % kNetAcc]), (uint32_t)(i / kNetAcc) & 1u);
                 }
             }
         }
     } else {
-        // ---- epilogue warps: warp w reads accumulator lanes 32 (w % 4) .. + 31
-        // (tile pixels m at (m / 16, m % 16)) and columns 16 (w / 4) .. + 15
-        const int quarter = warp & 3, half = warp >> 2;
+        // ---- epilogue warps: group g = w / 8 takes the tiles with i % 2 == g;
+        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (tile pixels m at
+        // (m / 16, m % 16)) and columns 16 ((w % 8) / 4) .. + 15
+        const int grp = warp >> 3, quarter = warp & 3, half = (warp >> 2) & 1;
         const bool cols = half * 16 < NC;   // warp-uniform
         const long fw = Wd + 2;
-        for (int k = 0; k < nk; ++k) {
-            const int i = i0 + k, acc = i & 1;
-            if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i >> 1) & 1u, abort)) {
+        for (int k = (grp - (i0 & 1) + 2) & 1; k < nk; k += kNetGroups) {
+            const int i = i0 + k, acc = i % kNetAcc;
+            if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i / kNetAcc) & 1u, abort)) {
                 fail();
                 break;
             }
@@ -779,7 +785,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
     irun = i0 + nk;
 }
 
-__global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
+__global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
                                                           const __grid_constant__ CUtensorMap m_a0,
                                                           const __grid_constant__ CUtensorMap m_a1, NetArgs a) {
     extern __shared__ __align__(1024) unsigned char net_smem[];
@@ -790,7 +796,7 @@ __global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constan
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == kNetMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&sh.tmem)),
-                     "r"(64)
+                     "r"(kNetTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
@@ -799,10 +805,10 @@ __global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constan
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.slotfree[s])) : "memory");
         }
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < kNetAcc; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&sh.accfree[s])),
-                         "r"(kNetEpiWarps)
+                         "r"(kNetEpiWarps / kNetGroups)
                          : "memory");
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
@@ -836,7 +842,8 @@ __global__ void __launch_bounds__(kNetThreads, 2) k_net_fwd(const __grid_constan
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == kNetMmaWarp)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(sh.tmem), "r"(64) : "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(sh.tmem), "r"(kNetTmemCols)
+                     : "memory");
 }
 
 // Framed copy of B images [B][H][Wd][16] (the layer-1 input written
@@ -1399,12 +1406,15 @@ int ensure_net_buffers(s2d_cnn* c) {
     if (c->netbar) return S2D_OK;
     const size_t fp = (size_t)c->maxB * (c->H + 2) * (c->Wd + 2);
     C_CUDA(cudaFuncSetAttribute(k_net_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kNetSmem));
-    // the largest carveout, so that two CTAs share an SM
-    C_CUDA(cudaFuncSetAttribute(k_net_fwd, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
     int occ = 0;
     C_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_net_fwd, kNetThreads, kNetSmem));
     if (occ < 1) return cerr(S2D_ERR_UNSUPPORTED, "the fused network kernel does not fit on an SM");
+    occ = 1;   // one CTA per SM by design (its TMEM columns, the launch bound)
     c->net_grid = occ * c->sms;
+    if (const char* e = std::getenv("S2D_NET_CTAS")) {   // for measurements: fewer CTAs
+        const int v = std::atoi(e);
+        if (v >= 1 && v < c->net_grid) c->net_grid = v;
+    }
     bool ok = cudaMalloc(&c->X0f, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMemset(c->X0f, 0, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->F[0], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
