@@ -506,13 +506,20 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
 // layers the CTAs meet at a grid barrier (the launch is cooperative, so all
 // of them are resident).
 //
-// One CTA per SM (the cooperative limit), a pipeline over its 128-pixel
-// tiles (8 x 16, as in k_conv_tc): warp 17 issues the TMA loads of the halo
-// boxes into six slots, warp 16 the 9 * KC / 16 MMAs of a tile into one of
-// four tensor-memory accumulators (descriptors precomputed per slot: a tap
-// is an offset of the start address), and two groups of eight warps take
-// alternate tiles: read the accumulator, release it (mbarrier), apply bias
-// and GELU and store, while the MMAs of the following tiles run.  The roles
+// The three column taps dx of a row of taps dy go side by side into the
+// MMA's N dimension: for a box of 10 x 16 pixels (one TMA box, the tile's
+// 8 x 14 outputs and their halo) D[m, (dx, n)] = sum over dy and channels of
+// box pixel m + 16 (dy + 1) times W[n, (dy, dx), :], so a tile is 3 KC / 16
+// MMAs of N = 3 NC (not 9 KC / 16 of N = NC, each of which streams the same
+// 4 KB of activations from shared memory for only 32 columns), and output
+// pixel m takes column block dx at pixel m + dx - 1, a warp shuffle.
+// One CTA per SM (the cooperative limit): warp 17 issues the TMA loads of
+// the boxes into eight slots, warp 16 the MMAs of a tile into one of four
+// tensor-memory accumulators (descriptors precomputed per slot: a row of
+// taps is an offset of the start address), and two groups of eight warps
+// take alternate tiles: read the accumulator, release it (mbarrier), sum the
+// taps, apply bias and GELU and store, while the MMAs of the following tiles
+// run.  The roles
 // meet only at mbarriers: full (slot landed), slotfree (its MMAs done),
 // mmad (accumulator ready), accfree (accumulator read).  Every wait is bounded: a wait that runs out sets bit 4 of *err and
 // the abort flag, the CTA skips the rest (after bounded waits for its copies
@@ -523,10 +530,13 @@ constexpr int kNetEpiWarps = 8 * kNetGroups;     // warps 0-15
 constexpr int kNetMmaWarp = kNetEpiWarps;        // warp 16
 constexpr int kNetProdWarp = kNetEpiWarps + 1;   // warp 17
 constexpr int kNetThreads = 32 * (kNetEpiWarps + 2);
-constexpr int kNetTmemCols = 32 * kNetAcc;
-constexpr int kNetSlots = 6;
-constexpr int kNetSlotBytes = ConvTile<32, 32>::SLOT;
-constexpr int kNetWBytes = ConvTile<32, 32>::WBYTES;
+constexpr int kNetAccCols = 128;                 // 3 * 32 columns used
+constexpr int kNetTmemCols = kNetAccCols * kNetAcc;
+constexpr int kNetOutH = 8, kNetOutW = 14;       // output tile
+constexpr int kNetBoxRows = kNetOutH + 2, kNetBoxW = kNetOutW + 2;   // its halo box: M = 8 x 16 = 128 pixels
+constexpr int kNetSlots = 8;
+constexpr int kNetSlotBytes = kNetBoxRows * kNetBoxW * 64;   // one box of 32-channel pixels
+constexpr int kNetWBytes = 3 * 96 * 4 * 16;                  // B operands of the three rows of taps
 constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
 
 struct NetArgs {
@@ -595,26 +605,35 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                                           const float* __restrict__ bias, __nv_bfloat16* out, float* yout,
                                           const NetArgs& a, NetShared& sh, unsigned char* gbase, uint32_t sbase,
                                           int& irun) {
-    using TL = ConvTile<KC, NC>;
-    constexpr int KG = TL::KG;
-    constexpr int ROWB = TL::ROWB;
+    constexpr int KG = KC / 8;                 // 8-channel groups of a pixel
+    constexpr int ROWB = KC * 2;               // bytes of one pixel
+    constexpr int BOX = kNetBoxRows * kNetBoxW * ROWB;
+    constexpr int N = 3 * NC;                  // the MMA's columns: (dx, output channel)
+    constexpr int NG = N / 8;                  // 8-column groups
+    constexpr int CORE = 128;
+    constexpr int WGROUP = KG * CORE;          // 8 columns x all input channels
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int H = a.H, Wd = a.Wd;
-    const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
-    const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
+    const int tiles_x = (Wd + kNetOutW - 1) / kNetOutW;
+    const int tiles_img = tiles_x * ((H + kNetOutH - 1) / kNetOutH);
     const int ntiles = tiles_img * a.B;
     const int nk = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
     const uint32_t bw = sbase + kNetSlots * kNetSlotBytes;
     volatile int* abort = &sh.abort;
 
-    // the layer's weights (the previous layer's MMAs are all complete) and bias
-    for (int i = tid; i < 9 * NC * KG; i += blockDim.x) {
+    // the layer's weights as the B operands of the three rows of taps: for
+    // row dy, column group g = (dx, 8 output channels), the input channels
+    // K-major in core matrices (the previous layer's MMAs are all complete)
+    for (int i = tid; i < 3 * N * KG; i += blockDim.x) {
         const int nl = i % 8;
         const int kg = (i / 8) % KG;
-        const int n = ((i / (8 * KG)) % (NC / 8)) * 8 + nl;
-        const int t = i / (KG * NC);
+        const int g = (i / (8 * KG)) % NG;
+        const int dyi = i / (8 * KG * NG);
+        const int dxi = g / (NC / 8);
+        const int n = (g % (NC / 8)) * 8 + nl;
+        const int t = dyi * 3 + dxi;
         const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
-        const int off = ((t * (NC / 8) + n / 8) * KG + kg) * TL::CORE + (n % 8) * 16;
+        const int off = ((dyi * NG + g) * KG + kg) * CORE + nl * 16;
         *reinterpret_cast<uint4*>(gbase + kNetSlots * kNetSlotBytes + off) = v;
     }
     if (tid < NC) sh.bias[tid] = bias[tid];
@@ -623,12 +642,15 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
-    auto tile_xy = [&](int k, int& b, int& tx0, int& ty0) {
+    // tile k: output rows [oy0, oy0 + 8), columns [ox0, ox0 + 14); its box is
+    // image rows oy0 - 1 .. oy0 + 8 and columns ox0 - 1 .. ox0 + 14, at
+    // framed coordinates (ox0, oy0)
+    auto tile_xy = [&](int k, int& b, int& ox0, int& oy0) {
         const int tile = (int)blockIdx.x + k * (int)gridDim.x;
         b = tile / tiles_img;
         const int tl = tile - b * tiles_img;
-        tx0 = (tl % tiles_x) * kConvTX;
-        ty0 = (tl / tiles_x) * kConvTY;
+        ox0 = (tl % tiles_x) * kNetOutW;
+        oy0 = (tl / tiles_x) * kNetOutH;
     };
     const int i0 = irun;
     auto fail = [&]() {
@@ -637,9 +659,8 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
     };
 
     if (warp == kNetProdWarp) {
-        // ---- TMA producer (one thread): the three halo boxes of each tile
-        // into slot i % kNetSlots once the MMAs of tile i - kNetSlots have
-        // read it
+        // ---- TMA producer (one thread): one box per tile into slot
+        // i % kNetSlots once the MMAs of tile i - kNetSlots have read it
         if (lane == 0 && !*abort) {
             asm volatile("fence.proxy.async.global;\n" ::: "memory");
             int kl = 0;
@@ -649,13 +670,11 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                 if (i >= kNetSlots &&
                     !(ok = net_wait(smem_u32(&sh.slotfree[s]), (uint32_t)(i / kNetSlots - 1) & 1u, abort)))
                     break;
-                int b, tx0, ty0;
-                tile_xy(kl, b, tx0, ty0);
+                int b, ox0, oy0;
+                tile_xy(kl, b, ox0, oy0);
                 const uint32_t bar = smem_u32(&sh.full[s]);
-                mbar_expect_tx(bar, (uint32_t)TL::SLOT);
-#pragma unroll
-                for (int d = 0; d < 3; ++d)
-                    tma_load_4d(sbase + s * kNetSlotBytes + d * TL::BOX, tin, 0, tx0 + d, ty0, b, bar);
+                mbar_expect_tx(bar, (uint32_t)BOX);
+                tma_load_4d(sbase + s * kNetSlotBytes, tin, 0, ox0, oy0, b, bar);
             }
             if (!ok) {
                 fail();
@@ -667,11 +686,13 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
             }
         }
     } else if (warp == kNetMmaWarp) {
-        // ---- MMA issuer (one thread): 9 * KC / 16 MMAs per tile into
-        // accumulator i % 4, committed to mmad (epilogue) and slotfree (producer)
+        // ---- MMA issuer (one thread): per tile 3 * KC / 16 MMAs of
+        // M = 128 box pixels, N = 3 NC (the three column taps side by side),
+        // K = 16 channels, one per row of taps dy and channel step, into
+        // accumulator i % 4; committed to mmad (epilogue) and slotfree
         if (lane == 0 && !*abort) {
-            const uint64_t bd0 = umma_desc(bw, TL::CORE, TL::WGROUP);
-            constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
+            const uint64_t bd0 = umma_desc(bw, CORE, WGROUP);
+            constexpr uint32_t idesc = umma_idesc_bf16(128, N);
             int km = -1;
             bool ok = true;
             for (int k = 0; k < nk; ++k) {
@@ -682,21 +703,19 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                     break;
                 asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
                 const uint64_t ad0 = umma_desc_sw<ROWB>(sbase + s * kNetSlotBytes);
-                const uint32_t dacc = sh.tmem + (uint32_t)(acc * 32);
+                const uint32_t dacc = sh.tmem + (uint32_t)(acc * kNetAccCols);
 #pragma unroll
-                for (int t = 0; t < 9; ++t) {
-                    const int dy = t / 3 - 1, dx = t % 3 - 1;
+                for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
                     for (int j = 0; j < KC / 16; ++j) {
-                        // start addresses advance in 16-byte units in the low field
-                        const uint64_t ad =
-                            ad0 + (uint64_t)(((dx + 1) * TL::BOX + (1 + dy) * kConvTX * ROWB + j * 32) >> 4);
-                        const uint64_t bd =
-                            bd0 + (uint64_t)((t * (NC / 8) * TL::WGROUP + j * 2 * TL::CORE) >> 4);
+                        // box rows dyi .. dyi + 7 (whole 8-pixel atoms); start
+                        // addresses advance in 16-byte units in the low field
+                        const uint64_t ad = ad0 + (uint64_t)((dyi * kNetBoxW * ROWB + j * 32) >> 4);
+                        const uint64_t bd = bd0 + (uint64_t)((dyi * NG * WGROUP + j * 2 * CORE) >> 4);
                         asm volatile(
                             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                             " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
-                            "l"(ad), "l"(bd), "r"(idesc), "r"((t | j) ? 1u : 0u)
+                            "l"(ad), "l"(bd), "r"(idesc), "r"((dyi | j) ? 1u : 0u)
                             : "memory");
                     }
                 }
@@ -720,8 +739,11 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         }
     } else {
         // ---- epilogue warps: group g = w / 8 takes the tiles with i % 2 == g;
-        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (tile pixels m at
-        // (m / 16, m % 16)) and columns 16 ((w % 8) / 4) .. + 15
+        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (box pixels m: row
+        // m / 16, column m % 16) and, of each tap column dx, the output
+        // channels 16 ((w % 8) / 4) .. + 15.  Output pixel m sums tap dx
+        // evaluated at box pixel m + dx: a shuffle within the 16 lanes of its
+        // row; box columns 1 .. 14 are the tile's outputs.
         const int grp = warp >> 3, quarter = warp & 3, half = (warp >> 2) & 1;
         const bool cols = half * 16 < NC;   // warp-uniform
         const long fw = Wd + 2;
@@ -732,36 +754,49 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            uint32_t r[16];
+            uint32_t r[3][16];
             if (cols) {
-                const uint32_t taddr = sh.tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(acc * 32 + half * 16);
-                asm volatile(
-                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
-                    "%15}, [%16];\n"
-                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                      "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                      "=r"(r[14]), "=r"(r[15])
-                    : "r"(taddr));
+#pragma unroll
+                for (int dxi = 0; dxi < 3; ++dxi) {
+                    const uint32_t taddr = sh.tmem + ((uint32_t)(quarter * 32) << 16) +
+                                           (uint32_t)(acc * kNetAccCols + dxi * NC + half * 16);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                        "%15}, [%16];\n"
+                        : "=r"(r[dxi][0]), "=r"(r[dxi][1]), "=r"(r[dxi][2]), "=r"(r[dxi][3]), "=r"(r[dxi][4]),
+                          "=r"(r[dxi][5]), "=r"(r[dxi][6]), "=r"(r[dxi][7]), "=r"(r[dxi][8]), "=r"(r[dxi][9]),
+                          "=r"(r[dxi][10]), "=r"(r[dxi][11]), "=r"(r[dxi][12]), "=r"(r[dxi][13]), "=r"(r[dxi][14]),
+                          "=r"(r[dxi][15])
+                        : "r"(taddr));
+                }
                 asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             __syncwarp();
             if (lane == 0) mbar_arrive(smem_u32(&sh.accfree[acc]));
+            if (!cols) continue;
 
-            int b, tx0, ty0;
-            tile_xy(k, b, tx0, ty0);
+            int b, ox0, oy0;
+            tile_xy(k, b, ox0, oy0);
             const int m = quarter * 32 + lane;
-            const int y = ty0 + m / kConvTX, x = tx0 + m % kConvTX;
-            if (!cols || y >= H || x >= Wd) continue;
+            const int c = m % kNetBoxW;
+            const int y = oy0 + m / kNetBoxW, x = ox0 - 1 + c;
+            const bool valid = c >= 1 && c <= kNetOutW && y < H && x < Wd;
+            float z[16];
+#pragma unroll
+            for (int e = 0; e < 16; ++e)
+                z[e] = __shfl_up_sync(0xffffffffu, __uint_as_float(r[0][e]), 1, kNetBoxW) +
+                       __uint_as_float(r[1][e]) +
+                       __shfl_down_sync(0xffffffffu, __uint_as_float(r[2][e]), 1, kNetBoxW);
+            if (!valid) continue;
             if (LAST) {
-                if (half == 0) yout[((long)b * H + y) * Wd + x] = __uint_as_float(r[0]) + sh.bias[0];
+                if (half == 0) yout[((long)b * H + y) * Wd + x] = z[0] + sh.bias[0];
             } else {
                 uint32_t v[8];
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int n = half * 16 + 2 * e;
-                    v[e] = pack_bf16(gelu_f(__uint_as_float(r[2 * e]) + sh.bias[n]),
-                                     gelu_f(__uint_as_float(r[2 * e + 1]) + sh.bias[n + 1]));
+                    v[e] = pack_bf16(gelu_f(z[2 * e] + sh.bias[n]), gelu_f(z[2 * e + 1] + sh.bias[n + 1]));
                 }
                 const uint4 lo = make_uint4(v[0], v[1], v[2], v[3]), hi = make_uint4(v[4], v[5], v[6], v[7]);
                 // the pixel and its copies in the frame
@@ -1459,7 +1494,7 @@ int forward_fused(s2d_cnn* c, int B, bool input_framed) {
     a.B = B;
     a.H = H;
     a.Wd = Wd;
-    const long ntiles = (long)((Wd + kConvTX - 1) / kConvTX) * ((H + kConvTY - 1) / kConvTY) * B;
+    const long ntiles = (long)((Wd + kNetOutW - 1) / kNetOutW) * ((H + kNetOutH - 1) / kNetOutH) * B;
     const int grid = (int)std::min<long>(ntiles, c->net_grid);
     C_CUDA(cudaMemsetAsync(c->netbar, 0, sizeof(unsigned int), c->stream));
     cudaLaunchConfig_t cfg = {};
