@@ -145,12 +145,14 @@ def test_cnn_forward_edge_tiles_vs_oracle(S, grid, B):
 @pytest.mark.parametrize("grid, B", [(8, 3), (20, 2), (40, 1), (192, 1), (192, 9)])
 def test_fused_forward_equals_the_layerwise_forward(S, grid, B):
     """The fused inference forward (all six layers in one persistent launch,
-    activations in framed images, grid barriers between layers) against one
-    launch per layer: the same MMAs in the same order and the same epilogue,
-    so the same bits -- at ragged and doubly wrapped tiles (8, 20, 40) and at
-    the 128^2 LES grid (192^2 pixels), one image (one tile per CTA) and nine
-    (several tiles per CTA, every slot and accumulator phase reused across
-    layers)."""
+    activations in framed images, grid barriers between layers, the three
+    column taps summed in the epilogue) against one launch per layer (all nine
+    taps summed in the tensor core): the same products in FP32 in another
+    order, so equal to FP32 rounding (and the rare BF16 rounding flip it
+    causes in an activation) -- at ragged and doubly wrapped tiles (8, 20,
+    40) and at the 128^2 LES grid (192^2 pixels), one image and nine (several
+    tiles per CTA, every slot and accumulator phase reused across layers).
+    Two fused calls give the same bits."""
     rng = np.random.default_rng(100 + grid + B)
     with S.ClosureNet(grid, max_batch=B, seed=11) as net:
         net.set_scales([1.0, 1.0, 1.0])
@@ -163,7 +165,9 @@ def test_fused_forward_equals_the_layerwise_forward(S, grid, B):
         net.status()
     assert np.all(np.isfinite(yf))
     assert np.array_equal(yf, yf2)
-    assert np.array_equal(yf, yl), _rel(yf, yl)
+    e = _rel(yf, yl)
+    print(f"grid {grid} batch {B}: fused vs per-layer rel-L2 {e:.1e}")
+    assert e < 1e-4
 
 
 def test_subgrid_flux_vs_oracle(S):
@@ -305,7 +309,8 @@ def test_batched_closure_les_matches_single_runs(S, precision):
 def test_les_closure_fused_network_matches_layerwise(S, precision):
     """The LES step's closure term with the fused network (the layer-1 input
     written framed by the transform kernel) against the per-layer launches:
-    the same state bits after the same steps, single run and batch."""
+    the same states to FP32 rounding of the network after the same steps,
+    single run and batch; the batch equals the single run bit for bit."""
     n, nu, steps = 128, 1e-3, 6
     with S.ClosureNet(192, max_batch=2, seed=13) as net:
         net.set_scales([1.0, 1.0, 0.05])
@@ -331,10 +336,13 @@ def test_les_closure_fused_network_matches_layerwise(S, precision):
                 ens.set_closure(None)
         net.status()
     assert np.all(np.isfinite(out[("single", True)]))
-    assert np.array_equal(out[("single", True)], out[("single", False)])
+    e = O.rel_l2(out[("single", True)], out[("single", False)])
+    print(f"{precision}: LES state fused vs per-layer network rel-L2 {e:.1e}")
+    assert e < 1e-6
     for i in range(2):
-        assert np.array_equal(out[("batch", True)][i], out[("batch", False)][i])
+        assert O.rel_l2(out[("batch", True)][i], out[("batch", False)][i]) < 1e-6
     assert np.array_equal(out[("single", True)], out[("batch", True)][0])
+    assert np.array_equal(out[("single", False)], out[("batch", False)][0])
 
 
 def test_trained_closure_beats_the_closure_free_les(S):
