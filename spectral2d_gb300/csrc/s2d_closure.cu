@@ -747,6 +747,11 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         const int grp = warp >> 3, quarter = warp & 3, half = (warp >> 2) & 1;
         const bool cols = half * 16 < NC;   // warp-uniform
         const long fw = Wd + 2;
+        // this thread's 16 biases in registers (shared-memory reads per tile
+        // would compete with the tensor core's operand reads)
+        float bv[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) bv[e] = cols ? sh.bias[half * 16 + e] : 0.0f;
         for (int k = (grp - (i0 & 1) + 2) & 1; k < nk; k += kNetGroups) {
             const int i = i0 + k, acc = i % kNetAcc;
             if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i / kNetAcc) & 1u, abort)) {
@@ -790,14 +795,11 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                        __shfl_down_sync(0xffffffffu, __uint_as_float(r[2][e]), 1, kNetBoxW);
             if (!valid) continue;
             if (LAST) {
-                if (half == 0) yout[((long)b * H + y) * Wd + x] = z[0] + sh.bias[0];
+                if (half == 0) yout[((long)b * H + y) * Wd + x] = z[0] + bv[0];
             } else {
                 uint32_t v[8];
 #pragma unroll
-                for (int e = 0; e < 8; ++e) {
-                    const int n = half * 16 + 2 * e;
-                    v[e] = pack_bf16(gelu_f(z[2 * e] + sh.bias[n]), gelu_f(z[2 * e + 1] + sh.bias[n + 1]));
-                }
+                for (int e = 0; e < 8; ++e) v[e] = pack_bf16(gelu_f(z[2 * e] + bv[2 * e]), gelu_f(z[2 * e + 1] + bv[2 * e + 1]));
                 const uint4 lo = make_uint4(v[0], v[1], v[2], v[3]), hi = make_uint4(v[4], v[5], v[6], v[7]);
                 // the pixel and its copies in the frame
                 const long img = (long)b * (H + 2) * fw;

@@ -166,8 +166,10 @@ def test_fused_forward_equals_the_layerwise_forward(S, grid, B):
     assert np.all(np.isfinite(yf))
     assert np.array_equal(yf, yf2)
     e = _rel(yf, yl)
-    print(f"grid {grid} batch {B}: fused vs per-layer rel-L2 {e:.1e}")
-    assert e < 1e-4
+    emax = float(np.max(np.abs(yf - yl)) / np.sqrt(np.mean(yl.astype(np.float64) ** 2)))
+    print(f"grid {grid} batch {B}: fused vs per-layer rel-L2 {e:.1e}, max/rms {emax:.1e}")
+    # a wrong tap or edge would be O(1) at the pixels it touches
+    assert e < 2e-3 and emax < 2e-2
 
 
 def test_subgrid_flux_vs_oracle(S):
