@@ -340,9 +340,10 @@ def test_les_closure_fused_network_matches_layerwise(S, precision):
     assert np.all(np.isfinite(out[("single", True)]))
     e = O.rel_l2(out[("single", True)], out[("single", False)])
     print(f"{precision}: LES state fused vs per-layer network rel-L2 {e:.1e}")
-    assert e < 1e-6
+    bar = 1e-6 if precision == "fp64" else 1e-5
+    assert e < bar
     for i in range(2):
-        assert O.rel_l2(out[("batch", True)][i], out[("batch", False)][i]) < 1e-6
+        assert O.rel_l2(out[("batch", True)][i], out[("batch", False)][i]) < bar
     assert np.array_equal(out[("single", True)], out[("batch", True)][0])
     assert np.array_equal(out[("single", False)], out[("batch", False)][0])
 
