@@ -14,8 +14,9 @@
 // in BF16, accumulation FP32, FP32 master weights, Adam.  Convolutions are
 // implicit GEMMs (pixels x out-channels x 9*in-channels): the forward pass and
 // the data gradient on the tcgen05 tensor cores (BF16 operands from shared
-// memory, FP32 accumulator in tensor memory), the weight gradient on the FP32
-// pipes with a deterministic two-stage reduction over pixels.  Channel counts are padded to multiples of 16
+// memory, FP32 accumulator in tensor memory), the weight gradient on the
+// tensor cores too (k_wgrad_tc: a contraction over pixels with MN-major
+// operands) with a deterministic two-stage reduction over CTAs.  Channel counts are padded to multiples of 16
 // (input 2 -> 16, output 1 -> 16) with zero weights.
 //
 // LES with closure: each step the network maps (w, psi) of the LES state to
@@ -460,15 +461,17 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // Tensor map of B activation images [B][H][Wd][KC] (BF16, channels
-// innermost) as the 4-D array {KC, Wd, H, B}, boxes of 16 pixels x 10 rows
-// with the 32- (KC = 16) or 64-byte (KC = 32) swizzle.
+// innermost) as the 4-D array {KC, Wd, H, B}, boxes of 16 pixels x `rows`
+// rows (10: a tile and its halo) with the 32- (KC = 16) or 64-byte (KC = 32)
+// swizzle.
 template <int KC>
-cudaError_t conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* act, int B, int H, int Wd) {
+cudaError_t conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* act, int B, int H, int Wd,
+                            int rows = kConvTY + 2) {
     const PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
     if (!enc) return cudaErrorNotSupported;
     const cuuint64_t dims[4] = {(cuuint64_t)KC, (cuuint64_t)Wd, (cuuint64_t)H, (cuuint64_t)B};
     const cuuint64_t strides[3] = {(cuuint64_t)KC * 2, (cuuint64_t)Wd * KC * 2, (cuuint64_t)H * Wd * KC * 2};
-    const cuuint32_t box[4] = {(cuuint32_t)KC, kConvTX, kConvTY + 2, 1};
+    const cuuint32_t box[4] = {(cuuint32_t)KC, kConvTX, (cuuint32_t)rows, 1};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<__nv_bfloat16*>(act), dims, strides,
                            box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -963,6 +966,256 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const __nv_bfloat16* __restr
 #pragma unroll
         for (int c = 0; c < CIG; ++c) out[((long)co * 9 + t) * CI + ci0 + c] = acc[t][c];
     if ((lane & 7) == 0) out[(long)CO * 9 * CI + co] = accb;
+}
+
+// Weight and bias gradient of one layer on the tcgen05 tensor cores:
+//   dW[co, t, ci] = sum_p dz[p, co] in[p + off_t, ci],   db[co] = sum_p dz[p, co],
+// a contraction over the pixels.  A persistent CTA accumulates, over its
+// 128-pixel tiles (8 x 16), one FP32 matrix in tensor memory
+//   D[(dy, co), (dx, ci | 1)] += sum over the tile's halo pixels q of
+//                                 dz_tile[q - (dy, 0), co] * in[q + (0, dx), ci]
+// with K = the 160 pixels of the 10 x 16 halo box (one MMA of K = 16 per box
+// row).  Both operands are MN-major (channels contiguous, as the images are
+// stored), read through 32/64-byte swizzled descriptors straight from TMA
+// boxes:
+//   A (M = 128): the tile's dz box in rows 2..9 of a zeroed 24-row buffer Z;
+//     row block dy (32 or 16 channels wide) starts at Z row 1 - dy, so the
+//     blocks dy = +1, 0, -1 are whole-row offsets (the rest of M is unused);
+//     the zero rows keep every pixel outside the tile out of the sum.
+//   B (N = 3 CI + 16): the three dx-shifted boxes of the input halo (the
+//     boxes of k_conv_tc, circular edges rewritten the same way) side by
+//     side, then a block of ones -- whose column gives db from the dy = 0 rows.
+// Thread 0 loads the next tile's boxes into the other of two slots while the
+// MMAs of this one run; at the end the 4 warps read D (warp w: lanes 32 w ..)
+// and write the CTA's partial sums in k_conv_wgrad's layout for k_reduce_rows.
+// Every wait is bounded (bit 4 of *err, the partial sums are then zero).
+template <int CI, int CO>
+struct WgTile {
+    static constexpr int ROWI = CI * 2;                       // bytes of an input pixel
+    static constexpr int ROWD = CO * 2;                       // bytes of a dz pixel
+    static constexpr int BOXI = (kConvTY + 2) * kConvTX * ROWI;   // one input box, 10 x 16
+    static constexpr int BOXD = kConvTY * kConvTX * ROWD;         // the dz box, 8 x 16
+    static constexpr int ZROWS = 24;
+    static constexpr int ZB = ZROWS * kConvTX * ROWD;
+    static constexpr int SLOT = 4 * BOXI + ZB;                // 3 dx boxes, the ones block, Z
+    static constexpr int N = 3 * CI + 16;
+    static constexpr size_t SMEM = 2 * (size_t)SLOT + 1024;
+    static_assert(BOXI % 1024 == 0 && ZB % 1024 == 0, "operands stay aligned to the swizzle pattern");
+};
+
+// Shared-memory descriptor of an MN-major operand with the 32- or 64-byte
+// swizzle (ROWB = the swizzle width): lbo = byte step between ROWB-wide
+// blocks along M (or N), sbo = byte step between groups of 8 rows along K.
+template <int ROWB>
+__device__ __forceinline__ uint64_t umma_desc_mn(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)(ROWB == 64 ? 4 : 6) << 61;
+    return d;
+}
+
+template <int CI, int CO>
+__global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUtensorMap tin,
+                                                     const __grid_constant__ CUtensorMap tdz,
+                                                     const __nv_bfloat16* __restrict__ in, float* part, int B,
+                                                     int H, int Wd, unsigned int* err) {
+    using WT = WgTile<CI, CO>;
+    constexpr int ROWI = WT::ROWI, ROWD = WT::ROWD, KGI = CI / 8;
+    constexpr int TMEM_COLS = 128;
+    extern __shared__ __align__(1024) unsigned char wg_smem[];
+    const uint32_t sraw = smem_u32(wg_smem);
+    const uint32_t sbase = (sraw + 1023u) & ~1023u;
+    unsigned char* gbase = wg_smem + (sbase - sraw);
+    __shared__ __align__(8) uint64_t mbar_full[2];
+    __shared__ __align__(8) uint64_t mbar_mma[2];
+    __shared__ uint32_t tmem_base;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
+    const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
+    const int ntiles = tiles_img * B;
+    const int nk = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_base)),
+                     "r"(TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+    }
+    // zero both Z buffers, ones in both ones blocks (its layout does not matter)
+    for (int s = 0; s < 2; ++s) {
+        uint4* z = reinterpret_cast<uint4*>(gbase + s * WT::SLOT + 4 * WT::BOXI);
+        for (int i = tid; i < WT::ZB / 16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
+        uint4* o = reinterpret_cast<uint4*>(gbase + s * WT::SLOT + 3 * WT::BOXI);
+        const uint32_t one2 = 0x3F803F80u;   // two BF16 ones
+        for (int i = tid; i < WT::BOXI / 16; i += blockDim.x) o[i] = make_uint4(one2, one2, one2, one2);
+    }
+    if (tid == 0) {
+        for (int s = 0; s < 2; ++s) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar_full[s])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar_mma[s])) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        s_ok = 1;
+    }
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    const uint32_t tmem = tmem_base;
+
+    auto tile_xy = [&](int k, int& b, int& tx0, int& ty0) {
+        const int tile = (int)blockIdx.x + k * (int)gridDim.x;
+        b = tile / tiles_img;
+        const int tl = tile - b * tiles_img;
+        tx0 = (tl % tiles_x) * kConvTX;
+        ty0 = (tl / tiles_x) * kConvTY;
+    };
+    auto issue_loads = [&](int k) {
+        const int s = k & 1;
+        int b, tx0, ty0;
+        tile_xy(k, b, tx0, ty0);
+        const uint32_t slot = sbase + s * WT::SLOT;
+        const uint32_t bar = smem_u32(&mbar_full[s]);
+        mbar_expect_tx(bar, (uint32_t)(3 * WT::BOXI + WT::BOXD));
+#pragma unroll
+        for (int d = 0; d < 3; ++d) tma_load_4d(slot + d * WT::BOXI, &tin, 0, tx0 + d - 1, ty0 - 1, b, bar);
+        tma_load_4d(slot + 4 * WT::BOXI + 2 * kConvTX * ROWD, &tdz, 0, tx0, ty0, b, bar);
+    };
+    // thread 0's bookkeeping: loads issued up to tile kl, MMAs committed up to km
+    int kl = 0, km = -1;
+    if (tid == 0 && nk > 0) issue_loads(kl++);
+
+    for (int k = 0; k < nk; ++k) {
+        const int s = k & 1;
+        int b, tx0, ty0;
+        tile_xy(k, b, tx0, ty0);
+        if (tid == 0 && !mbar_wait_bounded(smem_u32(&mbar_full[s]), (uint32_t)(k >> 1) & 1u)) s_ok = 0;
+        __syncthreads();
+        if (!s_ok) break;
+        // circular wrap at the image edges: rewrite the zero-filled positions
+        // of the three input boxes (as k_conv_tc)
+        if (tx0 == 0 || ty0 == 0 || tx0 + kConvTX >= Wd || ty0 + kConvTY >= H) {
+            (void)mbar_try_wait(smem_u32(&mbar_full[s]), (uint32_t)(k >> 1) & 1u);
+            const long img = (long)b * H * Wd;
+            unsigned char* slotp = gbase + s * WT::SLOT;
+            for (int i = tid; i < 3 * (kConvTY + 2) * kConvTX * KGI; i += blockDim.x) {
+                const int q = i % KGI;
+                int r = i / KGI;
+                const int c = r % kConvTX;
+                r /= kConvTX;
+                const int hr = r % (kConvTY + 2);
+                const int d = r / (kConvTY + 2);
+                int yy = ty0 + hr - 1, xx = tx0 + c + d - 1;
+                if (yy >= 0 && yy < H && xx >= 0 && xx < Wd) continue;
+                yy += yy < 0 ? H : 0;
+                yy -= yy >= H ? H : 0;
+                yy -= yy >= H ? H : 0;
+                xx += xx < 0 ? Wd : 0;
+                xx -= xx >= Wd ? Wd : 0;
+                xx -= xx >= Wd ? Wd : 0;
+                const uint4 v = *reinterpret_cast<const uint4*>(in + (img + (long)yy * Wd + xx) * CI + q * 8);
+                const int row = hr * kConvTX + c;
+                const int pq = ROWI == 64 ? (q ^ ((row >> 1) & 3)) : (q ^ ((row >> 2) & 1));
+                *reinterpret_cast<uint4*>(slotp + d * WT::BOXI + row * ROWI + pq * 16) = v;
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        if (tid == 0) {
+            constexpr uint32_t idesc = umma_idesc_bf16(128, WT::N) | (1u << 15) | (1u << 16);   // A, B MN-major
+            const uint32_t slot = sbase + s * WT::SLOT;
+            const uint32_t z = slot + 4 * WT::BOXI;
+#pragma unroll 1
+            for (int rho = 0; rho < kConvTY + 2; ++rho) {
+                const uint64_t ad = umma_desc_mn<ROWD>(z + rho * kConvTX * ROWD, kConvTX * ROWD, 8 * ROWD);
+                const uint64_t bd = umma_desc_mn<ROWI>(slot + rho * kConvTX * ROWI, WT::BOXI, 8 * ROWI);
+                const uint32_t acc = (k > 0 || rho > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                    " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+                             smem_u32(&mbar_mma[s]))
+                         : "memory");
+            km = k;
+            // the next tile's boxes go to the other slot once the MMAs that
+            // read it (tile k - 1) are done
+            if (kl < nk) {
+                if (k >= 1 && !mbar_wait_bounded(smem_u32(&mbar_mma[s ^ 1]), (uint32_t)((k - 1) >> 1) & 1u))
+                    s_ok = 0;
+                else
+                    issue_loads(kl++);
+            }
+        }
+    }
+    // every MMA complete before the accumulator is read
+    if (tid == 0 && km >= 0 && !mbar_wait_bounded(smem_u32(&mbar_mma[km & 1]), (uint32_t)(km >> 1) & 1u)) s_ok = 0;
+    if (tid == 0 && !s_ok) {
+        atomicOr(err, 4u);
+        for (int k = km + 1; k < kl; ++k) mbar_wait_bounded(smem_u32(&mbar_full[k & 1]), (uint32_t)(k >> 1) & 1u);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+
+    // D row m = (block i = m / CO: dy = 1 - i, channel co = m % CO); column
+    // n = (dx + 1) CI + ci, the ones column 3 CI
+    const long stride = (long)CO * 9 * CI + CO;
+    float* out = part + (long)blockIdx.x * stride;
+    const int m = warp * 32 + lane;
+    const int blk = m / CO, co = m % CO;
+    const bool ok = s_ok && nk > 0;
+#pragma unroll 1
+    for (int c0 = 0; c0 < WT::N; c0 += 16) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        if (blk > 2) continue;
+        const int dy = 1 - blk;
+#pragma unroll
+        for (int e = 0; e < 16; ++e) {
+            const int n = c0 + e;
+            const float v = ok ? __uint_as_float(r[e]) : 0.0f;
+            if (n < 3 * CI) {
+                const int dx = n / CI - 1, ci = n % CI;
+                const int t = (dy + 1) * 3 + (dx + 1);
+                out[((long)co * 9 + t) * CI + ci] = v;
+            } else if (n == 3 * CI && dy == 0) {
+                out[(long)CO * 9 * CI + co] = v;
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+}
+
+// Launch k_wgrad_tc over B images with up to `grid` CTAs (one per SM); the
+// partial sums of the CTAs launched go to part[0 .. returned count).
+template <int CI, int CO>
+cudaError_t launch_wgrad(const __nv_bfloat16* dz, const __nv_bfloat16* in, float* part, int B, int H, int Wd,
+                         int grid, unsigned int* err, cudaStream_t st, int* nblk) {
+    CUtensorMap mi, md;
+    cudaError_t e = conv_tensor_map<CI>(&mi, in, B, H, Wd);
+    if (e == cudaSuccess) e = conv_tensor_map<CO>(&md, dz, B, H, Wd, kConvTY);
+    if (e != cudaSuccess) return e;
+    const long ntiles = (long)((Wd + kConvTX - 1) / kConvTX) * ((H + kConvTY - 1) / kConvTY) * B;
+    *nblk = (int)std::max<long>(1, std::min<long>(ntiles, grid));
+    return launch_k(k_wgrad_tc<CI, CO>, *nblk, 128, WgTile<CI, CO>::SMEM, st, false, mi, md, in, part, B, H, Wd,
+                    err);
 }
 
 // out[i] = sum_b part[b * n + i], b in order.
@@ -1539,21 +1792,35 @@ int loss_backward(s2d_cnn* c, int B, bool grads, double* loss) {
     std::vector<double> lp(lb);
     C_CUDA(cudaMemcpyAsync(lp.data(), c->lpart, sizeof(double) * lb, cudaMemcpyDeviceToHost, c->stream));
     if (grads) {
+        // S2D_WGRAD_FP32=1: the weight gradient on the FP32 pipes (comparisons)
+        const char* wv = std::getenv("S2D_WGRAD_FP32");
+        const bool wgrad_fp32 = wv && wv[0] && wv[0] != '0';
         const __nv_bfloat16* dz = c->dZ6;
         __nv_bfloat16* bufs[2] = {c->dZa, c->dZb};
         for (int l = kLayers - 1; l >= 0; --l) {
             const __nv_bfloat16* in = l == 0 ? c->X0 : c->A[l - 1];
             const int CI = kCinP[l], CO = kCoutP[l];
-            const size_t sm = (size_t)(3 * c->Wd * CI + c->Wd * CO) * sizeof(__nv_bfloat16);
             const long n = (long)CO * 9 * CI + CO;
-            if (CI == 16)
-                k_conv_wgrad<16, 32><<<c->wg_blocks, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
-            else if (CO == 16)
-                k_conv_wgrad<32, 16><<<c->wg_blocks, 16 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
-            else
-                k_conv_wgrad<32, 32><<<c->wg_blocks, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
-            C_CUDA(cudaGetLastError());
-            k_reduce_rows<<<nblocks(n, 256), 256, 0, c->stream>>>(c->part, c->wg_blocks, n, c->grad + c->poff[l]);
+            int nblk = c->wg_blocks;
+            if (wgrad_fp32) {   // the FP32-pipe kernel, for comparisons
+                const size_t sm = (size_t)(3 * c->Wd * CI + c->Wd * CO) * sizeof(__nv_bfloat16);
+                if (CI == 16)
+                    k_conv_wgrad<16, 32><<<nblk, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+                else if (CO == 16)
+                    k_conv_wgrad<32, 16><<<nblk, 16 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+                else
+                    k_conv_wgrad<32, 32><<<nblk, 32 * 8, sm, c->stream>>>(dz, in, c->part, B, c->H, c->Wd);
+                C_CUDA(cudaGetLastError());
+            } else {
+                const int g = std::min(c->wg_blocks, c->sms);
+                if (CI == 16)
+                    C_CUDA((launch_wgrad<16, 32>(dz, in, c->part, B, c->H, c->Wd, g, c->cflags, c->stream, &nblk)));
+                else if (CO == 16)
+                    C_CUDA((launch_wgrad<32, 16>(dz, in, c->part, B, c->H, c->Wd, g, c->cflags, c->stream, &nblk)));
+                else
+                    C_CUDA((launch_wgrad<32, 32>(dz, in, c->part, B, c->H, c->Wd, g, c->cflags, c->stream, &nblk)));
+            }
+            k_reduce_rows<<<nblocks(n, 256), 256, 0, c->stream>>>(c->part, nblk, n, c->grad + c->poff[l]);
             C_CUDA(cudaGetLastError());
             if (l > 0) {
                 __nv_bfloat16* out = c->keep ? c->dZk[l - 1] : bufs[l & 1];
@@ -1910,6 +2177,12 @@ S2D_API int s2d_cnn_create(int32_t grid, int32_t max_batch, uint64_t seed, int32
         cudaFuncSetAttribute(k_conv_wgrad<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
         cudaFuncSetAttribute(k_conv_wgrad<32, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
         cudaFuncSetAttribute(k_conv_wgrad<32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+        cudaFuncSetAttribute(k_wgrad_tc<16, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WgTile<16, 32>::SMEM);
+        cudaFuncSetAttribute(k_wgrad_tc<32, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WgTile<32, 16>::SMEM);
+        cudaFuncSetAttribute(k_wgrad_tc<32, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)WgTile<32, 32>::SMEM);
     }
     // He-uniform initialisation from a seeded counter-based generator
     std::vector<float> pad(off, 0.f);

@@ -172,6 +172,31 @@ def test_fused_forward_equals_the_layerwise_forward(S, grid, B):
     assert e < 2e-3 and emax < 2e-2
 
 
+@pytest.mark.parametrize("grid, B", [(8, 3), (24, 2), (40, 2), (192, 2)])
+def test_tensor_core_weight_gradient_matches_the_fp32_pipes(S, grid, B, monkeypatch):
+    """The weight and bias gradients from the tensor cores (k_wgrad_tc: one
+    accumulator per CTA over its tiles, MN-major operands, the bias gradient
+    from a block of ones) against the FP32-pipe kernel on the same dL/dz and
+    activations: the same sums in another order, at ragged and doubly wrapped
+    tiles and at the 192^2 LES grid."""
+    rng = np.random.default_rng(300 + grid)
+    x = rng.standard_normal((B, grid, grid, 2)).astype(np.float32)
+    t = (0.3 * rng.standard_normal((B, grid, grid))).astype(np.float32)
+    with S.ClosureNet(grid, max_batch=B, seed=17) as net:
+        net.set_scales([1.0, 1.0, 1.0])
+        monkeypatch.setenv("S2D_WGRAD_FP32", "1")
+        l32, g32 = net.grad(x, t)
+        monkeypatch.setenv("S2D_WGRAD_FP32", "0")
+        ltc, gtc = net.grad(x, t)
+        net.status()
+    assert ltc == l32
+    a, b = _oracle_params(gtc, bf=False), _oracle_params(g32, bf=False)
+    for l in range(6):
+        eW, eb = _rel(a[l][0], b[l][0]), _rel(a[l][1], b[l][1])
+        print(f"grid {grid} layer {l}: dW rel {eW:.1e}, db rel {eb:.1e}")
+        assert eW < 1e-5 and eb < 1e-5
+
+
 def test_subgrid_flux_vs_oracle(S):
     nd, nl, nu = 64, 16, 2e-3
     gd, gl = O.get_grid_size(nd, nd), O.get_grid_size(nl, nl)
