@@ -985,8 +985,8 @@ __global__ void __launch_bounds__(256) k_conv_wgrad(const __nv_bfloat16* __restr
 //   B (N = 3 CI + 16): the three dx-shifted boxes of the input halo (the
 //     boxes of k_conv_tc, circular edges rewritten the same way) side by
 //     side, then a block of ones -- whose column gives db from the dy = 0 rows.
-// Thread 0 loads the next tile's boxes into the other of two slots while the
-// MMAs of this one run; at the end the 4 warps read D (warp w: lanes 32 w ..)
+// Thread 0 keeps the boxes of the next two tiles loading into three slots
+// while the MMAs of this one run; at the end the 4 warps read D (warp w: lanes 32 w ..)
 // and write the CTA's partial sums in k_conv_wgrad's layout for k_reduce_rows.
 // Every wait is bounded (bit 4 of *err, the partial sums are then zero).
 template <int CI, int CO>
@@ -995,11 +995,13 @@ struct WgTile {
     static constexpr int ROWD = CO * 2;                       // bytes of a dz pixel
     static constexpr int BOXI = (kConvTY + 2) * kConvTX * ROWI;   // one input box, 10 x 16
     static constexpr int BOXD = kConvTY * kConvTX * ROWD;         // the dz box, 8 x 16
-    static constexpr int ZROWS = 24;
+    // rows of Z the MMAs read: M / CO row blocks (4 or 8) + 10 - 1
+    static constexpr int ZROWS = CO == 32 ? 16 : 24;
     static constexpr int ZB = ZROWS * kConvTX * ROWD;
     static constexpr int SLOT = 4 * BOXI + ZB;                // 3 dx boxes, the ones block, Z
+    static constexpr int NSLOT = 3;
     static constexpr int N = 3 * CI + 16;
-    static constexpr size_t SMEM = 2 * (size_t)SLOT + 1024;
+    static constexpr size_t SMEM = NSLOT * (size_t)SLOT + 1024;
     static_assert(BOXI % 1024 == 0 && ZB % 1024 == 0, "operands stay aligned to the swizzle pattern");
 };
 
@@ -1028,8 +1030,9 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
     const uint32_t sraw = smem_u32(wg_smem);
     const uint32_t sbase = (sraw + 1023u) & ~1023u;
     unsigned char* gbase = wg_smem + (sbase - sraw);
-    __shared__ __align__(8) uint64_t mbar_full[2];
-    __shared__ __align__(8) uint64_t mbar_mma[2];
+    constexpr int NS = WT::NSLOT;
+    __shared__ __align__(8) uint64_t mbar_full[NS];
+    __shared__ __align__(8) uint64_t mbar_mma[NS];
     __shared__ uint32_t tmem_base;
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -1044,8 +1047,8 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
     }
-    // zero both Z buffers, ones in both ones blocks (its layout does not matter)
-    for (int s = 0; s < 2; ++s) {
+    // zero the Z buffers, ones in the ones blocks (their layout does not matter)
+    for (int s = 0; s < NS; ++s) {
         uint4* z = reinterpret_cast<uint4*>(gbase + s * WT::SLOT + 4 * WT::BOXI);
         for (int i = tid; i < WT::ZB / 16; i += blockDim.x) z[i] = make_uint4(0, 0, 0, 0);
         uint4* o = reinterpret_cast<uint4*>(gbase + s * WT::SLOT + 3 * WT::BOXI);
@@ -1053,7 +1056,7 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
         for (int i = tid; i < WT::BOXI / 16; i += blockDim.x) o[i] = make_uint4(one2, one2, one2, one2);
     }
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < NS; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar_full[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&mbar_mma[s])) : "memory");
         }
@@ -1074,11 +1077,11 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
         ty0 = (tl / tiles_x) * kConvTY;
     };
     auto issue_loads = [&](int k) {
-        const int s = k & 1;
+        const int s = k % NS;
         int b, tx0, ty0;
         tile_xy(k, b, tx0, ty0);
         const uint32_t slot = sbase + s * WT::SLOT;
-        const uint32_t bar = smem_u32(&mbar_full[s]);
+        const uint32_t bar = smem_u32(&mbar_full[s]);   // slot s, (k / NS)-th use
         mbar_expect_tx(bar, (uint32_t)(3 * WT::BOXI + WT::BOXD));
 #pragma unroll
         for (int d = 0; d < 3; ++d) tma_load_4d(slot + d * WT::BOXI, &tin, 0, tx0 + d - 1, ty0 - 1, b, bar);
@@ -1086,19 +1089,21 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
     };
     // thread 0's bookkeeping: loads issued up to tile kl, MMAs committed up to km
     int kl = 0, km = -1;
-    if (tid == 0 && nk > 0) issue_loads(kl++);
+    if (tid == 0)
+        while (kl < nk && kl < NS - 1) issue_loads(kl++);
 
     for (int k = 0; k < nk; ++k) {
-        const int s = k & 1;
+        const int s = k % NS;
+        const uint32_t par = (uint32_t)(k / NS) & 1u;
         int b, tx0, ty0;
         tile_xy(k, b, tx0, ty0);
-        if (tid == 0 && !mbar_wait_bounded(smem_u32(&mbar_full[s]), (uint32_t)(k >> 1) & 1u)) s_ok = 0;
+        if (tid == 0 && !mbar_wait_bounded(smem_u32(&mbar_full[s]), par)) s_ok = 0;
         __syncthreads();
         if (!s_ok) break;
         // circular wrap at the image edges: rewrite the zero-filled positions
         // of the three input boxes (as k_conv_tc)
         if (tx0 == 0 || ty0 == 0 || tx0 + kConvTX >= Wd || ty0 + kConvTY >= H) {
-            (void)mbar_try_wait(smem_u32(&mbar_full[s]), (uint32_t)(k >> 1) & 1u);
+            (void)mbar_try_wait(smem_u32(&mbar_full[s]), par);
             const long img = (long)b * H * Wd;
             unsigned char* slotp = gbase + s * WT::SLOT;
             for (int i = tid; i < 3 * (kConvTY + 2) * kConvTX * KGI; i += blockDim.x) {
@@ -1145,10 +1150,10 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
                              smem_u32(&mbar_mma[s]))
                          : "memory");
             km = k;
-            // the next tile's boxes go to the other slot once the MMAs that
-            // read it (tile k - 1) are done
+            // tile k + NS - 1 goes to the slot of tile k - 1 once the MMAs
+            // that read it are done
             if (kl < nk) {
-                if (k >= 1 && !mbar_wait_bounded(smem_u32(&mbar_mma[s ^ 1]), (uint32_t)((k - 1) >> 1) & 1u))
+                if (k >= 1 && !mbar_wait_bounded(smem_u32(&mbar_mma[(k - 1) % NS]), (uint32_t)((k - 1) / NS) & 1u))
                     s_ok = 0;
                 else
                     issue_loads(kl++);
@@ -1156,10 +1161,10 @@ __global__ void __launch_bounds__(128, 1) k_wgrad_tc(const __grid_constant__ CUt
         }
     }
     // every MMA complete before the accumulator is read
-    if (tid == 0 && km >= 0 && !mbar_wait_bounded(smem_u32(&mbar_mma[km & 1]), (uint32_t)(km >> 1) & 1u)) s_ok = 0;
+    if (tid == 0 && km >= 0 && !mbar_wait_bounded(smem_u32(&mbar_mma[km % NS]), (uint32_t)(km / NS) & 1u)) s_ok = 0;
     if (tid == 0 && !s_ok) {
         atomicOr(err, 4u);
-        for (int k = km + 1; k < kl; ++k) mbar_wait_bounded(smem_u32(&mbar_full[k & 1]), (uint32_t)(k >> 1) & 1u);
+        for (int k = km + 1; k < kl; ++k) mbar_wait_bounded(smem_u32(&mbar_full[k % NS]), (uint32_t)(k / NS) & 1u);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
