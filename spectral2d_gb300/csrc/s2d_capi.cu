@@ -100,6 +100,15 @@ int pick_launch(const s2d_handle* h, int threads_per_group, size_t bytes_per_gro
     return S2D_OK;
 }
 
+__global__ void k_round_f32(const double* __restrict__ in, float* out, long n) {
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+cudaError_t round_to_f32(const double* in, float* out, long n, cudaStream_t st) {
+    k_round_f32<<<(int)std::min<long>((n + 255) / 256, 152L * 8), 256, 0, st>>>(in, out, n);
+    return cudaGetLastError();
+}
+
 // join: an event on another stream that the epilogue (the first kernel that
 // reads h->src) waits for; the kernels before it run concurrently with that
 // stream's work
@@ -115,6 +124,8 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
     fs.op[2] = OP_W;
     fs.tab[0] = h->fu;
     fs.tab[1] = h->fv;
+    fs.tabf[0] = h->fu32;
+    fs.tabf[1] = h->fv32;
     fs.out[0] = h->I[0];
     fs.out[1] = h->I[1];
     fs.out[2] = h->I[2];
@@ -525,6 +536,10 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         S2D_ALLOC(h->rk2s, (size_t)d.KX * d.ldS * sizeof(double));
         S2D_ALLOC(h->fu, (size_t)d.KX * d.ldS * sizeof(double));
         S2D_ALLOC(h->fv, (size_t)d.KX * d.ldS * sizeof(double));
+        if (h->prec == S2D_FP32) {
+            S2D_ALLOC(h->fu32, (size_t)d.KX * d.ldS * sizeof(float));
+            S2D_ALLOC(h->fv32, (size_t)d.KX * d.ldS * sizeof(float));
+        }
     }
     // complex twiddles (M entries) followed by the FMA-form blocks
     std::vector<TwEnt<double>> tabd;
@@ -572,6 +587,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
     if (Kern<double>::init_rk2(d, h->rk2, h->stream) != cudaSuccess ||
         (h->rk2s && Kern<double>::init_rk2(d, h->rk2s, h->stream, std::sqrt(0.5) / (double)d.M) != cudaSuccess) ||
         (h->fu && Kern<double>::init_uv_factors(d, h->rk2s, h->fu, h->fv, h->stream) != cudaSuccess) ||
+        (h->fu32 && (round_to_f32(h->fu, h->fu32, (long)d.KX * d.ldS, h->stream) != cudaSuccess ||
+                     round_to_f32(h->fv, h->fv32, (long)d.KX * d.ldS, h->stream) != cudaSuccess)) ||
         (h->cc && Kern<double>::init_stage_factors(d, h->ph.nu, h->cc, h->vk, h->stream) != cudaSuccess))
         return bail(fail(S2D_ERR_CUDA, "rk2 init failed"));
 
@@ -626,7 +643,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
-    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->cc, h->vk, h->tw,  h->ref_stage,
+    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->fu32, h->fv32, h->cc, h->vk, h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
                     h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);

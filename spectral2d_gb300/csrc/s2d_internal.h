@@ -112,6 +112,7 @@ struct FieldSet {
     int op[4];
     void* out[4];
     const double* tab[4];
+    const float* tabf[4];   // FP32 runs: OP_TU / OP_TV factors already rounded (or null)
 };
 
 // Launch shape for one kernel: G groups of Tg threads, dynamic smem bytes.
@@ -257,6 +258,11 @@ struct s2d_handle {
     // on the FP64 pipe per mode saved)
     double* fu = nullptr;
     double* fv = nullptr;
+    // FP32 handles: the same factors rounded to FP32 once (the rounding the
+    // FP32 inverse y-pass applies per mode), read in half the bytes and with
+    // no FP64 conversion
+    float* fu32 = nullptr;
+    float* fv32 = nullptr;
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array

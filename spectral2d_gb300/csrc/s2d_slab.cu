@@ -146,6 +146,8 @@ int slab_phase(s2d_slab* s, int stage, int phase, double dt) {
         fs.op[1] = OP_TV;
         fs.tab[0] = h->fu + cs;
         fs.tab[1] = h->fv + cs;
+        fs.tabf[0] = h->fu32 ? h->fu32 + cs : nullptr;
+        fs.tabf[1] = h->fv32 ? h->fv32 + cs : nullptr;
         fs.out[0] = (VT*)h->I[0] + c0;
         fs.out[1] = (VT*)h->I[1] + c0;
         const VT* win = (const VT*)((stage <= 1) ? h->S0 : h->S1) + cs;

@@ -90,17 +90,22 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
     int op;
     void* outp;
     const double* tab;
+    const float* tabf;
     switch (f) {
-        case 0: op = fs.op[0]; outp = fs.out[0]; tab = fs.tab[0]; break;
-        case 1: op = fs.op[1]; outp = fs.out[1]; tab = fs.tab[1]; break;
-        case 2: op = fs.op[2]; outp = fs.out[2]; tab = fs.tab[2]; break;
-        default: op = fs.op[3]; outp = fs.out[3]; tab = fs.tab[3]; break;
+        case 0: op = fs.op[0]; outp = fs.out[0]; tab = fs.tab[0]; tabf = fs.tabf[0]; break;
+        case 1: op = fs.op[1]; outp = fs.out[1]; tab = fs.tab[1]; tabf = fs.tabf[1]; break;
+        case 2: op = fs.op[2]; outp = fs.out[2]; tab = fs.tab[2]; tabf = fs.tabf[2]; break;
+        default: op = fs.op[3]; outp = fs.out[3]; tab = fs.tab[3]; tabf = fs.tabf[3]; break;
     }
-    if (op == OP_TU || op == OP_TV) rk2 = tab;   // the factor table takes the 1/k^2 table's place
+    const bool tfac = op == OP_TU || op == OP_TV;
+    if (tfac) rk2 = tab;   // the factor table takes the 1/k^2 table's place
+    // FP32 with the factors pre-rounded: read them as FP32 (the same values)
+    const bool f32tab = sizeof(T) == 4 && tfac && tabf != nullptr;
     VT* buf = bufs + (size_t)g * d.M;
 
     const VT* col = S + (size_t)(active ? kx : 0) * d.ldS;
     const double* rcol = rk2 + (size_t)(active ? kx : 0) * d.ldS;
+    const float* fcol = f32tab ? tabf + (size_t)(active ? kx : 0) * d.ldS : nullptr;
     // M = kElemsPerThread * Tg: a fixed trip count lets every load of the
     // column be in flight at once (the loads are latency-bound)
 #pragma unroll
@@ -115,7 +120,15 @@ __device__ __forceinline__ void yinv_body(const Dims& d, const typename Vec<T>::
             ky = n - d.M;
             jc = ky + d.KY;
         }
-        if (active && jc >= 0) val = apply_op(op, __ldcg(&col[jc]), kx, ky, rcol[jc]);
+        if (active && jc >= 0) {
+            if (f32tab) {   // i f w, as scale_by forms it from the FP64 factor
+                const VT w = __ldcg(&col[jc]);
+                const T fv = (T)fcol[jc];
+                val = mk<VT>(-fv * w.y, fv * w.x);
+            } else {
+                val = apply_op(op, __ldcg(&col[jc]), kx, ky, rcol[jc]);
+            }
+        }
         buf[n] = val;
     }
     fft_run<true>(buf, d, lane, tw);
