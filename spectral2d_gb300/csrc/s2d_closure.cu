@@ -539,12 +539,7 @@ constexpr int kNetOutH = 8, kNetOutW = 14;       // output tile
 constexpr int kNetBoxRows = kNetOutH + 2, kNetBoxW = kNetOutW + 2;   // its halo box: M = 8 x 16 = 128 pixels
 constexpr int kNetSlots = 8;
 constexpr int kNetSlotBytes = kNetBoxRows * kNetBoxW * 64;   // one box of 32-channel pixels
-// B operands of the three rows of taps of all six layers, resident for the
-// whole launch: 3 dy x 3 NC columns x KC channels x 2 bytes per layer
-__host__ __device__ constexpr int net_woff(int L) {   // byte offset of layer L's operands
-    return L == 0 ? 0 : (L <= 5 ? 9216 + (L - 1) * 18432 : 92160);
-}
-constexpr int kNetWBytes = net_woff(kLayers);
+constexpr int kNetWBytes = 3 * 96 * 4 * 16;                  // B operands of the three rows of taps
 constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
 
 struct NetArgs {
@@ -564,7 +559,7 @@ struct NetShared {
     uint64_t accfree[kNetAcc];  // the 8 warps of its epilogue group have read an accumulator
     uint32_t tmem;
     int abort;
-    float bias[kLayers][32];
+    float bias[32];
 };
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
@@ -605,35 +600,14 @@ __device__ __forceinline__ bool net_grid_sync(unsigned int* bar, unsigned int ta
     return true;
 }
 
-// The weights of one layer as the B operands of its three rows of taps: for
-// row dy, column group g = (dx, 8 output channels), the input channels
-// K-major in core matrices; and its biases.
-template <int KC, int NC>
-__device__ __forceinline__ void net_stage_weights(const __nv_bfloat16* __restrict__ W,
-                                                  const float* __restrict__ bias, unsigned char* wdst,
-                                                  float* sbias) {
-    constexpr int KG = KC / 8, N = 3 * NC, NG = N / 8, CORE = 128;
-    for (int i = threadIdx.x; i < 3 * N * KG; i += blockDim.x) {
-        const int nl = i % 8;
-        const int kg = (i / 8) % KG;
-        const int g = (i / (8 * KG)) % NG;
-        const int dyi = i / (8 * KG * NG);
-        const int dxi = g / (NC / 8);
-        const int n = (g % (NC / 8)) * 8 + nl;
-        const int t = dyi * 3 + dxi;
-        const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
-        const int off = ((dyi * NG + g) * KG + kg) * CORE + nl * 16;
-        *reinterpret_cast<uint4*>(wdst + off) = v;
-    }
-    if ((int)threadIdx.x < NC) sbias[threadIdx.x] = bias[threadIdx.x];
-}
-
 // One layer over this CTA's tiles (tile blockIdx.x + k gridDim.x); irun is
 // the CTA's running tile count over all layers, which fixes every slot,
-// accumulator and barrier phase.  L: the layer (its weights at net_woff(L)).
+// accumulator and barrier phase.
 template <int KC, int NC, bool LAST>
-__device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bfloat16* out, float* yout,
-                                          const NetArgs& a, NetShared& sh, uint32_t sbase, int& irun) {
+__device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfloat16* __restrict__ W,
+                                          const float* __restrict__ bias, __nv_bfloat16* out, float* yout,
+                                          const NetArgs& a, NetShared& sh, unsigned char* gbase, uint32_t sbase,
+                                          int& irun) {
     constexpr int KG = KC / 8;                 // 8-channel groups of a pixel
     constexpr int ROWB = KC * 2;               // bytes of one pixel
     constexpr int BOX = kNetBoxRows * kNetBoxW * ROWB;
@@ -647,9 +621,29 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
     const int tiles_img = tiles_x * ((H + kNetOutH - 1) / kNetOutH);
     const int ntiles = tiles_img * a.B;
     const int nk = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
-    const uint32_t bw = sbase + kNetSlots * kNetSlotBytes + net_woff(L);
-    const float* lbias = sh.bias[L];
+    const uint32_t bw = sbase + kNetSlots * kNetSlotBytes;
     volatile int* abort = &sh.abort;
+
+    // the layer's weights as the B operands of the three rows of taps: for
+    // row dy, column group g = (dx, 8 output channels), the input channels
+    // K-major in core matrices (the previous layer's MMAs are all complete)
+    for (int i = tid; i < 3 * N * KG; i += blockDim.x) {
+        const int nl = i % 8;
+        const int kg = (i / 8) % KG;
+        const int g = (i / (8 * KG)) % NG;
+        const int dyi = i / (8 * KG * NG);
+        const int dxi = g / (NC / 8);
+        const int n = (g % (NC / 8)) * 8 + nl;
+        const int t = dyi * 3 + dxi;
+        const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
+        const int off = ((dyi * NG + g) * KG + kg) * CORE + nl * 16;
+        *reinterpret_cast<uint4*>(gbase + kNetSlots * kNetSlotBytes + off) = v;
+    }
+    if (tid < NC) sh.bias[tid] = bias[tid];
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
     // tile k: output rows [oy0, oy0 + 8), columns [ox0, ox0 + 14); its box is
     // image rows oy0 - 1 .. oy0 + 8 and columns ox0 - 1 .. ox0 + 14, at
@@ -760,7 +754,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
         // would compete with the tensor core's operand reads)
         float bv[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) bv[e] = cols ? lbias[half * 16 + e] : 0.0f;
+        for (int e = 0; e < 16; ++e) bv[e] = cols ? sh.bias[half * 16 + e] : 0.0f;
         for (int k = (grp - (i0 & 1) + 2) & 1; k < nk; k += kNetGroups) {
             const int i = i0 + k, acc = i % kNetAcc;
             if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i / kNetAcc) & 1u, abort)) {
@@ -860,17 +854,6 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         sh.abort = 0;
     }
-    // every layer's weights and biases, once
-    {
-        unsigned char* wb = gbase + kNetSlots * kNetSlotBytes;
-        net_stage_weights<16, 32>(a.W[0], a.bias[0], wb + net_woff(0), sh.bias[0]);
-        net_stage_weights<32, 32>(a.W[1], a.bias[1], wb + net_woff(1), sh.bias[1]);
-        net_stage_weights<32, 32>(a.W[2], a.bias[2], wb + net_woff(2), sh.bias[2]);
-        net_stage_weights<32, 32>(a.W[3], a.bias[3], wb + net_woff(3), sh.bias[3]);
-        net_stage_weights<32, 32>(a.W[4], a.bias[4], wb + net_woff(4), sh.bias[4]);
-        net_stage_weights<32, 16>(a.W[5], a.bias[5], wb + net_woff(5), sh.bias[5]);
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-    }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
@@ -885,17 +868,17 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         }
         __syncthreads();
     };
-    net_layer<16, 32, false>(&m_in, 0, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<16, 32, false>(&m_in, a.W[0], a.bias[0], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a0, 1, a.act[1], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a0, a.W[1], a.bias[1], a.act[1], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a1, 2, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a1, a.W[2], a.bias[2], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a0, 3, a.act[1], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a0, a.W[3], a.bias[3], a.act[1], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a1, 4, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a1, a.W[4], a.bias[4], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 16, true>(&m_a0, 5, nullptr, a.y, a, sh, sbase, irun);
+    net_layer<32, 16, true>(&m_a0, a.W[5], a.bias[5], nullptr, a.y, a, sh, gbase, sbase, irun);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == kNetMmaWarp)
