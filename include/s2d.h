@@ -326,6 +326,12 @@ S2D_API int s2d_cnn_forward_host(s2d_cnn* c, const float* x, int32_t batch, floa
  * a circular one-pixel frame; 0 runs one launch per layer, the kernels of the
  * gradient path.  Both give the same bits. */
 S2D_API int s2d_cnn_set_fused(s2d_cnn* c, int32_t on);
+/* Fault injection for tests, made on the host: with on != 0, CTA 0 of every
+ * fused forward skips its first grid-barrier arrival, so the other CTAs'
+ * bounded waits (about 1 s) run out, the forward's output is garbage and
+ * s2d_cnn_status reports S2D_ERR_TIMEOUT; on = 0 removes it (each launch
+ * starts its barrier count from zero, so the next forward is clean). */
+S2D_API int s2d_cnn_inject_stall(s2d_cnn* c, int32_t on);
 /* MSE loss of the normalised output against target/rms_Pi and its gradient
  * (same layout as the parameters) */
 S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, int32_t batch, float* grads,

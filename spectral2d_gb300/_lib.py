@@ -124,6 +124,7 @@ SIGNATURES = {
     "s2d_cnn_grad_host": (C.c_int, [C.c_void_p, _fp, _fp, C.c_int32, _fp, _dp]),
     "s2d_cnn_keep_layer_grads": (C.c_int, [C.c_void_p, C.c_int32]),
     "s2d_cnn_set_fused": (C.c_int, [C.c_void_p, C.c_int32]),
+    "s2d_cnn_inject_stall": (C.c_int, [C.c_void_p, C.c_int32]),
     "s2d_cnn_get_tensor": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, _fp]),
     "s2d_cnn_dataset_reserve": (C.c_int, [C.c_void_p, C.c_int32]),
     "s2d_cnn_dataset_size": (C.c_int, [C.c_void_p]),

@@ -550,6 +550,7 @@ struct NetArgs {
     unsigned int* bar;                 // grid barrier: arrivals of this launch
     unsigned int* err;
     int B, H, Wd;
+    int stall;                         // fault injection: CTA 0 skips its first grid-barrier arrival
 };
 
 struct NetShared {
@@ -862,7 +863,8 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
     auto barrier = [&]() {
         __syncthreads();
         ++nbar;
-        if (tid == 0 && !sh.abort && !net_grid_sync(a.bar, (unsigned int)nbar * gridDim.x)) {
+        const bool skip = a.stall && nbar == 1 && blockIdx.x == 0;   // host-injected fault (tests)
+        if (tid == 0 && !sh.abort && !skip && !net_grid_sync(a.bar, (unsigned int)nbar * gridDim.x)) {
             sh.abort = 1;
             atomicOr(a.err, 4u);
         }
@@ -1669,6 +1671,7 @@ struct s2d_cnn {
     // the fused inference forward (k_net_fwd): framed layer-1 input and the
     // two framed activation images, the grid barrier's arrival count
     bool fused = true;
+    bool net_stall = false;     // s2d_cnn_inject_stall
     int net_grid = 0;           // resident CTAs of k_net_fwd (cooperative launch)
     __nv_bfloat16* X0f = nullptr;
     __nv_bfloat16* F[2] = {};
@@ -1754,6 +1757,7 @@ int forward_fused(s2d_cnn* c, int B, bool input_framed) {
     a.B = B;
     a.H = H;
     a.Wd = Wd;
+    a.stall = c->net_stall ? 1 : 0;
     const long ntiles = (long)((Wd + kNetOutW - 1) / kNetOutW) * ((H + kNetOutH - 1) / kNetOutH) * B;
     const int grid = (int)std::min<long>(ntiles, c->net_grid);
     C_CUDA(cudaMemsetAsync(c->netbar, 0, sizeof(unsigned int), c->stream));
@@ -2471,6 +2475,12 @@ S2D_API int s2d_cnn_eval(s2d_cnn* c, int32_t first, int32_t count, double* mean_
 S2D_API int s2d_cnn_set_fused(s2d_cnn* c, int32_t on) {
     if (!c) return cerr(S2D_ERR_INVALID, "null network");
     c->fused = on != 0;
+    return S2D_OK;
+}
+
+S2D_API int s2d_cnn_inject_stall(s2d_cnn* c, int32_t on) {
+    if (!c) return cerr(S2D_ERR_INVALID, "null network");
+    c->net_stall = on != 0;
     return S2D_OK;
 }
 

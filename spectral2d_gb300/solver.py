@@ -445,6 +445,11 @@ class ClosureNet:
         launch per layer; the results are the same bits."""
         L.check(self._L.s2d_cnn_set_fused(self._c, int(bool(on))))
 
+    def inject_stall(self, on: bool = True) -> None:
+        """Host-made fault for tests: one CTA of the fused forward skips a grid
+        barrier, the others' bounded waits run out (S2D_ERR_TIMEOUT)."""
+        L.check(self._L.s2d_cnn_inject_stall(self._c, int(bool(on))))
+
     def keep_layer_grads(self, keep: bool = True) -> None:
         """Keep dL/dz of every hidden layer in the following gradient calls."""
         L.check(self._L.s2d_cnn_keep_layer_grads(self._c, int(bool(keep))))

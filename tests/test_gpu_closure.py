@@ -197,6 +197,32 @@ def test_tensor_core_weight_gradient_matches_the_fp32_pipes(S, grid, B, monkeypa
         assert eW < 1e-5 and eb < 1e-5
 
 
+def test_fused_forward_barrier_timeout_is_reported_and_recovers(S):
+    """Failure detection of the fused forward's grid barrier, the fault made
+    on the host: CTA 0 skips its first arrival, the others' bounded waits
+    run out (about 1 s), the forward returns S2D_ERR_TIMEOUT through
+    s2d_cnn_status instead of hanging, and once the stall is removed the
+    next forward gives the clean result bit for bit."""
+    import time
+    from spectral2d_gb300 import S2DError
+    grid, B = 192, 2
+    x = np.random.default_rng(5).standard_normal((B, grid, grid, 2)).astype(np.float32)
+    with S.ClosureNet(grid, max_batch=B, seed=19) as net:
+        net.set_scales([1.0, 1.0, 1.0])
+        y0 = net.forward(x)
+        net.inject_stall(True)
+        t0 = time.perf_counter()
+        with pytest.raises(S2DError) as ei:
+            net.forward(x)
+        waited = time.perf_counter() - t0
+        assert ei.value.code == -4   # S2D_ERR_TIMEOUT
+        assert 0.5 < waited < 60.0
+        net.inject_stall(False)
+        y1 = net.forward(x)
+        net.status()
+    assert np.array_equal(y0, y1)
+
+
 def test_subgrid_flux_vs_oracle(S):
     nd, nl, nu = 64, 16, 2e-3
     gd, gl = O.get_grid_size(nd, nd), O.get_grid_size(nl, nl)
