@@ -1709,10 +1709,6 @@ int ensure_net_buffers(s2d_cnn* c) {
     if (occ < 1) return cerr(S2D_ERR_UNSUPPORTED, "the fused network kernel does not fit on an SM");
     occ = 1;   // one CTA per SM by design (its TMEM columns, the launch bound)
     c->net_grid = occ * c->sms;
-    if (const char* e = std::getenv("S2D_NET_CTAS")) {   // for measurements: fewer CTAs
-        const int v = std::atoi(e);
-        if (v >= 1 && v < c->net_grid) c->net_grid = v;
-    }
     bool ok = cudaMalloc(&c->X0f, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMemset(c->X0f, 0, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->F[0], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
