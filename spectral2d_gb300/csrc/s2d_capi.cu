@@ -130,11 +130,6 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
     fs.out[1] = h->I[1];
     fs.out[2] = h->I[2];
     const void* win = (stage <= 1) ? h->S0 : h->S1;
-    if (h->coop_bar && bas && !ev && !join) {
-        S2D_CUDA(Kern<T>::stage_coop(d, win, h->rk2s, fs, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt,
-                                     h->ph, h->tw, h->coop_bar, h->flags, h->sms, h->stream));
-        return S2D_OK;
-    }
     if (ev) S2D_CUDA(cudaEventRecord(ev[0], h->stream));
     S2D_CUDA(Kern<T>::yinv(d, win, bas ? h->rk2s : h->rk2, fs, h->tw, h->stream, h->L_yinv));
     if (ev) S2D_CUDA(cudaEventRecord(ev[1], h->stream));
@@ -626,16 +621,6 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         const bool pdl = !(e && e[0] == '0');
         for (Launch* L : {&h->L_yinv, &h->L_xpass, &h->L_yfwd, &h->L_xrow, &h->L_ystore, &h->L_ycol}) L->pdl = pdl;
     }
-    // small Basdevant runs (M <= 384: at least four transforms per 128-thread
-    // CTA) take each RK3 stage in one cooperative launch (S2D_STAGE_COOP=0:
-    // three launches, for comparisons)
-    {
-        const char* e = std::getenv("S2D_STAGE_COOP");
-        const bool on = !(e && e[0] == '0');
-        if (on && h->ph.form == S2D_NL_BASDEVANT && kCoopThreads % d.Tg == 0 && kCoopThreads / d.Tg >= 4 &&
-            cudaMalloc((void**)&h->coop_bar, 64) != cudaSuccess)
-            return bail(fail(S2D_ERR_NOMEM, "cudaMalloc of 64 bytes failed"));
-    }
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
     *out = h;
@@ -658,7 +643,7 @@ S2D_API void s2d_destroy(s2d_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     drop_graph(h);
-    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->fu32, h->fv32, h->coop_bar, h->cc, h->vk, h->tw,  h->ref_stage,
+    void* ptrs[] = {h->S0,    h->S1,        h->Sdw,   h->Ibase, h->rk2,      h->rk2s, h->fu, h->fv, h->fu32, h->fv32, h->cc, h->vk, h->tw,  h->ref_stage,
                     h->flags, h->red64,     h->dscratch, h->src, h->pi, h->phys, h->les_tab, h->Fv,
                     h->zeros, h->cl_I};
     if (h->xstream) cudaStreamSynchronize(h->xstream);
@@ -991,7 +976,6 @@ S2D_API int s2d_check_finite(s2d_handle* h) {
     S2D_CUDA(cudaMemsetAsync(h->flags, 0, sizeof(f), h->stream));
     S2D_CUDA(cudaStreamSynchronize(h->stream));
     if (f & 1u) return fail(S2D_ERR_NONFINITE, "non-finite vorticity written by a stage update");
-    if (f & 2u) return fail(S2D_ERR_TIMEOUT, "a grid-barrier wait of the one-launch stage gave up");
     return S2D_OK;
 }
 

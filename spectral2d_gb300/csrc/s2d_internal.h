@@ -25,7 +25,6 @@ constexpr int kElemsPerThread = 12;   // FFT elements held per thread per pass
 // the FP32 x-pass with register radix-12/16 passes (s2d_xpass32.cuh): row
 // length and its padded shared-memory buffer (elements)
 constexpr int kX32M = 3072;
-constexpr int kCoopThreads = 128;   // CTA of the one-launch stage (k_stage_coop)
 constexpr int kX32Buf = kX32M + kX32M / 16;
 
 // Twiddles of one butterfly of a radix-4 (or radix-2) pass in FMA form:
@@ -173,15 +172,6 @@ struct Kern {
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
                                 void* Sdw, const void* src, int stage, double dt, const Phys& ph,
                                 const void* tw, unsigned int* flags, cudaStream_t st, const Launch& L);
-    // One Basdevant RK3 stage of a small run (Tg <= kCoopThreads / 2) in one
-    // cooperative launch: K1, K2 and K3 as phases between grid barriers
-    // (bar: an arrival count, zeroed by this call before the launch; flags
-    // bit 1: non-finite state, bit 2: a barrier wait ran out).  The same
-    // bodies as the three launches, so the same bits.
-    static cudaError_t stage_coop(const Dims& d, const void* Sin, const double* rk2, const FieldSet& fs, void* Iu,
-                                  void* Iv, void* S0, void* S1, void* Sdw, const void* src, int stage, double dt,
-                                  const Phys& ph, const void* tw, unsigned int* bar, unsigned int* flags,
-                                  int max_ctas, cudaStream_t st);
     // K3 in two launches: forward y-FFT of the columns of both products into
     // compact arrays Fu, Fv, then the epilogue (dW, stage update, Truncate)
     static cudaError_t yfwd_col(const Dims& d, const void* Iu, const void* Iv, void* Fu, void* Fv,
@@ -273,9 +263,6 @@ struct s2d_handle {
     // no FP64 conversion
     float* fu32 = nullptr;
     float* fv32 = nullptr;
-    // small Basdevant runs: each RK3 stage in one cooperative launch
-    // (Kern::stage_coop); its grid barrier's arrival count
-    unsigned int* coop_bar = nullptr;
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array

@@ -27,8 +27,6 @@
 
 #include <cuda_runtime.h>
 
-#include <algorithm>
-
 namespace s2d {
 
 // ------------------------------------------------------------------------
@@ -98,78 +96,6 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_yfwd_rk3
     const bool bad = yfwd_body<T>(d, Iu, Iv, S0, S1, Sdw, src, stage, dt, ph, tw, G, blockIdx.x,
                                   reinterpret_cast<VT*>(smem_raw));
     if (bad && flags) atomicOr(flags, 1u);   // flags may be null: no non-finite report
-}
-
-// One RK3 stage of a small single run in one cooperative launch.  At 128^2
-// or 256^2 every pass is a few dozen CTAs whose work is latency (L2 round
-// trips, a few thousand dependent instructions per warp), and each of the
-// three launches of a stage adds its own launch and dependency latency; here
-// the passes are phases of one grid, K1 -> barrier -> K2 -> barrier -> K3,
-// each CTA taking tiles of G = kCoopThreads / Tg transforms in a grid-stride
-// loop, with the bodies of the three kernels.  The barrier counts arrivals in
-// *bar (zeroed before the launch); a wait is bounded by the global timer (one
-// second) and sets flags bit 2, after which the CTA skips the rest.
-__device__ __forceinline__ unsigned long long coop_timer_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
-    return t;
-}
-__device__ __forceinline__ bool coop_grid_sync(unsigned int* bar, unsigned int target) {
-    __threadfence();
-    atomicAdd(bar, 1u);
-    const unsigned long long t0 = coop_timer_ns();
-    for (;;) {
-        unsigned int v;
-        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(bar) : "memory");
-        if (v >= target) return true;
-        if (coop_timer_ns() - t0 > 1000000000ull) return false;
-        __nanosleep(32);
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kCoopThreads) k_stage_coop(Dims d, const typename Vec<T>::t* __restrict__ Sin,
-                                                             const double* __restrict__ rk2, FieldSet fs,
-                                                             typename Vec<T>::t* Iu, typename Vec<T>::t* Iv,
-                                                             typename Vec<T>::t* S0, typename Vec<T>::t* S1,
-                                                             typename Vec<T>::t* Sdw,
-                                                             const typename Vec<T>::t* __restrict__ src, int stage,
-                                                             double dt, Phys ph,
-                                                             const typename Vec<T>::t* __restrict__ tw,
-                                                             unsigned int* bar, unsigned int* flags) {
-    using VT = typename Vec<T>::t;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    VT* bufs = reinterpret_cast<VT*>(smem_raw);
-    __shared__ int s_ok;
-    const int G1 = blockDim.x / d.Tg, G3 = G1 / 2;
-    const int n1 = fs.nf * ((d.KX + G1 - 1) / G1), n2 = (d.rows + G1 - 1) / G1, n3 = (d.KX + G3 - 1) / G3;
-    if (threadIdx.x == 0) s_ok = 1;
-    auto barrier = [&](unsigned int j) {
-        __syncthreads();
-        if (threadIdx.x == 0 && s_ok && !coop_grid_sync(bar, j * gridDim.x)) {
-            s_ok = 0;
-            atomicOr(flags, 2u);
-        }
-        __syncthreads();
-    };
-    for (int b = blockIdx.x; b < n1; b += gridDim.x) {
-        yinv_body<T>(d, Sin, rk2, fs, tw, G1, b, bufs);
-        __syncthreads();
-    }
-    barrier(1);
-    if (s_ok)
-        for (int b = blockIdx.x; b < n2; b += gridDim.x) {
-            xpass_bas_body<T>(d, Iu, Iv, tw, G1, (T)1, b, bufs);
-            __syncthreads();
-        }
-    barrier(2);
-    bool bad = false;
-    if (s_ok)
-        for (int b = blockIdx.x; b < n3; b += gridDim.x) {
-            bad |= yfwd_body<T>(d, Iu, Iv, S0, S1, Sdw, src, stage, dt, ph, tw, G3, b, bufs);
-            __syncthreads();
-        }
-    if (bad) atomicOr(flags, 1u);
 }
 
 // K3 split in two (FP64 single runs): forward y-FFT of one field's columns
@@ -926,38 +852,6 @@ cudaError_t Kern<T>::init_stage_factors(const Dims& d, double nu, double* cc, do
 template <typename T>
 size_t Kern<T>::smem_limit_yinv() {
     return 0;
-}
-
-template <typename T>
-cudaError_t Kern<T>::stage_coop(const Dims& d, const void* Sin, const double* rk2, const FieldSet& fs, void* Iu,
-                                void* Iv, void* S0, void* S1, void* Sdw, const void* src, int stage, double dt,
-                                const Phys& ph, const void* tw, unsigned int* bar, unsigned int* flags,
-                                int max_ctas, cudaStream_t st) {
-    using VT = typename Vec<T>::t;
-    const int G1 = kCoopThreads / d.Tg, G3 = G1 / 2;
-    if (G3 < 1 || kCoopThreads % d.Tg != 0 || fs.nf != 2) return cudaErrorInvalidConfiguration;
-    const long n1 = (long)fs.nf * ((d.KX + G1 - 1) / G1), n2 = (d.rows + G1 - 1) / G1, n3 = (d.KX + G3 - 1) / G3;
-    const size_t smem = (size_t)G1 * d.M * sizeof(VT);
-    // no more CTAs than are resident at once (a cooperative launch beyond it fails)
-    int occ = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_stage_coop<T>, kCoopThreads, smem);
-    if (e != cudaSuccess) return e;
-    if (occ < 1) return cudaErrorInvalidConfiguration;
-    const int grid = (int)std::max<long>(1, std::min<long>(std::max(n1, std::max(n2, n3)), (long)occ * max_ctas));
-    e = cudaMemsetAsync(bar, 0, sizeof(unsigned int), st);
-    if (e != cudaSuccess) return e;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(kCoopThreads);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeCooperative;
-    at[0].val.cooperative = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    return cudaLaunchKernelEx(&cfg, k_stage_coop<T>, d, (const VT*)Sin, rk2, fs, (VT*)Iu, (VT*)Iv, (VT*)S0,
-                              (VT*)S1, (VT*)Sdw, (const VT*)src, stage, dt, ph, (const VT*)tw, bar, flags);
 }
 
 template struct Kern<double>;

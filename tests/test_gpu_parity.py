@@ -439,35 +439,6 @@ def test_programmatic_launches_give_the_plain_order_bits(S2D, monkeypatch, preci
     assert np.array_equal(out["0"], out["1"])
 
 
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-@pytest.mark.parametrize("n", [16, 64, 128, 256])
-def test_one_launch_stage_gives_the_three_launch_bits(S2D, monkeypatch, precision, n):
-    """Small Basdevant runs (3/2-padded M <= 384) take each RK3 stage in one
-    cooperative launch (the three passes as phases between grid barriers,
-    the bodies of the three kernels, tiles of 128 / Tg transforms): after 20
-    steps, and for one RHS, the state is bit-identical to three launches per
-    stage (S2D_STAGE_COOP=0, read when the handle is created), and the RHS
-    matches the oracle."""
-    g = O.get_grid_size(n, n)
-    w0 = O.random_state(g, 70 + n, decay=0.1)
-    out, rhs = {}, {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("S2D_STAGE_COOP", mode)
-        with S2D(n, nu=1e-3, precision=precision) as s:
-            s.set_state(w0)
-            rhs[mode] = s.compute_rhs()
-            dt = s.compute_time_step(0.5)
-            s.integrate_steps(20, dt)
-            s.check_finite()
-            out[mode] = s.get_state()[0]
-    assert np.array_equal(out["0"], out["1"])
-    assert np.array_equal(rhs["0"], rhs["1"])
-    if precision == "fp64":
-        w, p = _oracle_state(w0, g)
-        ref, _ = O.compute_rhs(w, p, g, 1e-3, round_trip=False)
-        assert O.rel_l2(rhs["1"], O.truncate(ref, g)) < 1e-13
-
-
 @pytest.mark.parametrize("n", [64, 96, 256])
 @pytest.mark.parametrize("plan", [0, 1, 2])
 def test_every_radix_plan_vs_oracle(S2D, n, plan):
