@@ -111,12 +111,9 @@ cudaError_t round_to_f32(const double* in, float* out, long n, cudaStream_t st) 
 
 // join: an event on another stream that the epilogue (the first kernel that
 // reads h->src) waits for; the kernels before it run concurrently with that
-// stream's work.  k1_done: this stage's inverse y-pass ran inside the
-// previous stage's K3; fuse_next: this stage's K3 runs the next stage's
-// inverse y-pass too (fusable(): FP32 single runs, stages 1 and 2).
+// stream's work
 template <typename T>
-int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr,
-                     bool k1_done = false, bool fuse_next = false) {
+int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr) {
     const Dims& d = h->d;
     const bool bas = h->ph.form == S2D_NL_BASDEVANT;
     FieldSet fs{};
@@ -134,7 +131,7 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
     fs.out[2] = h->I[2];
     const void* win = (stage <= 1) ? h->S0 : h->S1;
     if (ev) S2D_CUDA(cudaEventRecord(ev[0], h->stream));
-    if (!k1_done) S2D_CUDA(Kern<T>::yinv(d, win, bas ? h->rk2s : h->rk2, fs, h->tw, h->stream, h->L_yinv));
+    S2D_CUDA(Kern<T>::yinv(d, win, bas ? h->rk2s : h->rk2, fs, h->tw, h->stream, h->L_yinv));
     if (ev) S2D_CUDA(cudaEventRecord(ev[1], h->stream));
     if (bas) S2D_CUDA(Kern<T>::xpass_bas(d, h->I[0], h->I[1], h->tw, h->stream, h->L_xrow, true));
     else S2D_CUDA(Kern<T>::xpass_rhs(d, h->I[0], h->I[1], h->I[2], h->tw, h->stream, h->L_xpass));
@@ -154,31 +151,20 @@ int launch_rhs_stage(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaE
             S2D_CUDA(cudaStreamWaitEvent(h->stream, join, 0));
             L.pdl = false;
         }
-        if (fuse_next)
-            S2D_CUDA(Kern<T>::yfwd_rk3_yinv(d, h->I[0], h->I[1], h->S0, h->S1, h->src, stage, dt, h->ph, h->tw,
-                                            h->flags, h->rk2s, fs, h->stream, L));
-        else
-            S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph,
-                                       h->tw, h->flags, h->stream, L));
+        S2D_CUDA(Kern<T>::yfwd_rk3(d, h->I[0], h->I[1], h->S0, h->S1, h->Sdw, h->src, stage, dt, h->ph, h->tw,
+                                   h->flags, h->stream, L));
     }
     if (ev) S2D_CUDA(cudaEventRecord(ev[3], h->stream));
     return S2D_OK;
 }
 
-int launch_rhs_stage_any(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr,
-                         bool k1_done = false, bool fuse_next = false) {
-    return h->prec == S2D_FP64 ? launch_rhs_stage<double>(h, stage, dt, ev, join, k1_done, fuse_next)
-                               : launch_rhs_stage<float>(h, stage, dt, ev, join, k1_done, fuse_next);
+int launch_rhs_stage_any(s2d_handle* h, int stage, double dt, cudaEvent_t* ev, cudaEvent_t join = nullptr) {
+    return h->prec == S2D_FP64 ? launch_rhs_stage<double>(h, stage, dt, ev, join)
+                               : launch_rhs_stage<float>(h, stage, dt, ev, join);
 }
 
-// K3 of stages 1 and 2 fused with the next stage's K1: FP32 single runs of
-// the Basdevant form whose K3 is one launch (S2D_FUSE_K3K1=0: apart)
-bool fusable(const s2d_handle* h) { return h->fuse_k3k1 && h->prec == S2D_FP32 && !h->Fv &&
-                                           h->ph.form == S2D_NL_BASDEVANT && h->L_yfwd.threads >= h->L_yfwd.G * h->d.Tg; }
-
 int launch_step(s2d_handle* h, double dt) {
-    const bool f = fusable(h);
-    for (int s = 1; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr, nullptr, f && s > 1, f && s < 3));
+    for (int s = 1; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr));
     return S2D_OK;
 }
 
@@ -634,8 +620,6 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
         const char* e = std::getenv("S2D_PDL");
         const bool pdl = !(e && e[0] == '0');
         for (Launch* L : {&h->L_yinv, &h->L_xpass, &h->L_yfwd, &h->L_xrow, &h->L_ystore, &h->L_ycol}) L->pdl = pdl;
-        const char* f = std::getenv("S2D_FUSE_K3K1");
-        h->fuse_k3k1 = !(f && f[0] == '0');
     }
 
     if (cudaStreamSynchronize(h->stream) != cudaSuccess) return bail(fail(S2D_ERR_CUDA, "setup failed"));
@@ -647,9 +631,8 @@ int s2d::create_handle(const s2d_config* cfg, cudaStream_t ext_stream, s2d_handl
 // first stage's inverse y-pass and x-pass run concurrently with that work,
 // its epilogue waits for src_ready.
 int s2d::launch_step_sourced(s2d_handle* h, double dt, cudaEvent_t src_ready) {
-    const bool f = fusable(h);
-    S2D_TRY(launch_rhs_stage_any(h, 1, dt, nullptr, src_ready, false, f));
-    for (int s = 2; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr, nullptr, f, f && s < 3));
+    S2D_TRY(launch_rhs_stage_any(h, 1, dt, nullptr, src_ready));
+    for (int s = 2; s <= 3; ++s) S2D_TRY(launch_rhs_stage_any(h, s, dt, nullptr));
     return S2D_OK;
 }
 

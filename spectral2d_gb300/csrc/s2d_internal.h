@@ -172,11 +172,6 @@ struct Kern {
     static cudaError_t yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, void* S0, void* S1,
                                 void* Sdw, const void* src, int stage, double dt, const Phys& ph,
                                 const void* tw, unsigned int* flags, cudaStream_t st, const Launch& L);
-    // K3 of stage 1 or 2 and K1 of the next stage in one launch (the state
-    // written to S1 and read back per column); same bits as the two launches
-    static cudaError_t yfwd_rk3_yinv(const Dims& d, void* Iu, void* Iv, void* S0, void* S1, const void* src,
-                                     int stage, double dt, const Phys& ph, const void* tw, unsigned int* flags,
-                                     const double* rk2, const FieldSet& fs, cudaStream_t st, const Launch& L);
     // K3 in two launches: forward y-FFT of the columns of both products into
     // compact arrays Fu, Fv, then the epilogue (dW, stage update, Truncate)
     static cudaError_t yfwd_col(const Dims& d, const void* Iu, const void* Iv, void* Fu, void* Fv,
@@ -268,7 +263,6 @@ struct s2d_handle {
     // no FP64 conversion
     float* fu32 = nullptr;
     float* fv32 = nullptr;
-    bool fuse_k3k1 = true;   // S2D_FUSE_K3K1=0 at creation: K3 and the next stage's K1 apart
     void* tw = nullptr;
     double* ref_stage = nullptr;   // reference-layout staging (2 arrays)
     size_t ref_bytes = 0;          // bytes of one reference-layout array

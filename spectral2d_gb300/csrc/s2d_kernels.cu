@@ -98,33 +98,6 @@ __global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>)) k_yfwd_rk3
     if (bad && flags) atomicOr(flags, 1u);   // flags may be null: no non-finite report
 }
 
-// K3 of one stage fused with K1 of the next (FP32 single runs, stages 1 and
-// 2): a CTA takes its G columns through the forward y-FFTs and the stage
-// update (writing the new state column, S1), then, from those values (its
-// own global stores, read back after a CTA barrier), through the next
-// stage's u, v factors and inverse y-FFTs into the same columns of Iu, Iv,
-// which it read at the start.  The bodies of the two kernels, so the same
-// bits, one launch and one state-column read fewer per stage.
-template <typename T, int B>
-__global__ void __launch_bounds__(kMaxThreads<B>, (kMinBlocks<T, B>))
-    k_yfwd_rk3_yinv(Dims d, typename Vec<T>::t* Iu, typename Vec<T>::t* Iv, typename Vec<T>::t* S0,
-                    typename Vec<T>::t* S1, const typename Vec<T>::t* __restrict__ src, int stage, double dt,
-                    Phys ph, const typename Vec<T>::t* __restrict__ tw, int G, const double* __restrict__ rk2,
-                    FieldSet fs, unsigned int* flags) {
-    using VT = typename Vec<T>::t;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    pdl_enter();
-    VT* bufs = reinterpret_cast<VT*>(smem_raw);
-    const bool bad = yfwd_body<T>(d, Iu, Iv, S0, S1, nullptr, src, stage, dt, ph, tw, G, blockIdx.x, bufs);
-    if (bad && flags) atomicOr(flags, 1u);
-    __syncthreads();   // the new state column is in global memory, visible to the CTA
-    const int ncg = (d.KX + G - 1) / G;
-    for (int f = 0; f < fs.nf; ++f) {
-        yinv_body<T>(d, S1, rk2, fs, tw, G, f * ncg + (int)blockIdx.x, bufs);
-        __syncthreads();
-    }
-}
-
 // K3 split in two (FP64 single runs): forward y-FFT of one field's columns
 // into a compact array, then the epilogue of every mode.
 template <typename T, int B>
@@ -726,20 +699,6 @@ cudaError_t Kern<T>::yfwd_rk3(const Dims& d, const void* Iu, const void* Iv, voi
 }
 
 template <typename T>
-cudaError_t Kern<T>::yfwd_rk3_yinv(const Dims& d, void* Iu, void* Iv, void* S0, void* S1, const void* src,
-                                   int stage, double dt, const Phys& ph, const void* tw, unsigned int* flags,
-                                   const double* rk2, const FieldSet& fs, cudaStream_t st, const Launch& L) {
-    using VT = typename Vec<T>::t;
-    const int nb = (d.KX + L.G - 1) / L.G;
-    if (stage < 1 || stage > 2 || L.threads < L.G * d.Tg) return cudaErrorInvalidConfiguration;
-    if (budget<T>(L.threads) == 1)
-        return launch_k(k_yfwd_rk3_yinv<T, 1>, nb, L.threads, L.smem, st, L.pdl, d, (VT*)Iu, (VT*)Iv, (VT*)S0,
-                        (VT*)S1, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G, rk2, fs, flags);
-    return launch_k(k_yfwd_rk3_yinv<T, 0>, nb, L.threads, L.smem, st, L.pdl, d, (VT*)Iu, (VT*)Iv, (VT*)S0,
-                    (VT*)S1, (const VT*)src, stage, dt, ph, (const VT*)tw, L.G, rk2, fs, flags);
-}
-
-template <typename T>
 cudaError_t Kern<T>::yfwd_col(const Dims& d, const void* Iu, const void* Iv, void* Fu, void* Fv, const void* tw,
                               cudaStream_t st, const Launch& L) {
     using VT = typename Vec<T>::t;
@@ -930,8 +889,6 @@ cudaError_t configure_kernels(int max_smem_optin) {
     S2D_SET((k_yfwd_rk3<double, 0>));
     S2D_SET((k_yfwd_rk3<float, 0>));
     S2D_SET((k_yfwd_rk3<float, 1>));
-    S2D_SET((k_yfwd_rk3_yinv<float, 1>));
-    S2D_SET((k_yfwd_rk3_yinv<float, 0>));
     S2D_SET(k_xinv_cfl<double>);
     S2D_SET(k_xinv_moments<double>);
     S2D_SET(k_xinv_moments<float>);

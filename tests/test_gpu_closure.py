@@ -399,28 +399,6 @@ def test_les_closure_fused_network_matches_layerwise(S, precision):
     assert np.array_equal(out[("single", False)], out[("batch", False)][0])
 
 
-def test_les_closure_step_with_fused_k3_k1_gives_the_separate_launch_bits(S, monkeypatch):
-    """The FP32 LES step with the closure on a second stream: K3 of stages 1
-    and 2 fused with the next K1 (stage 1's after the join on the closure
-    term) gives the bits of the separate launches."""
-    n, nu, steps, dt = 128, 1e-3, 6, 2e-3
-    w0 = O.random_state(O.get_grid_size(n, n), 41, decay=0.2)
-    out = {}
-    with S.ClosureNet(192, max_batch=1, seed=13) as net:
-        net.set_scales([1.0, 1.0, 0.05])
-        for mode in ("0", "1"):
-            monkeypatch.setenv("S2D_FUSE_K3K1", mode)
-            with S.Spectral2D(n, nu=nu, precision="fp32") as a:
-                a.set_state(w0)
-                S.les_set_closure(a, net)
-                S.les_integrate_steps(a, steps, dt)
-                out[mode] = a.get_state()[0]
-                S.les_set_closure(a, None)
-        net.status()
-    assert np.all(np.isfinite(out["1"]))
-    assert np.array_equal(out["0"], out["1"])
-
-
 def test_trained_closure_beats_the_closure_free_les(S):
     """The packaged closure (trained on the FP64 2048^2 DNS of seeds 0-7)
     against the closure-free 128^2 LES on held-out seed 9: both start from

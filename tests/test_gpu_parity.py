@@ -439,27 +439,6 @@ def test_programmatic_launches_give_the_plain_order_bits(S2D, monkeypatch, preci
     assert np.array_equal(out["0"], out["1"])
 
 
-@pytest.mark.parametrize("n", [16, 96, 256, 2048])
-def test_fused_k3_and_next_k1_give_the_separate_launch_bits(S2D, monkeypatch, n):
-    """FP32 single runs fuse K3 of stages 1 and 2 with the next stage's K1
-    (one launch per column group: forward y-FFTs, stage update, then the new
-    state column back through the u, v factors and the inverse y-FFTs): the
-    state after 10 steps is bit-identical to the separate launches
-    (S2D_FUSE_K3K1=0, read when the handle is created)."""
-    g = O.get_grid_size(n, n)
-    w0 = O.random_state(g, 80 + n, decay=0.1)
-    out = {}
-    for mode in ("0", "1"):
-        monkeypatch.setenv("S2D_FUSE_K3K1", mode)
-        with S2D(n, nu=1e-3, precision="fp32") as s:
-            s.set_state(w0)
-            dt = s.compute_time_step(0.5)
-            s.integrate_steps(10, dt)
-            s.check_finite()
-            out[mode] = s.get_state()[0]
-    assert np.array_equal(out["0"], out["1"])
-
-
 @pytest.mark.parametrize("n", [64, 96, 256])
 @pytest.mark.parametrize("plan", [0, 1, 2])
 def test_every_radix_plan_vs_oracle(S2D, n, plan):
