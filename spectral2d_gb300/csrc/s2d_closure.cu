@@ -517,18 +517,22 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
 // 4 KB of activations from shared memory for only 32 columns), and output
 // pixel m takes column block dx at pixel m + dx - 1, a warp shuffle.
 // One CTA per SM (the cooperative limit): warp 17 issues the TMA loads of
-// the boxes into eight slots, warp 16 the MMAs of a tile into one of four
+// the boxes into four slots, warp 16 the MMAs of a tile into one of four
 // tensor-memory accumulators (descriptors precomputed per slot: a row of
 // taps is an offset of the start address), and two groups of eight warps
 // take alternate tiles: read the accumulator, release it (mbarrier), sum the
 // taps, apply bias and GELU and store, while the MMAs of the following tiles
-// run.  The roles
-// meet only at mbarriers: full (slot landed), slotfree (its MMAs done),
-// mmad (accumulator ready), accfree (accumulator read).  Every wait is bounded: a wait that runs out sets bit 4 of *err and
+// run.  The roles meet only at mbarriers: full (slot landed), mmad (its MMAs
+// done: the accumulator ready, the slot free), accfree (accumulator read).
+// Every wait is bounded: a wait that runs out sets bit 4 of *err and
 // the abort flag, the CTA skips the rest (after bounded waits for its copies
 // and MMAs in flight) and frees its tensor memory.
-constexpr int kNetGroups = 2;                    // epilogue groups of 8 warps
-constexpr int kNetAcc = 4;                       // accumulators (tile i: i % 4, group i % 2)
+constexpr int kNetGroups = 2;                    // epilogue groups of 8 warps (tile i: group i % 2)
+// Accumulators = box slots: tile i uses slot and accumulator i % 4, and one
+// commit per tile (mmad) tells the epilogue the accumulator is ready and the
+// producer the slot is free (a tcgen05.commit costs the tensor pipe about as
+// much as three of these MMAs, so there is one per tile, not two).
+constexpr int kNetAcc = 4;
 constexpr int kNetEpiWarps = 8 * kNetGroups;     // warps 0-15
 constexpr int kNetMmaWarp = kNetEpiWarps;        // warp 16
 constexpr int kNetProdWarp = kNetEpiWarps + 1;   // warp 17
@@ -537,7 +541,7 @@ constexpr int kNetAccCols = 128;                 // 3 * 32 columns used
 constexpr int kNetTmemCols = kNetAccCols * kNetAcc;
 constexpr int kNetOutH = 8, kNetOutW = 14;       // output tile
 constexpr int kNetBoxRows = kNetOutH + 2, kNetBoxW = kNetOutW + 2;   // its halo box: M = 8 x 16 = 128 pixels
-constexpr int kNetSlots = 8;
+constexpr int kNetSlots = kNetAcc;
 constexpr int kNetSlotBytes = kNetBoxRows * kNetBoxW * 64;   // one box of 32-channel pixels
 constexpr int kNetWBytes = 3 * 96 * 4 * 16;                  // B operands of the three rows of taps
 constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
@@ -555,8 +559,7 @@ struct NetArgs {
 
 struct NetShared {
     uint64_t full[kNetSlots];   // the boxes of a slot have landed
-    uint64_t slotfree[kNetSlots];   // the MMAs that read a slot are complete
-    uint64_t mmad[kNetAcc];     // the MMAs into an accumulator are complete
+    uint64_t mmad[kNetAcc];     // the MMAs of the tile in slot / accumulator are complete
     uint64_t accfree[kNetAcc];  // the 8 warps of its epilogue group have read an accumulator
     uint32_t tmem;
     int abort;
@@ -665,6 +668,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
     if (warp == kNetProdWarp) {
         // ---- TMA producer (one thread): one box per tile into slot
         // i % kNetSlots once the MMAs of tile i - kNetSlots have read it
+        // (their commit on mmad, the slot's accumulator)
         if (lane == 0 && !*abort) {
             asm volatile("fence.proxy.async.global;\n" ::: "memory");
             int kl = 0;
@@ -672,7 +676,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
             for (; kl < nk; ++kl) {
                 const int i = i0 + kl, s = i % kNetSlots;
                 if (i >= kNetSlots &&
-                    !(ok = net_wait(smem_u32(&sh.slotfree[s]), (uint32_t)(i / kNetSlots - 1) & 1u, abort)))
+                    !(ok = net_wait(smem_u32(&sh.mmad[s]), (uint32_t)(i / kNetSlots - 1) & 1u, abort)))
                     break;
                 int b, ox0, oy0;
                 tile_xy(kl, b, ox0, oy0);
@@ -693,7 +697,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         // ---- MMA issuer (one thread): per tile 3 * KC / 16 MMAs of
         // M = 128 box pixels, N = 3 NC (the three column taps side by side),
         // K = 16 channels, one per row of taps dy and channel step, into
-        // accumulator i % 4; committed to mmad (epilogue) and slotfree
+        // accumulator i % 4; one commit to mmad (epilogue and producer)
         if (lane == 0 && !*abort) {
             const uint64_t bd0 = umma_desc(bw, CORE, WGROUP);
             constexpr uint32_t idesc = umma_idesc_bf16(128, N);
@@ -726,10 +730,6 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
                 asm volatile(
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
                         smem_u32(&sh.mmad[acc]))
-                    : "memory");
-                asm volatile(
-                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                        smem_u32(&sh.slotfree[s]))
                     : "memory");
                 km = k;
             }
@@ -844,7 +844,6 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
     if (tid == 0) {
         for (int s = 0; s < kNetSlots; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.slotfree[s])) : "memory");
         }
         for (int s = 0; s < kNetAcc; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
