@@ -783,26 +783,29 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
             for (int t = 0; t < 2; ++t) {
                 const int s = (i0 + k + t) % kNetSlots;
                 if (cols && k + t < nk) {
-                    uint32_t r[3][16];
+                    // one tap block at a time (dx = 0, -1, +1): 16 values live
+                    const uint32_t tbase =
+                        sh.tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(s * kNetAccCols + half * 16);
 #pragma unroll
-                    for (int dxi = 0; dxi < 3; ++dxi) {
-                        const uint32_t taddr = sh.tmem + ((uint32_t)(quarter * 32) << 16) +
-                                               (uint32_t)(s * kNetAccCols + dxi * NC + half * 16);
+                    for (int o = 0; o < 3; ++o) {
+                        const int dxi = o == 0 ? 1 : (o == 1 ? 0 : 2);
+                        uint32_t r[16];
                         asm volatile(
                             "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
                             "%14,%15}, [%16];\n"
-                            : "=r"(r[dxi][0]), "=r"(r[dxi][1]), "=r"(r[dxi][2]), "=r"(r[dxi][3]), "=r"(r[dxi][4]),
-                              "=r"(r[dxi][5]), "=r"(r[dxi][6]), "=r"(r[dxi][7]), "=r"(r[dxi][8]), "=r"(r[dxi][9]),
-                              "=r"(r[dxi][10]), "=r"(r[dxi][11]), "=r"(r[dxi][12]), "=r"(r[dxi][13]),
-                              "=r"(r[dxi][14]), "=r"(r[dxi][15])
-                            : "r"(taddr));
-                    }
-                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+                              "=r"(r[14]), "=r"(r[15])
+                            : "r"(tbase + (uint32_t)(dxi * NC)));
+                        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 #pragma unroll
-                    for (int e = 0; e < 16; ++e)
-                        z[t][e] = __shfl_up_sync(0xffffffffu, __uint_as_float(r[0][e]), 1, kNetBoxW) +
-                                  __uint_as_float(r[1][e]) +
-                                  __shfl_down_sync(0xffffffffu, __uint_as_float(r[2][e]), 1, kNetBoxW);
+                        for (int e = 0; e < 16; ++e) {
+                            const float v = __uint_as_float(r[e]);
+                            if (o == 0) z[t][e] = v;
+                            else if (o == 1) z[t][e] += __shfl_up_sync(0xffffffffu, v, 1, kNetBoxW);
+                            else z[t][e] += __shfl_down_sync(0xffffffffu, v, 1, kNetBoxW);
+                        }
+                    }
                 }
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -849,11 +852,11 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
     irun = i0 + nkp;
 }
 
-// 112 registers at most (one CTA of 576 threads per SM): the epilogue holds
-// both tiles' tap sums of a pair.
-__global__ void __maxnreg__(112) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
-                                           const __grid_constant__ CUtensorMap m_a0,
-                                           const __grid_constant__ CUtensorMap m_a1, NetArgs a) {
+// One CTA of 576 threads per SM: 96 registers a thread (five warps share a
+// sub-partition's 16K registers).
+__global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
+                                                          const __grid_constant__ CUtensorMap m_a0,
+                                                          const __grid_constant__ CUtensorMap m_a1, NetArgs a) {
     extern __shared__ __align__(1024) unsigned char net_smem[];
     __shared__ NetShared sh;
     const uint32_t sraw = smem_u32(net_smem);
