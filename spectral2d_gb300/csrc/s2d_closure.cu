@@ -559,8 +559,8 @@ struct NetArgs {
 
 struct NetShared {
     uint64_t full[kNetSlots];   // the boxes of a slot have landed
-    uint64_t mmad[2];           // pair P % 2: the MMAs of both tiles are complete
-    uint64_t accfree[2];        // pair P % 2: its epilogue group has read both accumulators
+    uint64_t mmad[kNetAcc];     // the MMAs of the tile in slot / accumulator are complete
+    uint64_t accfree[kNetAcc];  // the 8 warps of its epilogue group have read an accumulator
     uint32_t tmem;
     int abort;
     float bias[32];
@@ -665,34 +665,24 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         atomicOr(a.err, 4u);
     };
 
-    // Tiles go in pairs (running indices 2P, 2P + 1; a layer's count is
-    // rounded up to even with a dummy tile that loads and computes nothing):
-    // one tcgen05.commit per pair on mmad[P % 2] -- a commit holds back the
-    // tensor pipe for about three MMAs' time -- tells epilogue group P % 2
-    // that both accumulators are ready and the producer that both slots are
-    // free.  Slot and accumulator of tile i: i % 4.
-    const int nkp = nk + (nk & 1);
     if (warp == kNetProdWarp) {
-        // ---- TMA producer (one thread): one box per tile into slot i % 4
-        // once the pair that last used the slot (tile i - 4) has committed
+        // ---- TMA producer (one thread): one box per tile into slot
+        // i % kNetSlots once the MMAs of tile i - kNetSlots have read it
+        // (their commit on mmad, the slot's accumulator)
         if (lane == 0 && !*abort) {
             asm volatile("fence.proxy.async.global;\n" ::: "memory");
             int kl = 0;
             bool ok = true;
-            for (; kl < nkp; ++kl) {
+            for (; kl < nk; ++kl) {
                 const int i = i0 + kl, s = i % kNetSlots;
                 if (i >= kNetSlots &&
-                    !(ok = net_wait(smem_u32(&sh.mmad[((i - 4) >> 1) & 1]), (uint32_t)((i - 4) >> 2) & 1u, abort)))
+                    !(ok = net_wait(smem_u32(&sh.mmad[s]), (uint32_t)(i / kNetSlots - 1) & 1u, abort)))
                     break;
+                int b, ox0, oy0;
+                tile_xy(kl, b, ox0, oy0);
                 const uint32_t bar = smem_u32(&sh.full[s]);
-                if (kl < nk) {
-                    int b, ox0, oy0;
-                    tile_xy(kl, b, ox0, oy0);
-                    mbar_expect_tx(bar, (uint32_t)BOX);
-                    tma_load_4d(sbase + s * kNetSlotBytes, tin, 0, ox0, oy0, b, bar);
-                } else {
-                    mbar_arrive(bar);   // the dummy tile: its slot phase completes at once
-                }
+                mbar_expect_tx(bar, (uint32_t)BOX);
+                tma_load_4d(sbase + s * kNetSlotBytes, tin, 0, ox0, oy0, b, bar);
             }
             if (!ok) {
                 fail();
@@ -707,61 +697,53 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         // ---- MMA issuer (one thread): per tile 3 * KC / 16 MMAs of
         // M = 128 box pixels, N = 3 NC (the three column taps side by side),
         // K = 16 channels, one per row of taps dy and channel step, into
-        // accumulator i % 4; one commit per pair
+        // accumulator i % 4; one commit to mmad (epilogue and producer)
         if (lane == 0 && !*abort) {
             const uint64_t bd0 = umma_desc(bw, CORE, WGROUP);
             constexpr uint32_t idesc = umma_idesc_bf16(128, N);
-            int pm = (i0 >> 1) - 1;   // the last pair committed (running index)
+            int km = -1;
             bool ok = true;
-            for (int k = 0; k < nkp && ok; k += 2) {
-                const int P = (i0 + k) >> 1, q = P & 1;
-                if (P >= 2 && !(ok = net_wait(smem_u32(&sh.accfree[q]), (uint32_t)((P >> 1) - 1) & 1u, abort)))
+            for (int k = 0; k < nk; ++k) {
+                const int i = i0 + k, s = i % kNetSlots, acc = i % kNetAcc;
+                if (!(ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort))) break;
+                if (i >= kNetAcc &&
+                    !(ok = net_wait(smem_u32(&sh.accfree[acc]), (uint32_t)(i / kNetAcc - 1) & 1u, abort)))
                     break;
-                for (int t = 0; t < 2; ++t) {
-                    const int i = i0 + k + t, s = i % kNetSlots;
-                    if (!(ok = net_wait(smem_u32(&sh.full[s]), (uint32_t)(i / kNetSlots) & 1u, abort))) break;
-                    if (k + t >= nk) continue;   // the dummy tile
-                    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-                    const uint64_t ad0 = umma_desc_sw<ROWB>(sbase + s * kNetSlotBytes);
-                    const uint32_t dacc = sh.tmem + (uint32_t)(s * kNetAccCols);
+                asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+                const uint64_t ad0 = umma_desc_sw<ROWB>(sbase + s * kNetSlotBytes);
+                const uint32_t dacc = sh.tmem + (uint32_t)(acc * kNetAccCols);
 #pragma unroll
-                    for (int dyi = 0; dyi < 3; ++dyi) {
+                for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
-                        for (int j = 0; j < KC / 16; ++j) {
-                            // box rows dyi .. dyi + 7 (whole 8-pixel atoms); start
-                            // addresses advance in 16-byte units in the low field
-                            const uint64_t ad = ad0 + (uint64_t)((dyi * kNetBoxW * ROWB + j * 32) >> 4);
-                            const uint64_t bd = bd0 + (uint64_t)((dyi * NG * WGROUP + j * 2 * CORE) >> 4);
-                            asm volatile(
-                                "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-                                " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
-                                "l"(ad), "l"(bd), "r"(idesc), "r"((dyi | j) ? 1u : 0u)
-                                : "memory");
-                        }
+                    for (int j = 0; j < KC / 16; ++j) {
+                        // box rows dyi .. dyi + 7 (whole 8-pixel atoms); start
+                        // addresses advance in 16-byte units in the low field
+                        const uint64_t ad = ad0 + (uint64_t)((dyi * kNetBoxW * ROWB + j * 32) >> 4);
+                        const uint64_t bd = bd0 + (uint64_t)((dyi * NG * WGROUP + j * 2 * CORE) >> 4);
+                        asm volatile(
+                            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+                            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dacc),
+                            "l"(ad), "l"(bd), "r"(idesc), "r"((dyi | j) ? 1u : 0u)
+                            : "memory");
                     }
                 }
-                if (!ok) break;
                 asm volatile(
                     "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                        smem_u32(&sh.mmad[q]))
+                        smem_u32(&sh.mmad[acc]))
                     : "memory");
-                pm = P;
+                km = k;
             }
             if (!ok) {
                 fail();
-                // a pair's MMAs issued but not committed are waited for by a
-                // commit of their own; the last commit covers everything before
-                asm volatile(
-                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-                        smem_u32(&sh.mmad[(pm + 1) & 1]))
-                    : "memory");
-                mbar_wait_bounded(smem_u32(&sh.mmad[(pm + 1) & 1]), (uint32_t)(((pm + 1) >> 1)) & 1u);
+                if (km >= 0) {
+                    const int i = i0 + km;
+                    mbar_wait_bounded(smem_u32(&sh.mmad[i % kNetAcc]), (uint32_t)(i / kNetAcc) & 1u);
+                }
             }
         }
     } else {
-        // ---- epilogue warps: group g = w / 8 takes the pairs with P % 2 == g
-        // (both tiles: their accumulators, then bias, GELU, stores); warp w
-        // reads accumulator lanes 32 (w % 4) .. + 31 (box pixels m: row
+        // ---- epilogue warps: group g = w / 8 takes the tiles with i % 2 == g;
+        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (box pixels m: row
         // m / 16, column m % 16) and, of each tap column dx, the output
         // channels 16 ((w % 8) / 4) .. + 15.  Output pixel m sums tap dx
         // evaluated at box pixel m + dx: a shuffle within the 16 lanes of its
@@ -769,91 +751,81 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfl
         const int grp = warp >> 3, quarter = warp & 3, half = (warp >> 2) & 1;
         const bool cols = half * 16 < NC;   // warp-uniform
         const long fw = Wd + 2;
-        const float* bv = sh.bias + half * 16;   // this thread's 16 biases (shared memory)
-        for (int k = 2 * ((grp - ((i0 >> 1) & 1) + 2) & 1); k < nkp; k += 2 * kNetGroups) {
-            const int P = (i0 + k) >> 1;
-            if (!net_wait(smem_u32(&sh.mmad[P & 1]), (uint32_t)(P >> 1) & 1u, abort)) {
+        // this thread's 16 biases in registers (shared-memory reads per tile
+        // would compete with the tensor core's operand reads)
+        float bv[16];
+#pragma unroll
+        for (int e = 0; e < 16; ++e) bv[e] = cols ? sh.bias[half * 16 + e] : 0.0f;
+        for (int k = (grp - (i0 & 1) + 2) & 1; k < nk; k += kNetGroups) {
+            const int i = i0 + k, acc = i % kNetAcc;
+            if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i / kNetAcc) & 1u, abort)) {
                 fail();
                 break;
             }
             asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-            // both tiles' taps summed (the accumulators read), then released
-            float z[2][16];
+            uint32_t r[3][16];
+            if (cols) {
 #pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                const int s = (i0 + k + t) % kNetSlots;
-                if (cols && k + t < nk) {
-                    // one tap block at a time (dx = 0, -1, +1): 16 values live
-                    const uint32_t tbase =
-                        sh.tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(s * kNetAccCols + half * 16);
-#pragma unroll
-                    for (int o = 0; o < 3; ++o) {
-                        const int dxi = o == 0 ? 1 : (o == 1 ? 0 : 2);
-                        uint32_t r[16];
-                        asm volatile(
-                            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-                            "%14,%15}, [%16];\n"
-                            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-                              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-                              "=r"(r[14]), "=r"(r[15])
-                            : "r"(tbase + (uint32_t)(dxi * NC)));
-                        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-#pragma unroll
-                        for (int e = 0; e < 16; ++e) {
-                            const float v = __uint_as_float(r[e]);
-                            if (o == 0) z[t][e] = v;
-                            else if (o == 1) z[t][e] += __shfl_up_sync(0xffffffffu, v, 1, kNetBoxW);
-                            else z[t][e] += __shfl_down_sync(0xffffffffu, v, 1, kNetBoxW);
-                        }
-                    }
+                for (int dxi = 0; dxi < 3; ++dxi) {
+                    const uint32_t taddr = sh.tmem + ((uint32_t)(quarter * 32) << 16) +
+                                           (uint32_t)(acc * kNetAccCols + dxi * NC + half * 16);
+                    asm volatile(
+                        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,"
+                        "%15}, [%16];\n"
+                        : "=r"(r[dxi][0]), "=r"(r[dxi][1]), "=r"(r[dxi][2]), "=r"(r[dxi][3]), "=r"(r[dxi][4]),
+                          "=r"(r[dxi][5]), "=r"(r[dxi][6]), "=r"(r[dxi][7]), "=r"(r[dxi][8]), "=r"(r[dxi][9]),
+                          "=r"(r[dxi][10]), "=r"(r[dxi][11]), "=r"(r[dxi][12]), "=r"(r[dxi][13]), "=r"(r[dxi][14]),
+                          "=r"(r[dxi][15])
+                        : "r"(taddr));
                 }
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
             }
             asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
             __syncwarp();
-            if (lane == 0) mbar_arrive(smem_u32(&sh.accfree[P & 1]));
+            if (lane == 0) mbar_arrive(smem_u32(&sh.accfree[acc]));
             if (!cols) continue;
+
+            int b, ox0, oy0;
+            tile_xy(k, b, ox0, oy0);
+            const int m = quarter * 32 + lane;
+            const int c = m % kNetBoxW;
+            const int y = oy0 + m / kNetBoxW, x = ox0 - 1 + c;
+            const bool valid = c >= 1 && c <= kNetOutW && y < H && x < Wd;
+            float z[16];
 #pragma unroll
-            for (int t = 0; t < 2; ++t) {
-                if (k + t >= nk) break;
-                int b, ox0, oy0;
-                tile_xy(k + t, b, ox0, oy0);
-                const int m = quarter * 32 + lane;
-                const int c = m % kNetBoxW;
-                const int y = oy0 + m / kNetBoxW, x = ox0 - 1 + c;
-                const bool valid = c >= 1 && c <= kNetOutW && y < H && x < Wd;
-                if (!valid) continue;
-                if (LAST) {
-                    if (half == 0) yout[((long)b * H + y) * Wd + x] = z[t][0] + bv[0];
-                } else {
-                    uint32_t v[8];
+            for (int e = 0; e < 16; ++e)
+                z[e] = __shfl_up_sync(0xffffffffu, __uint_as_float(r[0][e]), 1, kNetBoxW) +
+                       __uint_as_float(r[1][e]) +
+                       __shfl_down_sync(0xffffffffu, __uint_as_float(r[2][e]), 1, kNetBoxW);
+            if (!valid) continue;
+            if (LAST) {
+                if (half == 0) yout[((long)b * H + y) * Wd + x] = z[0] + bv[0];
+            } else {
+                uint32_t v[8];
 #pragma unroll
-                    for (int e = 0; e < 8; ++e)
-                        v[e] = pack_bf16(gelu_f(z[t][2 * e] + bv[2 * e]), gelu_f(z[t][2 * e + 1] + bv[2 * e + 1]));
-                    const uint4 lo = make_uint4(v[0], v[1], v[2], v[3]), hi = make_uint4(v[4], v[5], v[6], v[7]);
-                    // the pixel and its copies in the frame
-                    const long img = (long)b * (H + 2) * fw;
-                    const int wy = y == 0 ? H + 1 : (y == H - 1 ? 0 : -1);
-                    const int wx = x == 0 ? Wd + 1 : (x == Wd - 1 ? 0 : -1);
-                    auto put = [&](int fy, int fx) {
-                        uint4* p = reinterpret_cast<uint4*>(out + (img + fy * fw + fx) * 32 + half * 16);
-                        p[0] = lo;
-                        p[1] = hi;
-                    };
-                    put(y + 1, x + 1);
-                    if (wy >= 0) put(wy, x + 1);
-                    if (wx >= 0) put(y + 1, wx);
-                    if (wy >= 0 && wx >= 0) put(wy, wx);
-                }
+                for (int e = 0; e < 8; ++e) v[e] = pack_bf16(gelu_f(z[2 * e] + bv[2 * e]), gelu_f(z[2 * e + 1] + bv[2 * e + 1]));
+                const uint4 lo = make_uint4(v[0], v[1], v[2], v[3]), hi = make_uint4(v[4], v[5], v[6], v[7]);
+                // the pixel and its copies in the frame
+                const long img = (long)b * (H + 2) * fw;
+                const int wy = y == 0 ? H + 1 : (y == H - 1 ? 0 : -1);
+                const int wx = x == 0 ? Wd + 1 : (x == Wd - 1 ? 0 : -1);
+                auto put = [&](int fy, int fx) {
+                    uint4* p = reinterpret_cast<uint4*>(out + (img + fy * fw + fx) * 32 + half * 16);
+                    p[0] = lo;
+                    p[1] = hi;
+                };
+                put(y + 1, x + 1);
+                if (wy >= 0) put(wy, x + 1);
+                if (wx >= 0) put(y + 1, wx);
+                if (wy >= 0 && wx >= 0) put(wy, wx);
             }
         }
         // this layer's stores are read by the next layer's TMA (async proxy)
         asm volatile("fence.proxy.async.global;\n" ::: "memory");
     }
-    irun = i0 + nkp;
+    irun = i0 + nk;
 }
 
-// One CTA of 576 threads per SM: 96 registers a thread (five warps share a
-// sub-partition's 16K registers).
 __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constant__ CUtensorMap m_in,
                                                           const __grid_constant__ CUtensorMap m_a0,
                                                           const __grid_constant__ CUtensorMap m_a1, NetArgs a) {
@@ -873,7 +845,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         for (int s = 0; s < kNetSlots; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
         }
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < kNetAcc; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&sh.accfree[s])),
                          "r"(kNetEpiWarps / kNetGroups)
