@@ -63,7 +63,12 @@ __device__ __forceinline__ int ld_acquire(const int* p) {
     return v;
 }
 
-template <typename T>
+// X32: the batch holds an FP32 run of M = 3072, whose x-pass tiles take the
+// register radix-12/16 body of the single run (k_xpass32).  That body needs
+// 128 registers in this kernel, the rest 64, so only such batches get the
+// variant that contains it (at 64 registers a 256^2 FP32 stage took 1.11
+// instead of 1.62 ms).
+template <typename T, bool X32>
 __global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict__ runs, int nruns,
                                                      const int4* __restrict__ tasks, int ntasks, int stage,
                                                      int* ctrl, int* done, unsigned int* flags) {
@@ -113,7 +118,7 @@ __global__ void __launch_bounds__(512) k_batch_stage(const RunDev<T>* __restrict
                 yinv_body<T>(R.d, stage <= 1 ? R.S0 : R.S1, R.rk2, fs, R.tw, R.G12, blk, bufs);
             } else if (ph == 1) {
                 bool done32 = false;
-                if constexpr (sizeof(T) == 4) {
+                if constexpr (sizeof(T) == 4 && X32) {
                     // FP32 rows of M = 3072: the register radix-12/16 x-pass of
                     // the single run (k_xpass32), one row per 256 threads
                     if (R.d.M == kX32M && !R.d.xgen) {
@@ -180,6 +185,7 @@ struct s2d_batch {
     s2d_cnn* cnn = nullptr;   // closure network of every run (LES batches)
     void* cl_tab = nullptr;   // its device table (closure_table)
     int stall_run = -1;       // s2d_batch_inject_stall
+    bool x32 = false;         // an FP32 run of M = 3072: the k_batch_stage variant with k_xpass32's body
 };
 
 namespace {
@@ -194,8 +200,12 @@ int berr(int code, const char* m) { return set_error(code, m); }
 
 template <typename T>
 cudaError_t launch_stage(s2d_batch* b, int stage) {
-    k_batch_stage<T><<<b->grid, b->threads, b->smem, b->stream>>>((const RunDev<T>*)b->d_runs, b->n, b->d_tasks,
-                                                                 b->ntasks, stage, b->d_ctrl, b->d_done, b->d_flags);
+    if (b->x32)
+        k_batch_stage<T, true><<<b->grid, b->threads, b->smem, b->stream>>>(
+            (const RunDev<T>*)b->d_runs, b->n, b->d_tasks, b->ntasks, stage, b->d_ctrl, b->d_done, b->d_flags);
+    else
+        k_batch_stage<T, false><<<b->grid, b->threads, b->smem, b->stream>>>(
+            (const RunDev<T>*)b->d_runs, b->n, b->d_tasks, b->ntasks, stage, b->d_ctrl, b->d_done, b->d_flags);
     return cudaGetLastError();
 }
 
@@ -259,7 +269,10 @@ int configure(s2d_batch* b, int threads, int ctas_per_sm) {
     std::vector<int4> all;
     for (int p = 0; p < 3; ++p) all.insert(all.end(), tasks[p].begin(), tasks[p].end());
     int occ = 0;
-    B_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_stage<T>, threads, smem));
+    if (b->x32)
+        B_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_stage<T, true>, threads, smem));
+    else
+        B_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_batch_stage<T, false>, threads, smem));
     if (occ < 1) return berr(S2D_ERR_UNSUPPORTED, "persistent kernel does not fit an SM");
     const int cps = ctas_per_sm > 0 ? std::min(ctas_per_sm, occ) : occ;
     B_CUDA(cudaStreamSynchronize(b->stream));
@@ -344,14 +357,17 @@ S2D_API int s2d_batch_create(int32_t nruns, const s2d_config* cfgs, s2d_batch** 
         const int r = create_handle(&cfgs[i], b->stream, &h);
         if (r != S2D_OK) return bail(r);
         b->runs.push_back(h);
+        if (h->prec == S2D_FP32 && h->d.M == kX32M && !h->d.xgen) b->x32 = true;
     }
     {
         static std::atomic<bool> attr[64];  // per device, set once the attributes are (a second setter only repeats them)
         if (b->device >= 0 && b->device < 64 && !attr[b->device]) {
             const int dyn = b->max_smem - (int)sizeof(RunDev<double>) - 64;
-            if (cudaFuncSetAttribute(k_batch_stage<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=
+            if (cudaFuncSetAttribute(k_batch_stage<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=
                     cudaSuccess ||
-                cudaFuncSetAttribute(k_batch_stage<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=
+                cudaFuncSetAttribute(k_batch_stage<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=
+                    cudaSuccess ||
+                cudaFuncSetAttribute(k_batch_stage<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) !=
                     cudaSuccess)
                 return bail(berr(S2D_ERR_CUDA, "cudaFuncSetAttribute failed"));
             attr[b->device] = true;
