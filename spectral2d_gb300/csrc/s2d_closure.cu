@@ -543,16 +543,8 @@ constexpr int kNetOutH = 8, kNetOutW = 14;       // output tile
 constexpr int kNetBoxRows = kNetOutH + 2, kNetBoxW = kNetOutW + 2;   // its halo box: M = 8 x 16 = 128 pixels
 constexpr int kNetSlots = kNetAcc;
 constexpr int kNetSlotBytes = kNetBoxRows * kNetBoxW * 64;   // one box of 32-channel pixels
-// B operands of the three rows of taps of one layer (at most 3 dy x 96
-// columns x 32 channels x 2 bytes), two buffers: layer L + 1's image is
-// bulk-copied into one while layer L runs from the other.
-constexpr int kNetWBytes = 3 * 96 * 32 * 2;
-// byte offset of layer L's image in the pre-permuted weight image (9216 bytes
-// for the 16 -> 32 and 32 -> 16 layers, 18432 for the hidden ones)
-__host__ __device__ constexpr int net_woff(int L) {
-    return L == 0 ? 0 : (L <= 5 ? 9216 + (L - 1) * 18432 : 92160);
-}
-constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + 2 * kNetWBytes + 1024;
+constexpr int kNetWBytes = 3 * 96 * 4 * 16;                  // B operands of the three rows of taps
+constexpr size_t kNetSmem = (size_t)kNetSlots * kNetSlotBytes + kNetWBytes + 1024;
 
 struct NetArgs {
     const __nv_bfloat16* W[kLayers];   // BF16 working weights W[n][t][k]
@@ -563,18 +555,15 @@ struct NetArgs {
     unsigned int* err;
     int B, H, Wd;
     int stall;                         // fault injection: CTA 0 skips its first grid-barrier arrival
-    const unsigned char* wimg;         // every layer's B operands in their shared-memory layout (net_woff)
 };
 
 struct NetShared {
     uint64_t full[kNetSlots];   // the boxes of a slot have landed
     uint64_t mmad[kNetAcc];     // the MMAs of the tile in slot / accumulator are complete
     uint64_t accfree[kNetAcc];  // the 8 warps of its epilogue group have read an accumulator
-    uint64_t wbar[2];           // a layer's weight image has landed in its buffer
     uint32_t tmem;
     int abort;
-    int wlast;                  // the last layer whose weight copy the producer issued
-    float bias[kLayers][32];
+    float bias[32];
 };
 
 __device__ __forceinline__ void mbar_arrive(uint32_t bar) {
@@ -615,38 +604,14 @@ __device__ __forceinline__ bool net_grid_sync(unsigned int* bar, unsigned int ta
     return true;
 }
 
-// The weights of one layer as the fused kernel's B operands of its three
-// rows of taps (row dy, column group g = (dx, 8 output channels), the input
-// channels K-major in core matrices), built once per weight update so that a
-// launch bulk-copies them.
-template <int KC, int NC>
-__global__ void k_net_wimage(const __nv_bfloat16* __restrict__ W, unsigned char* img) {
-    constexpr int KG = KC / 8, N = 3 * NC, NG = N / 8, CORE = 128;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 3 * N * KG; i += gridDim.x * blockDim.x) {
-        const int nl = i % 8;
-        const int kg = (i / 8) % KG;
-        const int g = (i / (8 * KG)) % NG;
-        const int dyi = i / (8 * KG * NG);
-        const int dxi = g / (NC / 8);
-        const int n = (g % (NC / 8)) * 8 + nl;
-        const int t = dyi * 3 + dxi;
-        const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
-        *reinterpret_cast<uint4*>(img + ((dyi * NG + g) * KG + kg) * CORE + nl * 16) = v;
-    }
-}
-
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
-                 "l"(src), "r"(bytes), "r"(bar)
-                 : "memory");
-}
-
 // One layer over this CTA's tiles (tile blockIdx.x + k gridDim.x); irun is
 // the CTA's running tile count over all layers, which fixes every slot,
 // accumulator and barrier phase.
 template <int KC, int NC, bool LAST>
-__device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bfloat16* out, float* yout,
-                                          const NetArgs& a, NetShared& sh, uint32_t sbase, int& irun) {
+__device__ __forceinline__ void net_layer(const CUtensorMap* tin, const __nv_bfloat16* __restrict__ W,
+                                          const float* __restrict__ bias, __nv_bfloat16* out, float* yout,
+                                          const NetArgs& a, NetShared& sh, unsigned char* gbase, uint32_t sbase,
+                                          int& irun) {
     constexpr int KG = KC / 8;                 // 8-channel groups of a pixel
     constexpr int ROWB = KC * 2;               // bytes of one pixel
     constexpr int BOX = kNetBoxRows * kNetBoxW * ROWB;
@@ -660,10 +625,29 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
     const int tiles_img = tiles_x * ((H + kNetOutH - 1) / kNetOutH);
     const int ntiles = tiles_img * a.B;
     const int nk = (int)blockIdx.x < ntiles ? (ntiles - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x : 0;
-    const uint32_t wbuf0 = sbase + kNetSlots * kNetSlotBytes;
-    const uint32_t bw = wbuf0 + (uint32_t)((L & 1) * kNetWBytes);   // this layer's weights (bulk-copied)
-    const float* lbias = sh.bias[L];
+    const uint32_t bw = sbase + kNetSlots * kNetSlotBytes;
     volatile int* abort = &sh.abort;
+
+    // the layer's weights as the B operands of the three rows of taps: for
+    // row dy, column group g = (dx, 8 output channels), the input channels
+    // K-major in core matrices (the previous layer's MMAs are all complete)
+    for (int i = tid; i < 3 * N * KG; i += blockDim.x) {
+        const int nl = i % 8;
+        const int kg = (i / 8) % KG;
+        const int g = (i / (8 * KG)) % NG;
+        const int dyi = i / (8 * KG * NG);
+        const int dxi = g / (NC / 8);
+        const int n = (g % (NC / 8)) * 8 + nl;
+        const int t = dyi * 3 + dxi;
+        const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
+        const int off = ((dyi * NG + g) * KG + kg) * CORE + nl * 16;
+        *reinterpret_cast<uint4*>(gbase + kNetSlots * kNetSlotBytes + off) = v;
+    }
+    if (tid < NC) sh.bias[tid] = bias[tid];
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+    asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
     // tile k: output rows [oy0, oy0 + 8), columns [ox0, ox0 + 14); its box is
     // image rows oy0 - 1 .. oy0 + 8 and columns ox0 - 1 .. ox0 + 14, at
@@ -687,15 +671,6 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
         // (their commit on mmad, the slot's accumulator)
         if (lane == 0 && !*abort) {
             asm volatile("fence.proxy.async.global;\n" ::: "memory");
-            // the next layer's weights into the other buffer (read by the
-            // previous layer's MMAs, which are all complete)
-            if (L + 1 < kLayers) {
-                const uint32_t wb = smem_u32(&sh.wbar[(L + 1) & 1]);
-                const uint32_t bytes = (uint32_t)(net_woff(L + 2) - net_woff(L + 1));
-                mbar_expect_tx(wb, bytes);
-                bulk_load(wbuf0 + (uint32_t)(((L + 1) & 1) * kNetWBytes), a.wimg + net_woff(L + 1), bytes, wb);
-                sh.wlast = L + 1;
-            }
             int kl = 0;
             bool ok = true;
             for (; kl < nk; ++kl) {
@@ -723,11 +698,6 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
         // M = 128 box pixels, N = 3 NC (the three column taps side by side),
         // K = 16 channels, one per row of taps dy and channel step, into
         // accumulator i % 4; one commit to mmad (epilogue and producer)
-        if (lane == 0 && !*abort &&
-            !net_wait(smem_u32(&sh.wbar[L & 1]), (uint32_t)(L >> 1) & 1u, abort)) {
-            *abort = 1;
-            atomicOr(a.err, 4u);
-        }
         if (lane == 0 && !*abort) {
             const uint64_t bd0 = umma_desc(bw, CORE, WGROUP);
             constexpr uint32_t idesc = umma_idesc_bf16(128, N);
@@ -785,7 +755,7 @@ __device__ __forceinline__ void net_layer(const CUtensorMap* tin, int L, __nv_bf
         // would compete with the tensor core's operand reads)
         float bv[16];
 #pragma unroll
-        for (int e = 0; e < 16; ++e) bv[e] = cols ? lbias[half * 16 + e] : 0.0f;
+        for (int e = 0; e < 16; ++e) bv[e] = cols ? sh.bias[half * 16 + e] : 0.0f;
         for (int k = (grp - (i0 & 1) + 2) & 1; k < nk; k += kNetGroups) {
             const int i = i0 + k, acc = i % kNetAcc;
             if (!net_wait(smem_u32(&sh.mmad[acc]), (uint32_t)(i / kNetAcc) & 1u, abort)) {
@@ -863,6 +833,7 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
     __shared__ NetShared sh;
     const uint32_t sraw = smem_u32(net_smem);
     const uint32_t sbase = (sraw + 1023u) & ~1023u;
+    unsigned char* gbase = net_smem + (sbase - sraw);
     const int tid = threadIdx.x, warp = tid >> 5;
     if (warp == kNetMmaWarp) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&sh.tmem)),
@@ -874,8 +845,6 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         for (int s = 0; s < kNetSlots; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.full[s])) : "memory");
         }
-        for (int s = 0; s < 2; ++s)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.wbar[s])) : "memory");
         for (int s = 0; s < kNetAcc; ++s) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_u32(&sh.mmad[s])) : "memory");
             asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(&sh.accfree[s])),
@@ -885,21 +854,9 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         sh.abort = 0;
     }
-    // every layer's biases (from the FP32 master parameters)
-    for (int i = tid; i < kLayers * 32; i += blockDim.x) {
-        const int l = i / 32, n = i % 32;
-        sh.bias[l][n] = n < (l == kLayers - 1 ? 16 : 32) ? a.bias[l][n] : 0.0f;   // output channels padded
-    }
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    // layer 0's weights (each later layer's are copied while the one before runs)
-    if (warp == kNetProdWarp && (tid & 31) == 0) {
-        const uint32_t wb = smem_u32(&sh.wbar[0]);
-        mbar_expect_tx(wb, (uint32_t)net_woff(1));
-        bulk_load(sbase + kNetSlots * kNetSlotBytes, a.wimg, (uint32_t)net_woff(1), wb);
-        sh.wlast = 0;
-    }
 
     int irun = 0, nbar = 0;
     auto barrier = [&]() {
@@ -912,25 +869,17 @@ __global__ void __launch_bounds__(kNetThreads, 1) k_net_fwd(const __grid_constan
         }
         __syncthreads();
     };
-    net_layer<16, 32, false>(&m_in, 0, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<16, 32, false>(&m_in, a.W[0], a.bias[0], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a0, 1, a.act[1], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a0, a.W[1], a.bias[1], a.act[1], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a1, 2, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a1, a.W[2], a.bias[2], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a0, 3, a.act[1], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a0, a.W[3], a.bias[3], a.act[1], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 32, false>(&m_a1, 4, a.act[0], nullptr, a, sh, sbase, irun);
+    net_layer<32, 32, false>(&m_a1, a.W[4], a.bias[4], a.act[0], nullptr, a, sh, gbase, sbase, irun);
     barrier();
-    net_layer<32, 16, true>(&m_a0, 5, nullptr, a.y, a, sh, sbase, irun);
-    // after an abort a weight copy may still be in flight: the last two
-    // issued (one per buffer, each its barrier's latest phase) land first
-    __syncthreads();
-    if (sh.abort && warp == kNetProdWarp && (tid & 31) == 0) {
-        const int j = sh.wlast;
-        mbar_wait_bounded(smem_u32(&sh.wbar[j & 1]), (uint32_t)(j >> 1) & 1u);
-        if (j >= 1) mbar_wait_bounded(smem_u32(&sh.wbar[(j - 1) & 1]), (uint32_t)((j - 1) >> 1) & 1u);
-    }
+    net_layer<32, 16, true>(&m_a0, a.W[5], a.bias[5], nullptr, a.y, a, sh, gbase, sbase, irun);
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
     __syncthreads();
     if (warp == kNetMmaWarp)
@@ -1726,7 +1675,6 @@ struct s2d_cnn {
     __nv_bfloat16* X0f = nullptr;
     __nv_bfloat16* F[2] = {};
     unsigned int* netbar = nullptr;
-    unsigned char* Wimg = nullptr;   // k_net_wimage: every layer's operands in the kernel's layout
 };
 
 namespace {
@@ -1748,13 +1696,6 @@ int refresh_all(s2d_cnn* c) {
                                                            c->WTb[l]);
         C_CUDA(cudaGetLastError());
     }
-    if (c->Wimg) {   // the fused forward's weight image, from the new BF16 weights
-        k_net_wimage<16, 32><<<8, 256, 0, c->stream>>>(c->Wb[0], c->Wimg + net_woff(0));
-        for (int l = 1; l < kLayers - 1; ++l)
-            k_net_wimage<32, 32><<<8, 256, 0, c->stream>>>(c->Wb[l], c->Wimg + net_woff(l));
-        k_net_wimage<32, 16><<<8, 256, 0, c->stream>>>(c->Wb[kLayers - 1], c->Wimg + net_woff(kLayers - 1));
-        C_CUDA(cudaGetLastError());
-    }
     return S2D_OK;
 }
 
@@ -1771,16 +1712,14 @@ int ensure_net_buffers(s2d_cnn* c) {
               cudaMemset(c->X0f, 0, fp * 16 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->F[0], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
               cudaMalloc(&c->F[1], fp * 32 * sizeof(__nv_bfloat16)) == cudaSuccess &&
-              cudaMalloc(&c->netbar, 64) == cudaSuccess && cudaMalloc(&c->Wimg, net_woff(kLayers)) == cudaSuccess;
+              cudaMalloc(&c->netbar, 64) == cudaSuccess;
     if (!ok) {
         cudaFree(c->X0f);
         cudaFree(c->F[0]);
         cudaFree(c->F[1]);
         cudaFree(c->netbar);
-        cudaFree(c->Wimg);
         c->X0f = c->F[0] = c->F[1] = nullptr;
         c->netbar = nullptr;
-        c->Wimg = nullptr;
         return cerr(S2D_ERR_NOMEM, "cudaMalloc failed (fused network buffers)");
     }
     return S2D_OK;
@@ -1814,7 +1753,6 @@ int forward_fused(s2d_cnn* c, int B, bool input_framed) {
     a.H = H;
     a.Wd = Wd;
     a.stall = c->net_stall ? 1 : 0;
-    a.wimg = c->Wimg;
     const long ntiles = (long)((Wd + kNetOutW - 1) / kNetOutW) * ((H + kNetOutH - 1) / kNetOutH) * B;
     const int grid = (int)std::min<long>(ntiles, c->net_grid);
     C_CUDA(cudaMemsetAsync(c->netbar, 0, sizeof(unsigned int), c->stream));
@@ -2278,8 +2216,7 @@ S2D_API void s2d_cnn_destroy(s2d_cnn* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     void* ptrs[] = {c->master, c->grad, c->m, c->v, c->X0, c->dZ6, c->dZa, c->dZb, c->Y, c->tgt, c->part,
-                    c->lpart, c->idx, c->data, c->amp, c->sumsq, c->cflags, c->X0f, c->F[0], c->F[1], c->netbar,
-                    c->Wimg};
+                    c->lpart, c->idx, c->data, c->amp, c->sumsq, c->cflags, c->X0f, c->F[0], c->F[1], c->netbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int l = 0; l < kLayers; ++l) {
