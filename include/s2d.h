@@ -339,7 +339,8 @@ S2D_API int s2d_cnn_grad_host(s2d_cnn* c, const float* x, const float* target, i
 /* Introspection for tests and debugging.  With keep != 0 the gradient calls
  * that follow keep dL/dz of every hidden layer in buffers of their own (five
  * more activation-sized buffers; keep = 0 frees them).  s2d_cnn_get_tensor
- * copies, as float, a BF16 tensor of the last forward/gradient call for the
+ * copies, as float, a BF16 tensor of the last gradient call (or per-layer
+ * forward: the fused forward keeps no per-layer tensors) for the
  * first `batch` images, layout [batch][grid][grid][channels padded to 16 or
  * 32]: kind 0 = the input activations of `layer` (layer 0: the normalised
  * network input), 1 = its pre-activation z (layers 0-4, after a gradient
