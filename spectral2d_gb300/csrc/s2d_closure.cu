@@ -155,27 +155,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 }
 
 // Implicit-GEMM 3x3 circular convolution on the tcgen05 tensor cores.
-// A CTA (8 warps) owns a tile of 8 x 16 = 128 pixels of one image at a time
-// (persistent: tiles blockIdx.x, + gridDim.x, ...): the GEMM is
-// D[128 pixels, NC] += A_t[128, KC] B_t[KC, NC] over the 9 taps t, with the
-// FP32 accumulator in tensor memory (NC columns of 128 lanes).
-//   A_t: the tile shifted by the tap's offset.  The halo (10 rows x 16
-//        pixels) is loaded by TMA three times, shifted by dx = -1, 0, +1:
-//        one box per copy, a pixel's KC channels (32 or 64 bytes) per box
-//        row, swizzled (32 or 64 B) as the tensor core reads K-major
-//        operands.  A row shift dy is a whole number of 8-pixel atoms, so
-//        every A_t is a descriptor into one of the three copies.  The tensor
-//        map zero-fills what lies outside the image; for tiles at an edge
-//        those positions are rewritten with the circularly wrapped pixels
-//        once the boxes have landed.
-//   B_t: the tap's weights W[n, t, :] (N x K, K-major, no swizzle), staged
-//        once.
-// Thread 0 issues the TMA loads and the 9 * KC/16 MMAs (M=128, N=NC, K=16),
-// commits them to an mbarrier and waits for it (every wait bounded); once the
-// MMAs have read the halo it loads the next tile's boxes into the same slot,
-// so that they fly while this tile's epilogue runs.  The 8 warps read the
-// accumulator for the epilogue, warp w lanes 32 (w % 4) .. + 31 (tcgen05.ld
-// reaches the lane quarter w % 4) and columns 16 (w / 4) .. + 15:
+// A CTA (8 warps) owns an output tile of 8 rows x 14 columns of one image at
+// a time (persistent: tiles blockIdx.x, + gridDim.x, ...).  Its halo, image
+// rows ty0 - 1 .. ty0 + 8 and columns tx0 - 1 .. tx0 + 14, is one TMA box of
+// 10 x 16 pixels, a pixel's KC channels (32 or 64 bytes) per box row,
+// swizzled (32 or 64 B) as the tensor core reads K-major operands.  The
+// three column taps sit side by side in the MMA's N dimension:
+//   D[128 box pixels, (dx, n)] += A_dy[128, KC] B_dy[KC, 3 NC]
+// over the three rows of taps dy and the K steps of 16 channels (3 KC / 16
+// MMAs of N = 3 NC per tile), A_dy being box rows dy .. dy + 7 (a whole
+// number of 8-pixel atoms: a descriptor into the box) and B_dy the weights
+// of row dy, column group (dx, 8 output channels), K-major, no swizzle,
+// staged once.  Output pixel (r, c) of the box (columns 1 .. 14 are the
+// tile's) sums tap dx evaluated at box pixel (r, c + dx - 1): the epilogue
+// adds the three column blocks with shuffles inside the 16 lanes of a box
+// row.  The tensor map zero-fills what lies outside the image; for tiles at
+// an edge those positions are rewritten with the circularly wrapped pixels
+// once the box has landed.
+// Thread 0 issues the TMA load and the MMAs, commits them to an mbarrier and
+// waits for it (every wait bounded); once the MMAs have read the box it
+// loads the next tile's box into the same slot, so that it flies while this
+// tile's epilogue runs.  The 8 warps read the accumulator for the epilogue,
+// warp w lanes 32 (w % 4) .. + 31 (tcgen05.ld reaches the lane quarter
+// w % 4) and, of each column block, channels 16 (w / 4) .. + 15:
 //   EPI 0: + bias, store z (unless z is null: no backward follows) and
 //   gelu(z) (BF16); 1: + bias, channel 0 as FP32;
 //   2: multiply by gelu'(zprev), store BF16.
@@ -184,8 +186,9 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
 // A wait that exceeds its iteration limit sets bit 4 of *err and skips the
 // rest (the kernel waits, bounded, for its loads and MMAs in flight, frees
 // its tensor memory and returns).
-constexpr int kConvTY = 8;
-constexpr int kConvTX = 16;
+constexpr int kConvTY = 8;    // output rows of a tile
+constexpr int kConvTX = 16;   // box width in pixels
+constexpr int kConvOW = 14;   // output columns of a tile (box columns 1 .. 14)
 
 template <int KC, int NC>
 struct ConvTile {
@@ -194,11 +197,14 @@ struct ConvTile {
     static constexpr int CORE = 128;                       // bytes of one no-swizzle core matrix
     static constexpr int ROWB = KC * 2;                    // bytes of one pixel (one swizzled row)
     static constexpr int BOX = HR * kConvTX * ROWB;        // one TMA box: 10 rows x 16 pixels
-    static constexpr int SLOT = 3 * BOX;                   // the three dx copies of one tile
-    static constexpr int WGROUP = KG * CORE;               // weights of 8 output channels, all input channels
-    static constexpr int WBYTES = 9 * (NC / 8) * WGROUP;   // weights of all taps
-    static constexpr size_t SMEM = SLOT + WBYTES + 1024;   // + slack to align the base to 1024 B
+    static constexpr int N = 3 * NC;                       // MMA columns: (dx, output channel)
+    static constexpr int NG = N / 8;                       // 8-column groups
+    static constexpr int WGROUP = KG * CORE;               // weights of 8 columns, all input channels
+    static constexpr int WBYTES = 3 * NG * WGROUP;         // weights of all taps
+    static constexpr int TMEM_COLS = N <= 64 ? 64 : 128;   // power of two >= N
+    static constexpr size_t SMEM = BOX + WBYTES + 1024;    // + slack to align the base to 1024 B
     static_assert(BOX % 1024 == 0, "boxes stay aligned to the swizzle pattern");
+    static_assert(N % 16 == 0 && N <= 256, "M = 128 MMA shape");
 };
 
 constexpr int kConvThreads = 256;
@@ -214,19 +220,20 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
     using TL = ConvTile<KC, NC>;
     constexpr int KG = TL::KG;
     constexpr int ROWB = TL::ROWB;
-    constexpr int TMEM_COLS = 32;   // NC <= 32 FP32 columns; the allocation minimum
+    constexpr int NG = TL::NG;
+    constexpr int TMEM_COLS = TL::TMEM_COLS;
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     const uint32_t sraw = smem_u32(tc_smem);
-    const uint32_t sbase = (sraw + 1023u) & ~1023u;        // the halo slot, then the weights
+    const uint32_t sbase = (sraw + 1023u) & ~1023u;        // the halo box, then the weights
     unsigned char* gbase = tc_smem + (sbase - sraw);
-    const uint32_t bw = sbase + TL::SLOT;
+    const uint32_t bw = sbase + TL::BOX;
     __shared__ __align__(8) uint64_t mbar_mma;
     __shared__ __align__(8) uint64_t mbar_full;
     __shared__ uint32_t tmem_base;
     __shared__ int s_ok;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const int tiles_x = (Wd + kConvTX - 1) / kConvTX;
+    const int tiles_x = (Wd + kConvOW - 1) / kConvOW;
     const int tiles_img = tiles_x * ((H + kConvTY - 1) / kConvTY);
     const int ntiles = tiles_img * B;
 
@@ -244,15 +251,21 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         s_ok = 1;
     }
-    // weights (once per CTA): tap t, output channel n, channels [8 kg, 8 kg + 8)
-    for (int i = tid; i < 9 * NC * KG; i += blockDim.x) {
+    // weights (once per CTA): row of taps dyi, column group g = (dxi, 8
+    // output channels), channels [8 kg, 8 kg + 8).  Block (dyi, dxi) meets
+    // the input at offset (dyi - 1, dxi - 1): tap (dyi, dxi) of W forward,
+    // the mirrored tap of W^T for the data gradient.
+    for (int i = tid; i < 3 * TL::N * KG; i += blockDim.x) {
         const int nl = i % 8;
         const int kg = (i / 8) % KG;
-        const int n = ((i / (8 * KG)) % (NC / 8)) * 8 + nl;
-        const int t = i / (KG * NC);
+        const int g = (i / (8 * KG)) % NG;
+        const int dyi = i / (8 * KG * NG);
+        const int dxi = g / (NC / 8);
+        const int n = (g % (NC / 8)) * 8 + nl;
+        const int t = (SIGN * (dyi - 1) + 1) * 3 + (SIGN * (dxi - 1) + 1);
         const uint4 v = *reinterpret_cast<const uint4*>(W + ((long)n * 9 + t) * KC + kg * 8);
-        const int off = ((t * (NC / 8) + n / 8) * KG + kg) * TL::CORE + (n % 8) * 16;
-        *reinterpret_cast<uint4*>(gbase + TL::SLOT + off) = v;
+        const int off = ((dyi * NG + g) * KG + kg) * TL::CORE + nl * 16;
+        *reinterpret_cast<uint4*>(gbase + TL::BOX + off) = v;
     }
     asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
     asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
@@ -263,33 +276,30 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
     // only, where the weights do not change), the prologue above -- TMEM
     // columns, barriers, the layer's weights -- overlaps the previous kernel;
     // the input activations and the outputs are touched only after this.  A
-    // waiting CTA holds 32 TMEM columns: at most eight CTAs of 256 threads
-    // share an SM (2048 threads), 256 of its 512 columns, so no allocation
-    // waits on a CTA that waits in turn.
+    // CTA waiting for its TMEM columns waits only on CTAs (of this launch or
+    // the one before) that run to completion without waiting on it.
     pdl_enter();
 
     // thread 0's bookkeeping: the parity to wait for on each barrier and what
     // is in flight
     uint32_t ph_mma = 0, ph_full = 0;
     bool pend = false, mma_pend = false;
-    auto issue_loads = [&](int tile) {
+    auto issue_load = [&](int tile) {
         const int b = tile / tiles_img;
         const int tl = tile - b * tiles_img;
-        const int tx0 = (tl % tiles_x) * kConvTX;
+        const int tx0 = (tl % tiles_x) * kConvOW;
         const int ty0 = (tl / tiles_x) * kConvTY;
-        mbar_expect_tx(bar_full, (uint32_t)TL::SLOT);
-#pragma unroll
-        for (int d = 0; d < 3; ++d)
-            tma_load_4d(sbase + d * TL::BOX, &tin, 0, tx0 + d - 1, ty0 - 1, b, bar_full);
+        mbar_expect_tx(bar_full, (uint32_t)TL::BOX);
+        tma_load_4d(sbase, &tin, 0, tx0 - 1, ty0 - 1, b, bar_full);
         pend = true;
     };
-    if (tid == 0 && (int)blockIdx.x < ntiles) issue_loads(blockIdx.x);
+    if (tid == 0 && (int)blockIdx.x < ntiles) issue_load(blockIdx.x);
 
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int b = tile / tiles_img;
         const int tl = tile - b * tiles_img;
-        const int tx0 = (tl % tiles_x) * kConvTX;
+        const int tx0 = (tl % tiles_x) * kConvOW;
         const int ty0 = (tl / tiles_x) * kConvTY;
         const long img = (long)b * H * Wd;
 
@@ -305,20 +315,19 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
         if (!s_ok) break;
 
         // circular wrap at the image edges: rewrite the zero-filled positions
-        if (tx0 == 0 || ty0 == 0 || tx0 + kConvTX >= Wd || ty0 + kConvTY >= H) {
+        // (box columns tx0 - 1 .. tx0 + 14, rows ty0 - 1 .. ty0 + 8)
+        if (tx0 == 0 || ty0 == 0 || tx0 + kConvOW >= Wd || ty0 + kConvTY >= H) {
             // each writer observes the completed phase itself (the k-th load
             // has parity k & 1), so its stores follow the box's fill
             (void)mbar_try_wait(bar_full, (uint32_t)it & 1u);
-            for (int i = tid; i < 3 * TL::HR * kConvTX * KG; i += blockDim.x) {
+            for (int i = tid; i < TL::HR * kConvTX * KG; i += blockDim.x) {
                 const int q = i % KG;   // 16-byte chunk of the pixel
-                int r = i / KG;
+                const int r = i / KG;
                 const int c = r % kConvTX;
-                r /= kConvTX;
-                const int hr = r % TL::HR;
-                const int d = r / TL::HR;
-                int yy = ty0 + hr - 1, xx = tx0 + c + d - 1;
+                const int hr = r / kConvTX;
+                int yy = ty0 + hr - 1, xx = tx0 + c - 1;
                 if (yy >= 0 && yy < H && xx >= 0 && xx < Wd) continue;
-                // yy in [-1, H + 8], xx in [-1, Wd + 16): at most two wraps (grid >= 8)
+                // yy in [-1, H + 8), xx in [-1, Wd + 14): at most two wraps (grid >= 8)
                 yy += yy < 0 ? H : 0;
                 yy -= yy >= H ? H : 0;
                 yy -= yy >= H ? H : 0;
@@ -326,9 +335,8 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
                 xx -= xx >= Wd ? Wd : 0;
                 xx -= xx >= Wd ? Wd : 0;
                 const uint4 v = *reinterpret_cast<const uint4*>(in + (img + (long)yy * Wd + xx) * KC + q * 8);
-                const int row = hr * kConvTX + c;
-                const int pq = ROWB == 64 ? (q ^ ((row >> 1) & 3)) : (q ^ ((row >> 2) & 1));
-                *reinterpret_cast<uint4*>(gbase + d * TL::BOX + row * ROWB + pq * 16) = v;
+                const int pq = ROWB == 64 ? (q ^ ((r >> 1) & 3)) : (q ^ ((r >> 2) & 1));
+                *reinterpret_cast<uint4*>(gbase + r * ROWB + pq * 16) = v;
             }
         }
         // the rewritten positions must be visible to the tensor core (async proxy)
@@ -338,22 +346,20 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
         if (tid == 0) {
-            constexpr uint32_t idesc = umma_idesc_bf16(128, NC);
-            const uint32_t a0 = sbase;
-#pragma unroll 1
-            for (int t = 0; t < 9; ++t) {
-                const int dy = SIGN * (t / 3 - 1), dx = SIGN * (t % 3 - 1);
-                const uint32_t abase = a0 + (dx + 1) * TL::BOX + (1 + dy) * kConvTX * ROWB;
-                const uint32_t bbase = bw + t * (NC / 8) * TL::WGROUP;
+            constexpr uint32_t idesc = umma_idesc_bf16(128, TL::N);
+            const uint64_t ad0 = umma_desc_sw<ROWB>(sbase);
+            const uint64_t bd0 = umma_desc(bw, TL::CORE, TL::WGROUP);
+#pragma unroll
+            for (int dyi = 0; dyi < 3; ++dyi) {
 #pragma unroll
                 for (int j = 0; j < KC / 16; ++j) {
-                    const uint64_t ad = umma_desc_sw<ROWB>(abase + j * 32);   // K step: 16 channels = 32 B
-                    const uint64_t bd = umma_desc(bbase + j * 2 * TL::CORE, TL::CORE, TL::WGROUP);
-                    const uint32_t acc = (t | j) ? 1u : 0u;
+                    // start addresses advance in 16-byte units in the low field
+                    const uint64_t ad = ad0 + (uint64_t)((dyi * kConvTX * ROWB + j * 32) >> 4);
+                    const uint64_t bd = bd0 + (uint64_t)((dyi * NG * TL::WGROUP + j * 2 * TL::CORE) >> 4);
                     asm volatile(
                         "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
                         " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-                        "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                        "l"(ad), "l"(bd), "r"(idesc), "r"((dyi | j) ? 1u : 0u)
                         : "memory");
                 }
             }
@@ -363,9 +369,9 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
             if (mbar_wait_bounded(bar_mma, ph_mma)) {
                 ph_mma ^= 1u;
                 mma_pend = false;
-                // the MMAs have read the slot: the next tile's boxes load
+                // the MMAs have read the box: the next tile's box loads
                 // while this tile's epilogue runs
-                if (tile + (int)gridDim.x < ntiles) issue_loads(tile + gridDim.x);
+                if (tile + (int)gridDim.x < ntiles) issue_load(tile + gridDim.x);
             } else {
                 s_ok = 0;
             }
@@ -374,21 +380,47 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
         if (!s_ok) break;
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
 
-        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (its tile pixels m,
-        // at (m / 16, m % 16)) and columns 16 (w / 4) .. + 15
+        // warp w reads accumulator lanes 32 (w % 4) .. + 31 (box pixels m:
+        // row m / 16, column m % 16) and, of each column block dx, channels
+        // 16 (w / 4) .. + 15; pixel m sums block dx at box pixel m + dx - 1
         const int quarter = warp & 3, half = warp >> 2;
         const bool cols = half * 16 < NC;   // warp-uniform
-        uint32_t r[16];
+        float s[16];
         if (cols) {
-            const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * 16);
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
-                "[%16];\n"
-                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
-                  "=r"(r[15])
-                : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)(half * 16);
+#pragma unroll
+            for (int e = 0; e < 16; ++e) s[e] = 0.0f;
+#pragma unroll
+            for (int dxi = 0; dxi < 3; ++dxi) {
+                if constexpr (EPI == 1) {   // channel 0 only
+                    uint32_t r0;
+                    asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n"
+                                 : "=r"(r0)
+                                 : "r"(trow + (uint32_t)(dxi * NC)));
+                    asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+                    const float v = __uint_as_float(r0);
+                    s[0] += dxi == 0   ? __shfl_up_sync(0xffffffffu, v, 1, kConvTX)
+                            : dxi == 1 ? v
+                                       : __shfl_down_sync(0xffffffffu, v, 1, kConvTX);
+                    continue;
+                }
+                uint32_t r[16];
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];\n"
+                    : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                      "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                      "=r"(r[15])
+                    : "r"(trow + (uint32_t)(dxi * NC)));
+                asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const float v = __uint_as_float(r[e]);
+                    s[e] += dxi == 0   ? __shfl_up_sync(0xffffffffu, v, 1, kConvTX)
+                            : dxi == 1 ? v
+                                       : __shfl_down_sync(0xffffffffu, v, 1, kConvTX);
+                }
+            }
         }
         // the next tile's MMAs may overwrite the accumulator only after every
         // warp has read it
@@ -396,11 +428,12 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
         __syncthreads();
 
         const int m = quarter * 32 + lane;
-        const int y = ty0 + m / kConvTX, x = tx0 + m % kConvTX;
-        if (cols && y < H && x < Wd) {
+        const int c = m % kConvTX;
+        const int y = ty0 + m / kConvTX, x = tx0 - 1 + c;
+        if (cols && c >= 1 && c <= kConvOW && y < H && x < Wd) {
             const long p = img + (long)y * Wd + x;
             if (EPI == 1) {
-                if (half == 0) yout[p] = __uint_as_float(r[0]) + bias[0];
+                if (half == 0) yout[p] = s[0] + bias[0];
             } else {
 #pragma unroll
                 for (int qq = 0; qq < 2; ++qq) {
@@ -412,7 +445,7 @@ __global__ void __launch_bounds__(kConvThreads, 4) k_conv_tc(const __grid_consta
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         const int n = q * 8 + 2 * e;
-                        float v0 = __uint_as_float(r[qq * 8 + 2 * e]), v1 = __uint_as_float(r[qq * 8 + 2 * e + 1]);
+                        float v0 = s[qq * 8 + 2 * e], v1 = s[qq * 8 + 2 * e + 1];
                         if (EPI == 0) {
                             v0 += bias[n];
                             v1 += bias[n + 1];
@@ -481,8 +514,8 @@ cudaError_t conv_tensor_map(CUtensorMap* map, const __nv_bfloat16* act, int B, i
 }
 
 // Launch k_conv_tc over B images of H x Wd: a persistent grid of up to four
-// CTAs of 256 threads per SM (50 KB of shared memory each at KC = 32), each
-// looping over 128-pixel tiles.
+// CTAs of 256 threads per SM (29 KB of shared memory each at KC = 32), each
+// looping over 8 x 14-pixel output tiles.
 template <int KC, int NC, int SIGN, int EPI>
 cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const float* bias,
                         const __nv_bfloat16* zprev, __nv_bfloat16* z, __nv_bfloat16* a, float* yout, int B, int H,
@@ -490,7 +523,7 @@ cudaError_t launch_conv(const __nv_bfloat16* in, const __nv_bfloat16* W, const f
     CUtensorMap map;
     const cudaError_t e = conv_tensor_map<KC>(&map, in, B, H, Wd);
     if (e != cudaSuccess) return e;
-    const long ntiles = (long)((Wd + kConvTX - 1) / kConvTX) * ((H + kConvTY - 1) / kConvTY) * B;
+    const long ntiles = (long)((Wd + kConvOW - 1) / kConvOW) * ((H + kConvTY - 1) / kConvTY) * B;
     const int grid = (int)std::min<long>(ntiles, 4L * sms);
     return launch_k(k_conv_tc<KC, NC, SIGN, EPI>, grid, kConvThreads, ConvTile<KC, NC>::SMEM, st, pdl, map, in, W,
                     bias, zprev, z, a, yout, B, H, Wd, err);
